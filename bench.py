@@ -1,0 +1,378 @@
+#!/usr/bin/env python3
+"""bench.py -- BDF steps/s of foeuler's implicit inner loop on one GB300.
+
+Workload (default, 5,308,416 tets): unit cube of 96^3 hexahedra x 6 Kuhn tetrahedra
+with seeded +-0.1h interior-node jitter, sinusoidal density/velocity state, p = 1,
+slip walls, BDF2 at dt = 5e-4, Newton tolerance 1e-8, GMRES(30) + block ILU(0).
+A "step" is one BDF step of the whole mesh (residuals, Jacobian assembly, ILU(0)
+factor and apply, Krylov iterations) with the state resident in HBM.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One JSON line on rank 0.  `value` is device-resident throughput (CUDA events on the
+library's stream); `e2e` is the same metric through the host-buffer C-ABI entry
+point fos_bdf_run_host with the state copied host->device and back every step;
+`roofline` covers the operation with the largest share of the step, timed with CUDA
+events over repeated launches; `cpu_baseline` times the CPU oracle (a C restatement
+of the reference arithmetic) on this machine's host cores on a bounded sample.
+N > 1 runs independent replicas (the path is not partitioned across GPUs here).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "BDF steps/s at 5.3M tets, 1 GB300: FP32+learned FGMRES vs FP64 ILU, tol 1e-8"
+UNIT = "BDF steps/s"
+FULL_CELLS = 96 ** 3 * 6
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="sine96")
+    ap.add_argument("--scale", type=int, default=None, help="hexes along x (small cases)")
+    ap.add_argument("--mode", choices=["fp64", "fp32"], default="fp64",
+                    help="fp64: FP64 flux + FP64 ILU(0); fp32: FP32 flux + FP32 ILU(0) apply")
+    ap.add_argument("--precond", choices=["ilu", "none"], default="ilu")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-oracle baseline")
+    ap.add_argument("--no-ops", action="store_true", help="skip the per-operation timing")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--op-reps", type=int, default=5)
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ clocks
+class Clocks:
+    """nvidia-smi sampler during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev_index: int):
+        self.dev = dev_index
+        self.proc = None
+        self.path = Path(f"/tmp/fos_clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.dev)], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        self.path.unlink(missing_ok=True)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ distributed
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def allmax(pg, x: float, device=None) -> float:
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ CPU oracle baseline
+def cpu_oracle_sample(workload: str, steps: int, warmup: int, sample_scale: int = 32):
+    """The oracle (C restatement of the reference arithmetic, OpenMP on all host cores,
+    atomic-scatter pair loop like Euler.f90:84-154) running fixed-step BDF on a
+    sample of the same workload; BDF steps/s scaled to the full cell count."""
+    from fosolvers_gb300 import mesh as M
+    from fosolvers_gb300.euler import PolyFvGrid
+    from oracle import pyoracle as O
+    threads = os.cpu_count() or 1
+    wl = M.make_workload(workload, scale=sample_scale)
+    grid = PolyFvGrid.from_mesh(wl.mesh)
+    ibc = M.ibc_for(wl.mesh, wl.bc_gid)
+    e = O.Euler(grid.__dict__, ibc, wl.bc_type, wl.bc_param, wl.gamm, wl.r, wl.elem_state,
+                threads=threads)
+    y = M.soa(wl.elem_state, grid.nC)
+    rhs, pset, psol = e.callbacks()
+    if warmup:
+        yw = y.copy()
+        O.bdf_run(5 * grid.nC, rhs, pset, psol, e.h, yw,
+                  O.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=warmup))
+    t0 = time.perf_counter()
+    rc, st = O.bdf_run(5 * grid.nC, rhs, pset, psol, e.h, y,
+                       O.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=steps))
+    dt = time.perf_counter() - t0
+    # residual evaluations/s on the same sample
+    f = np.zeros_like(y)
+    t1 = time.perf_counter()
+    nrep = 5
+    for _ in range(nrep):
+        e.rhs(0.0, y, f)
+    trhs = (time.perf_counter() - t1) / nrep
+    e.close()
+    full = FULL_CELLS if workload == "sine96" else None
+    scale = (full / grid.nC) if full else 1.0
+    per_step = dt / max(st["n_steps"], 1)
+    return {
+        "value": 1.0 / (per_step * scale), "unit": UNIT, "cores": threads, "kind": "port",
+        "sample": (f"{st['n_steps']} BDF steps of the same workload at {sample_scale}^3 x 6 = "
+                   f"{grid.nC} tets ({per_step:.3f} s/step, {st['n_newton']} Newton, "
+                   f"{st['n_lin_iters']} Krylov iterations), scaled by the cell ratio "
+                   f"{scale:.1f} to {full or grid.nC} tets; OpenMP only in the residual loops "
+                   f"as in the reference, ILU(0)/Krylov serial"),
+        "residual_evals_per_s_sample": 1.0 / trhs, "rc": rc,
+    }
+
+
+def run_reference(args, world, rank, pg):
+    if rank != 0:
+        return
+    cb = cpu_oracle_sample(args.workload, args.steps, args.warmup)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / cb["value"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded mesh and state)",
+        "config": {"workload": workload_desc(args.workload), "runner": "CPU oracle (reference "
+                   "arithmetic restated in C; the Fortran reference cannot be compiled here)"},
+        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_desc(name: str) -> str:
+    return {
+        "sine96": "unit cube 96^3 hexes x 6 = 5,308,416 tets, +-0.1h node jitter (seed 0), "
+                  "sinusoidal rho/u state, p = 1, slip walls, BDF2 dt = 5e-4, Newton rtol 1e-8, "
+                  "GMRES(30) forcing 1e-3",
+        "sod16": "unit cube 16^3 x 6 = 24,576 tets, Sod, walls, BDF1 dt = 1e-3",
+        "bump192": "bump channel 192x64x32 x 6 = 2,359,296 tets, Mach 2 inflow, BDF1 CFL~5",
+        "bump320": "bump channel 320x107x53 x 6 = 10,888,320 tets, Mach 2 inflow, BDF2 CFL~5",
+    }.get(name, name)
+
+
+# ------------------------------------------------------------------ GPU arm
+def main():
+    args = parse()
+    world, rank, local, pg = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank, pg)
+        if pg is not None:
+            pg.barrier()
+        return
+    import torch
+    from __graft_entry__ import build
+    build()
+    from fosolvers_gb300 import mesh as M
+    from fosolvers_gb300.euler import FLUX_FP32, ILU_FP32, FOEuler, PolyFvGrid
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    t_setup = time.perf_counter()
+    wl = M.make_workload(args.workload, scale=args.scale)
+    grid = PolyFvGrid.from_mesh(wl.mesh)
+    ibc = M.ibc_for(wl.mesh, wl.bc_gid)
+    flags = (FLUX_FP32 | ILU_FP32) if args.mode == "fp32" else 0
+    stream = torch.cuda.current_stream(dev)
+    ctx = FOEuler(grid, ibc, wl.bc_type, wl.bc_param, wl.gamm, wl.r, flags=flags, stream=stream)
+    nC, nF = grid.nC, grid.nP
+    N = 5 * nC
+    y0_host = M.soa(wl.elem_state, nC)
+    y0_ref = torch.from_numpy(y0_host).to(dev)
+    y0 = torch.empty_like(y0_ref)
+    ctx.to_internal(y0_ref, y0)
+    precond = 1 if args.precond == "ilu" else 0
+    mk = lambda n, **kw: ctx.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=n, precond=precond, **kw)
+    setup_s = time.perf_counter() - t_setup
+
+    # warm-up (also builds the block sparsity, level sets and the driver workspace)
+    y = y0.clone()
+    rc, _ = ctx.bdf_run(y, mk(args.warmup))
+    assert rc == 0, f"warm-up failed: {rc}"
+    torch.cuda.synchronize(dev)
+
+    # timed region: K BDF steps from the initial state (inputs > L2: state 0.2 GB, factors 5 GB)
+    y = y0.clone()
+    clocks = Clocks(local)
+    if pg is not None:
+        pg.barrier()
+    torch.cuda.synchronize(dev)
+    launches0 = ctx.info()["launches"]
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    rc, st = ctx.bdf_run(y, mk(args.steps))
+    ev1.record(stream)
+    torch.cuda.synchronize(dev)
+    clk = clocks.stop()
+    if pg is not None:
+        pg.barrier()
+    assert rc == 0, f"timed run failed: {rc} {st}"
+    launches = ctx.info()["launches"] - launches0
+    ms = ev0.elapsed_time(ev1)
+    ms_max = allmax(pg, ms, dev)
+    value = world * args.steps / (ms_max / 1000.0)
+
+    # end to end: host buffer in the caller's cell order, copied in and out every step
+    e2e = None
+    if not args.no_e2e:
+        yh = torch.from_numpy(y0_host.copy()).pin_memory()
+        yhn = yh.numpy()
+        ctx.bdf_run_host(yhn, mk(1))  # warm
+        yhn[:] = y0_host
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            rc_e, _ = ctx.bdf_run_host(yhn, mk(1, resume=1 if k else 0))
+            assert rc_e == 0
+        e2e_s = allmax(pg, time.perf_counter() - t0, dev)
+        e2e = {"value": world * args.steps / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": 8 * N, "d2h_bytes_per_step": 8 * N}
+
+    # per-operation timing (CUDA events on the library stream)
+    ops = {}
+    if not args.no_ops:
+        import math
+        f = torch.empty_like(y)
+        v = torch.randn(N, dtype=torch.float64, device=dev)
+        out = torch.empty_like(y)
+        ynorm = float(torch.linalg.norm(y))
+        gamma = wl.dt * (2.0 / 3.0 if wl.order == 2 else 1.0)
+        info = ctx.info()
+        nnzb = info["nnzb"]
+        fb = 4 if args.mode == "fp32" else 8
+
+        def timeit(fn, reps):
+            fn()
+            torch.cuda.synchronize(dev)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(reps):
+                fn()
+            b.record(stream)
+            torch.cuda.synchronize(dev)
+            return a.elapsed_time(b) / reps
+
+        R = args.op_reps
+        t_rhs = timeit(lambda: ctx.rhs_dev(0.0, y, f), 3 * R)
+        t_jv = timeit(lambda: ctx.jv_dev(0.0, y, f, v, out, 1.0, -gamma, ynorm), 3 * R)
+        t_pset = timeit(lambda: ctx.pset_dev(0.0, y, 0, gamma), max(2, R // 2))
+        t_psol = timeit(lambda: ctx.psol_dev(v, out), R)
+        lev = info["nlev_fwd"] + info["nlev_bwd"]
+        a_, f_ = nC, nF
+        ops = {
+            "residual": {"ms": t_rhs, "bytes": 88 * a_ + 40 * f_, "count": st["n_rhs"] - st["n_jv"]},
+            "jv": {"ms": t_jv, "bytes": 168 * a_ + 40 * f_, "count": st["n_jv"]},
+            "ilu_apply": {"ms": t_psol, "bytes": 25 * fb * nnzb + 80 * a_, "count": st["n_psol"],
+                          "levels": lev},
+            "pset": {"ms": t_pset, "bytes": 88 * a_ + 40 * f_ + 600 * nnzb, "count": st["n_pset"]},
+        }
+        for k, o in ops.items():
+            o["GBps"] = o["bytes"] / (o["ms"] * 1e-3) / 1e9
+            o["ms_per_step"] = o["ms"] * o["count"] / args.steps
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    roof = None
+    if ops:
+        dom = max(ops, key=lambda k: ops[k]["ms_per_step"])
+        o = ops[dom]
+        roof = {"bound": "hbm", "achieved": round(o["GBps"], 1), "peak": hbm, "unit": "GB/s",
+                "frac": round(o["GBps"] / hbm, 4), "traffic": None, "op": dom,
+                "peak_source": "measured" if peaks else "fallback",
+                "per_op": {k: {"ms": round(v["ms"], 4), "GBps": round(v["GBps"], 1),
+                               "frac": round(v["GBps"] / hbm, 4), "per_step": v["count"] / args.steps,
+                               "ms_per_step": round(v["ms_per_step"], 3)}
+                           for k, v in ops.items()}}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        try:
+            cb = cpu_oracle_sample(args.workload, 2, 0)
+            cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+            cpu["residual_evals_per_s_sample"] = cb["residual_evals_per_s_sample"]
+        except Exception as exc:  # the baseline never blocks the GPU line
+            cpu = {"value": None, "error": repr(exc)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.mode == "fp64" else "f32 flux/ILU, f64 Newton+Krylov",
+            "data": "synthetic (seeded mesh and state)",
+            "config": {"workload": workload_desc(args.workload) if args.scale is None else
+                       f"{args.workload} at scale {args.scale}",
+                       "cells": nC, "faces": nF, "mode": args.mode, "precond": args.precond,
+                       "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
+                       "l2": "inputs larger than L2 (state 0.2 GB, ILU factors ~5 GB); no flush",
+                       "setup_s": round(setup_s, 2)},
+            "clocks": clk, "e2e": e2e, "gpu_launches": launches,
+            "roofline": roof, "cpu_baseline": cpu,
+            "stats": {k: st[k] for k in ("n_rhs", "n_jv", "n_psol", "n_pset", "n_newton",
+                                          "n_lin_iters", "n_steps")},
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if pg is not None:
+        pg.barrier()
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

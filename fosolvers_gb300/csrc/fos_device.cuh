@@ -1,0 +1,92 @@
+// fos_device.cuh -- device helpers shared by the residual and Jacobian kernels.
+#pragma once
+#include "fos_internal.h"
+
+// Ghost conserved state of a boundary face (foeuler.f90:209-330); U = interior
+// conserved (rho, mx, my, mz, E), n = unit normal out of the interior cell.
+static __device__ __noinline__ void ghost_state(int type, const double* __restrict__ bp, const double U[5],
+                            double nx, double ny, double nz, double g, double r, double G[5]) {
+  const double gm1 = g - 1.0;
+  switch (type) {
+    case FOS_BC_IN_STATIC: {
+      double pG = bp[0], TG = bp[1], u0 = bp[2], u1 = bp[3], u2 = bp[4];
+      double Mach = sqrt(u0 * u0 + u1 * u1 + u2 * u2) / sqrt(g * r * TG);
+      double rG = pG / r / TG;
+      if (Mach < 1.0) { u0 = U[1] / rG; u1 = U[2] / rG; u2 = U[3] / rG; }
+      G[0] = rG; G[1] = rG * u0; G[2] = rG * u1; G[3] = rG * u2;
+      G[4] = rG * (1.0 / gm1 * r * TG + 0.5 * (u0 * u0 + u1 * u1 + u2 * u2));
+      return;
+    }
+    case FOS_BC_IN_TOTAL: {
+      double ptG = bp[0], TtG = bp[1], u0 = bp[2], u1 = bp[3], u2 = bp[4];
+      double q2 = u0 * u0 + u1 * u1 + u2 * u2;
+      double TG = TtG - 0.5 * gm1 / g / r * q2;
+      double Mach = sqrt(q2) / sqrt(g * r * TG);
+      double pG = ptG * pow(1.0 + 0.5 * gm1 * Mach * Mach, -g / gm1);
+      double rG = pG / r / TG;
+      if (Mach < 1.0) {
+        double ui0 = U[1] / U[0], ui1 = U[2] / U[0], ui2 = U[3] / U[0];
+        double sc = (ui0 * u0 + ui1 * u1 + ui2 * u2) / q2;
+        u0 *= sc; u1 *= sc; u2 *= sc;
+        q2 = u0 * u0 + u1 * u1 + u2 * u2;
+        TG = TtG - 0.5 * gm1 / g / r * q2;
+        Mach = sqrt(q2) / sqrt(g * r * TG);
+        pG = ptG * pow(1.0 + 0.5 * gm1 * Mach * Mach, -g / gm1);
+        rG = pG / r / TG;
+      }
+      G[0] = rG; G[1] = rG * u0; G[2] = rG * u1; G[3] = rG * u2;
+      G[4] = rG * (1.0 / gm1 * r * TG + 0.5 * q2);
+      return;
+    }
+    case FOS_BC_OUT: {
+      G[0] = U[0]; G[1] = U[1]; G[2] = U[2]; G[3] = U[3];
+      G[4] = 1.0 / gm1 * bp[0] + 0.5 * (U[1] * U[1] + U[2] * U[2] + U[3] * U[3]) / U[0];
+      return;
+    }
+    case FOS_BC_OUT_EXTRAP: {
+      for (int q = 0; q < 5; q++) G[q] = U[q];
+      return;
+    }
+    case FOS_BC_FAR: {
+      double pG = bp[0], TG = bp[1], g0 = bp[2], g1 = bp[3], g2 = bp[4];
+      double rm = U[0], Em = U[4];
+      double charO = (g0 * nx + g1 * ny + g2 * nz) - 2.0 * sqrt(g * r * TG) / gm1;
+      double ui0 = U[1] / rm, ui1 = U[2] / rm, ui2 = U[3] / rm;
+      double uu = ui0 * ui0 + ui1 * ui1 + ui2 * ui2;
+      double charI = (ui0 * nx + ui1 * ny + ui2 * nz) + 2.0 * sqrt(g / rm / gm1 * (Em - 0.5 * uu * rm));
+      double un0 = 0.5 * nx * (charI + charO), un1 = 0.5 * ny * (charI + charO),
+             un2 = 0.5 * nz * (charI + charO);
+      double a = 0.25 * gm1 * (charI - charO);
+      double ut0, ut1, ut2, ptG, Mach;
+      if (un0 * nx + un1 * ny + un2 * nz > 0.0) {
+        double sN = nx * ui0 + ny * ui1 + nz * ui2;
+        ut0 = ui0 - nx * sN; ut1 = ui1 - ny * sN; ut2 = ui2 - nz * sN;
+        Mach = sqrt(uu) / sqrt(g / rm * gm1 * (Em - 0.5 * uu * rm));
+        ptG = gm1 * (Em - 0.5 * uu * rm) * pow(1.0 + 0.5 * gm1 * Mach * Mach, g / gm1);
+      } else {
+        ut0 = g0 - un0; ut1 = g1 - un1; ut2 = g2 - un2;
+        Mach = sqrt(g0 * g0 + g1 * g1 + g2 * g2) / sqrt(g * r * TG);
+        ptG = pG * pow(1.0 + 0.5 * gm1 * Mach * Mach, g / gm1);
+      }
+      double u0 = un0 + ut0, u1 = un1 + ut1, u2 = un2 + ut2;
+      double q2 = u0 * u0 + u1 * u1 + u2 * u2;
+      TG = a * a / g / r;
+      Mach = sqrt(q2) / a;
+      pG = ptG * pow(1.0 + 0.5 * gm1 * Mach * Mach, -g / gm1);
+      double rG = pG / r / TG;
+      G[0] = rG; G[1] = rG * u0; G[2] = rG * u1; G[3] = rG * u2;
+      G[4] = rG * (1.0 / gm1 * r * TG + 0.5 * q2);
+      return;
+    }
+    default: {  // FOS_BC_WALL: mirror the momentum (foeuler.f90:217-228)
+      double dn = U[1] * nx + U[2] * ny + U[3] * nz;
+      G[0] = U[0];
+      G[1] = U[1] - 2.0 * dn * nx;
+      G[2] = U[2] - 2.0 * dn * ny;
+      G[3] = U[3] - 2.0 * dn * nz;
+      G[4] = U[4];
+      return;
+    }
+  }
+}
+

@@ -1,0 +1,123 @@
+// fos_internal.h -- private declarations shared by the libfosgpu translation units.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/fosgpu.h"
+
+#include <cuda_runtime.h>
+
+void fos_set_error(const std::string& msg);
+
+#define FOS_CUDA(call)                                                                   \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess) {                                                             \
+      fos_set_error(std::string(#call) + ": " + cudaGetErrorString(e_));                 \
+      return -100;                                                                       \
+    }                                                                                    \
+  } while (0)
+#define FOS_LAUNCH_CHECK()                                                               \
+  do {                                                                                   \
+    cudaError_t e_ = cudaGetLastError();                                                 \
+    if (e_ != cudaSuccess) {                                                             \
+      fos_set_error(std::string("kernel launch: ") + cudaGetErrorString(e_));            \
+      return -101;                                                                       \
+    }                                                                                    \
+  } while (0)
+
+// fixed grid size of the deterministic two-stage reductions (independent of the device)
+constexpr int kRedBlocks = 608;  // 4 x 152 SMs
+constexpr int kRedThreads = 256;
+
+struct fos_bdf_work;
+void fos_bdf_work_free(fos_bdf_work* w);
+
+struct fos_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int nC = 0, nE = 0, nPi = 0, nPb = 0, nP = 0, flags = 0;
+  int nFi = 0, nFb = 0, nF = 0;  // internal faces: interior first, boundary after
+  double gamm = 1.4, r = 1.0;
+  int nBC = 0, maxP = 0;
+  long bandwidth = 0;
+  std::vector<int> old2new, new2old;
+  std::vector<int> h_faceL, h_faceR;  // interior faces (internal ids)
+
+  // ---- device grid
+  int* d_old2new = nullptr;
+  int* d_new2old = nullptr;
+  int2* d_faceLR = nullptr;   // [nF] (L, R) internal ids; boundary faces: (L, bc row)
+  double2* d_faceNA = nullptr;  // [2*nF] (nx, ny), (nz, aP)
+  float4* d_faceNA32 = nullptr; // [nF]  (nx, ny, nz, aP) for the FP32 flux
+  int* d_crow = nullptr;      // [nC+1] cell -> face entries
+  int* d_cent = nullptr;      // (face << 1) | (cell is R)
+  double* d_invV = nullptr;   // [nC]
+  int* d_bcT = nullptr;       // [nBC]
+  double* d_bcP = nullptr;    // [maxP*nBC]
+
+  // ---- device work
+  double* d_W = nullptr;      // [8*nC] primitive AoS (rho,u,v,w,H,p,sqrt(rho),0)
+  float* d_W32 = nullptr;     // [8*nC]
+  double* d_F = nullptr;      // [5*nF] face flows (FP64 path)
+  double* d_stage = nullptr;  // [5*nC] reference-order staging
+  double* d_y = nullptr;      // [5*nC] internal-order callback buffers
+  double* d_f = nullptr;
+  double* d_z = nullptr;
+  double* d_red = nullptr;    // [kRedBlocks * 64] reduction partials
+  double* d_scal = nullptr;   // [256] device scalars
+  int* d_flag = nullptr;      // non-finite flag
+  double* h_scal = nullptr;   // pinned [256]
+
+  // ---- Jacobian (block CSR, internal order) and ILU(0)
+  long nnzb = 0;
+  std::vector<int> h_rowptr, h_col;
+  int* d_rowptr = nullptr;    // [nC+1]
+  int* d_col = nullptr;       // [nnzb]
+  int* d_diag = nullptr;      // [nC] slot of the diagonal block
+  int* d_fslot = nullptr;     // [2*nFi] slots of blocks (L,R) and (R,L) per interior face
+  double* d_J = nullptr;      // [25*nnzb] unscaled Jacobian blocks
+  double* d_Jb = nullptr;     // [25*nFb] boundary-face diagonal terms
+  int* d_ierr = nullptr;
+  bool has_jac = false;
+  double* d_LU = nullptr;     // [25*nnzb] factors (FP64), diag blocks hold the inverse
+  float* d_LU32 = nullptr;    // [25*nnzb] FP32 copy for the FP32 apply
+  // ILU ordering (may differ from the residual ordering)
+  int ilu_nlev_f = 0, ilu_nlev_b = 0;
+  std::vector<int> lev_f, lev_b;    // host level pointers into the level-ordered rows
+  int* d_lrows_f = nullptr;         // rows in forward level order
+  int* d_lrows_b = nullptr;         // rows in backward level order
+  // factor update lists: for row i, k in lower(i): triples (slot_ik, slot_kj, slot_ij)
+  int* d_upd_ptr = nullptr;   // [nC+1] per row
+  int3* d_upd = nullptr;      // updates
+  int ilu_ierr = 0;
+  double* d_ilu_tmp = nullptr;  // [5*nC]
+  fos_bdf_work* bdf = nullptr;  // driver workspace, kept between calls
+  long n_launch = 0;            // kernels launched through fos_launch
+
+  ~fos_ctx();
+};
+
+// every kernel of the library is launched through this (counts launches per context)
+#ifdef __CUDACC__
+template <typename... KArgs, typename... Args>
+inline void fos_launch(fos_ctx* c, void (*k)(KArgs...), dim3 g, dim3 b, Args... args) {
+  c->n_launch++;
+  k<<<g, b, 0, c->stream>>>(args...);
+}
+#endif
+
+// kernels / helpers implemented in fos_residual.cu
+int fos_residual_launch(fos_ctx* c, const double* y, const double* v, const double* d_s,
+                        const double* fy, double* out, double a, double b, int mode);
+int fos_norm2_dev(fos_ctx* c, const double* x, long n, double* d_out_sq);
+int fos_permute(fos_ctx* c, const double* in, double* out, int dir);
+int fos_jv_sigma(fos_ctx* c, double* d_scal, double ynorm, double eps);
+int fos_prim_launch(fos_ctx* c, const double* y);
+// fos_jacobian.cu
+int fos_jac_setup(fos_ctx* c);
+int fos_jac_assemble(fos_ctx* c, const double* y);
+int fos_ilu_factor(fos_ctx* c, double gamma);
+int fos_ilu_apply(fos_ctx* c, const double* r, double* z);

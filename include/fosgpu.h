@@ -1,0 +1,166 @@
+/*
+ * fosgpu.h -- C ABI of libfosgpu.so, the GB300 implementation of foeuler's
+ * implicit inner loop (mianzhi/fosolvers).
+ *
+ * All entry points are extern "C" with plain pointers and sizes.  Host-pointer
+ * entry points (fos_euler_rhs/pset/psol) are the drop-in replacements for the
+ * three CVODE user callbacks of src/foeuler/foeuler.f90; *_dev entry points
+ * take device pointers and run on the context's CUDA stream; fos_bdf_run is the
+ * device-resident fixed-step BDF Newton--Krylov driver.
+ *
+ * Vector layout (every y / ydot / r / z argument): SoA by conserved variable,
+ * [rho(1:nC), rhou(1:nC), rhov(1:nC), rhow(1:nC), rhoE(1:nC)], length 5*nC,
+ * exactly the N_Vector layout of foeuler.f90:161-170.  Host-pointer entry
+ * points take vectors in the caller's (reference) cell order; *_dev entry
+ * points take vectors in the library's internal (renumbered) cell order, see
+ * fos_ctx_permute_dev.
+ *
+ * Return codes follow the CVODE callback convention: 0 = success, > 0 =
+ * recoverable failure (non-finite residual, zero pivot), < 0 = unrecoverable
+ * (bad argument, CUDA error).  fos_last_error() describes the last failure.
+ */
+#ifndef FOSGPU_H
+#define FOSGPU_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fos_ctx fos_ctx;
+
+/* Boundary condition codes (foeuler.f90:17-25).  FOS_BC_OUT_EXTRAP has no
+ * reference counterpart: zero-gradient (supersonic) outflow, ghost = interior. */
+enum {
+  FOS_BC_WALL = 0,
+  FOS_BC_IN_STATIC = 10,
+  FOS_BC_IN_TOTAL = 11,
+  FOS_BC_OUT = 20,
+  FOS_BC_OUT_EXTRAP = 21,
+  FOS_BC_FAR = 30
+};
+
+/* Precision of the Roe flux / preconditioner (flags of fos_ctx_create) */
+enum {
+  FOS_FLUX_FP64 = 0,   /* reference arithmetic, FP64 throughout */
+  FOS_FLUX_FP32 = 1,   /* FP32 flux, FP64 accumulation and FD perturbation */
+  FOS_ORDER_RCM = 0,   /* reverse Cuthill--McKee renumbering (default) */
+  FOS_ORDER_NATURAL = 2,
+  FOS_ILU_FP32 = 4,    /* ILU(0) factors and apply in FP32 */
+  FOS_ILU_COLOR = 8    /* ILU(0) on a multicolour ordering (few levels) */
+};
+
+/* ------------------------------------------------------------------ setup */
+
+/* Grid face arrays from element connectivity: the result of polyGrid%up and
+ * polyFvGrid%up (polyGrid.f90:64-136, polyFvGrid.f90:48-227).  Elements are
+ * TET (20) / HEX (21) cells and TRI (10) / QUAD (11) facets, iNE is m x nE
+ * column-major with 1-based node ids.  Pairs come out in the reference order
+ * (built per cell face, then ordered by max(iEP) with the same quicksort).
+ * Returns an opaque handle; read it with fos_grid_sizes / fos_grid_copy. */
+typedef struct fos_grid fos_grid;
+int fos_grid_build(fos_grid** out, int nN, const double* pN, int nE, int m, const int* sE,
+                   const int* nNE, const int* iNE, const int* gid);
+/* out[0..6] = nC, nE, nP, nPi, nPb, maxFace, nF */
+void fos_grid_sizes(const fos_grid* g, int* out);
+/* iEP 2*nP (1-based), aP nP, normP 3*nP, pP 3*nP, v nC, neib maxFace*nC,
+ * gid nE, p 3*nE (centroids), sE nE -- all in reference (sorted) element order.
+ * Any output may be NULL. */
+void fos_grid_copy(const fos_grid* g, int* iEP, double* aP, double* normP, double* pP,
+                   double* v, int* neib, int* gid, double* p, int* sE);
+void fos_grid_free(fos_grid* g);
+
+/* Create a solver context from the face arrays of a polyFvGrid (the module
+ * state that foeuler's init() builds, foeuler.f90:60-175).
+ *   iEP      2*nP pair element ids (index_base 0 or 1), interior pairs first
+ *   aP, normP, v  pair area, unit normal (3*nP), cell volume
+ *   iBC      nE: row of the condition table per element (1-based, 0 = default wall)
+ *   bcType   nBC condition codes, bcParam maxP*nBC (column-major, bc%p)
+ *   flags    FOS_FLUX_*, FOS_ORDER_*, FOS_ILU_* bits
+ * Uploads the grid to the current CUDA device.  Returns 0 or < 0. */
+int fos_ctx_create(fos_ctx** out, int nC, int nE, int nPi, int nPb, const int* iEP,
+                   const double* aP, const double* normP, const double* v, const int* iBC,
+                   int nBC, const int* bcType, const double* bcParam, int maxP, double gamm,
+                   double r, int index_base, int flags);
+void fos_ctx_destroy(fos_ctx* ctx);
+/* CUDA stream (cudaStream_t as void*) for all subsequent launches; NULL = legacy default */
+int fos_ctx_set_stream(fos_ctx* ctx, void* stream);
+/* out[0..8] = nC, nPi, nPb, nlev_fwd, nlev_bwd, nnzb, bandwidth, flags,
+ * number of kernels launched so far on this context */
+void fos_ctx_info(const fos_ctx* ctx, long* out);
+/* reference<->internal order on the device: dir 0 = reference -> internal, 1 = back */
+int fos_ctx_permute_dev(fos_ctx* ctx, const double* in, double* out, int dir);
+/* internal cell id of every reference cell (old2new, 0-based), length nC */
+int fos_ctx_renumbering(const fos_ctx* ctx, int* old2new);
+const char* fos_last_error(void);
+
+/* ------------------------------------------------------------------ CVODE callbacks (host) */
+
+/* rhs: dy/dt = -(sum of Roe face fluxes)/v with BC ghosts (foeuler.f90:349-375) */
+int fos_euler_rhs(double t, const double* y, double* ydot, void* user_data);
+/* pset: on jok == 0 assemble the Roe Jacobian (Euler.f90:159-333) and set *jcur = 1;
+ * form P = I - gamma diag(1/v) J and factor it with block ILU(0)
+ * (stub in the reference, foeuler.f90:378-405) */
+int fos_euler_pset(double t, const double* y, const double* fy, int jok, int* jcur,
+                   double gamma, void* user_data);
+/* psol: z = P^{-1} r by the ILU(0) triangular solves (stub z = r in the reference,
+ * foeuler.f90:408-437; SPARSKIT lusol, ilut.f:2272-2320) */
+int fos_euler_psol(double t, const double* y, const double* fy, const double* r, double* z,
+                   double gamma, double delta, int lr, void* user_data);
+
+/* ------------------------------------------------------------------ device entry points */
+
+int fos_euler_rhs_dev(fos_ctx* ctx, double t, const double* y, double* ydot);
+/* Fused finite-difference Jacobian-vector product of G(y) = y - gamma f(y) - h:
+ *   out = a*v + b*(f(y + s v) - fy)/s,  s = eps (1 + ||y||_2)/||v||_2
+ * (the difference quotient CVODE's SPGMR forms through rhs); ynorm = ||y||_2.
+ * a = 1, b = -gamma gives J_G v; a = 0, b = 1 gives J_f v. */
+int fos_euler_jv_dev(fos_ctx* ctx, double t, const double* y, const double* fy, const double* v,
+                     double* out, double a, double b, double ynorm, double eps);
+int fos_euler_pset_dev(fos_ctx* ctx, double t, const double* y, int jok, int* jcur,
+                       double gamma);
+int fos_euler_psol_dev(fos_ctx* ctx, const double* r, double* z);
+/* Block Jacobian J (5x5 blocks, before scaling by -gamma/v): copies out the
+ * block-CSR in internal order.  rowptr nC+1, col nnzb, val 25*nnzb (row-major
+ * blocks).  Pass NULL to query nnzb through the return value. */
+long fos_euler_jac_copy(fos_ctx* ctx, int* rowptr, int* col, double* val);
+
+/* ------------------------------------------------------------------ driver */
+
+typedef struct {
+  int order;          /* 1 = BDF1; 2 = BDF2 (first step BDF1) */
+  int nsteps;
+  double dt;
+  double newton_rtol; /* Newton: ||G(y)||_WRMS <= 1 with w = 1/(rtol |y_n| + atol) */
+  double newton_atol;
+  int max_newton;
+  int maxl;           /* (F)GMRES restart length */
+  int max_restarts;
+  double lin_rtol;    /* Krylov: ||r|| <= lin_rtol ||b|| */
+  double jv_eps;      /* finite-difference increment scale (sqrt of machine epsilon) */
+  int precond;        /* 0 = none, 1 = block ILU(0), 2 = learned (GNN) with ILU(0) fallback */
+  int jac_reuse;      /* 0 = assemble J every BDF step (jok = 0), 1 = keep J from the first step */
+  int resume;         /* 1 = continue the BDF history of the previous call (y must be its result) */
+} fos_bdf_opts;
+
+typedef struct {
+  long n_rhs, n_jv, n_psol, n_pset, n_newton, n_lin_iters, n_steps, fails, n_fallback;
+  double last_gnorm;
+  double t;
+} fos_bdf_stats;
+
+void fos_bdf_defaults(fos_bdf_opts* o);
+/* Advance y (device, internal order, 5*nC) by opts->nsteps fixed BDF steps from t0.
+ * Returns 0, > 0 if a step failed to converge (1), hit a non-finite residual (2) or a
+ * zero pivot (3); < 0 on errors. */
+int fos_bdf_run(fos_ctx* ctx, double t0, double* y, const fos_bdf_opts* opts,
+                fos_bdf_stats* stats);
+/* Same with y a HOST array in the caller's (reference) cell order: copied to the device,
+ * advanced, and copied back (the N_Vector-level entry point). */
+int fos_bdf_run_host(fos_ctx* ctx, double t0, double* y, const fos_bdf_opts* opts,
+                     fos_bdf_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

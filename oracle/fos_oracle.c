@@ -1,0 +1,1287 @@
+/*
+ * fos_oracle.c -- CPU oracle for the foeuler implicit inner loop.
+ *
+ * TEST INFRASTRUCTURE ONLY (see fos_oracle.h).  A plain-C restatement of the
+ * reference arithmetic; every function cites the reference file:line it
+ * follows (paths relative to the mianzhi/fosolvers source tree).  Used as the
+ * checker by tests/, by __graft_entry__.smoke() and as the CPU baseline by
+ * bench.py; the GPU library never links it.
+ */
+#include "fos_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define DIMS 3
+static void* xcalloc(size_t n, size_t s) {
+  void* p = calloc(n ? n : 1, s);
+  if (!p) {
+    fprintf(stderr, "fos_oracle: out of memory (%zu x %zu)\n", n, s);
+    abort();
+  }
+  return p;
+}
+
+/* ====================================================================== geometry
+ * geometry.f90:17-91 */
+double og_a3p(const double* p) { /* geometry.f90:17-27 */
+  double a[3], b[3];
+  for (int d = 0; d < 3; d++) {
+    a[d] = p[3 + d] - p[d];
+    b[d] = p[6 + d] - p[d];
+  }
+  double c1 = a[1] * b[2] - a[2] * b[1];
+  double c2 = a[2] * b[0] - a[0] * b[2];
+  double c3 = a[0] * b[1] - a[1] * b[0];
+  return sqrt(c1 * c1 + c2 * c2 + c3 * c3) / 2.0;
+}
+static double og_a4p(const double* p) { /* geometry.f90:30-35: a3p([1,2,3]) + a3p([3,4,1]) */
+  double q[9];
+  memcpy(q, p + 6, 3 * sizeof(double));
+  memcpy(q + 3, p + 9, 3 * sizeof(double));
+  memcpy(q + 6, p, 3 * sizeof(double));
+  return og_a3p(p) + og_a3p(q);
+}
+void og_n3p(const double* p, double* n) { /* geometry.f90:38-49 */
+  double a[3], b[3], c[3];
+  for (int d = 0; d < 3; d++) {
+    a[d] = p[3 + d] - p[d];
+    b[d] = p[6 + d] - p[3 + d];
+  }
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+  double nn = sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+  for (int d = 0; d < 3; d++) n[d] = c[d] / nn;
+}
+static void og_n4p(const double* p, double* n) { /* geometry.f90:52-58 */
+  double q[9], n1[3], n2[3];
+  memcpy(q, p + 6, 3 * sizeof(double));
+  memcpy(q + 3, p + 9, 3 * sizeof(double));
+  memcpy(q + 6, p, 3 * sizeof(double));
+  og_n3p(p, n1);
+  og_n3p(q, n2);
+  for (int d = 0; d < 3; d++) n[d] = n1[d] + n2[d];
+  double nn = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+  for (int d = 0; d < 3; d++) n[d] /= nn;
+}
+double og_v4p(const double* p) { /* geometry.f90:61-82 (cofactor expansion, same term order) */
+#define X(k) p[3 * ((k)-1) + 0]
+#define Y(k) p[3 * ((k)-1) + 1]
+#define Z(k) p[3 * ((k)-1) + 2]
+  double y1z2 = Y(1) * Z(2), y1z3 = Y(1) * Z(3), y1z4 = Y(1) * Z(4);
+  double y2z1 = Y(2) * Z(1), y2z3 = Y(2) * Z(3), y2z4 = Y(2) * Z(4);
+  double y3z1 = Y(3) * Z(1), y3z2 = Y(3) * Z(2), y3z4 = Y(3) * Z(4);
+  double y4z1 = Y(4) * Z(1), y4z2 = Y(4) * Z(2), y4z3 = Y(4) * Z(3);
+  double d = (X(2) * (y3z4 - y4z3) - X(3) * (y2z4 - y4z2) + X(4) * (y2z3 - y3z2)) -
+             (X(1) * (y3z4 - y4z3) - X(3) * (y1z4 - y4z1) + X(4) * (y1z3 - y3z1)) +
+             (X(1) * (y2z4 - y4z2) - X(2) * (y1z4 - y4z1) + X(4) * (y1z2 - y2z1)) -
+             (X(1) * (y2z3 - y3z2) - X(2) * (y1z3 - y3z1) + X(3) * (y1z2 - y2z1));
+#undef X
+#undef Y
+#undef Z
+  return fabs(d) / 6.0;
+}
+double og_v8p(const double* p) { /* geometry.f90:85-91 */
+  static const int t[6][4] = {{1, 2, 3, 6}, {1, 3, 4, 6}, {1, 4, 5, 6},
+                              {4, 5, 6, 7}, {3, 4, 6, 7}, {4, 5, 7, 8}};
+  double s = 0.0, q[12];
+  for (int k = 0; k < 6; k++) {
+    for (int l = 0; l < 4; l++) memcpy(q + 3 * l, p + 3 * (t[k][l] - 1), 3 * sizeof(double));
+    s += og_v4p(q);
+  }
+  return s;
+}
+
+/* ====================================================================== sort
+ * sort.f90:15-65 -- quicksort (not stable) carrying a permutation */
+static void qsort_actual(int* a, int* perm, int first, int last) { /* 1-based bounds */
+  int pivot = a[(first + last) / 2 - 1];
+  int i = first, j = last, tmp;
+  for (;;) {
+    while (a[i - 1] < pivot) i++;
+    while (pivot < a[j - 1]) j--;
+    if (i >= j) break;
+    tmp = a[i - 1]; a[i - 1] = a[j - 1]; a[j - 1] = tmp;
+    tmp = perm[i - 1]; perm[i - 1] = perm[j - 1]; perm[j - 1] = tmp;
+    i++;
+    j--;
+  }
+  if (first < i - 1) qsort_actual(a, perm, first, i - 1);
+  if (j + 1 < last) qsort_actual(a, perm, j + 1, last);
+}
+void og_qsort_perm(int n, int* a, int* perm) {
+  for (int i = 0; i < n; i++) perm[i] = i + 1;
+  if (n > 0) qsort_actual(a, perm, 1, n);
+}
+
+/* ====================================================================== grid */
+struct og_grid {
+  int nN, nE, m, nC, nF, nP, nPi, nPb, maxFace;
+  double* pN;
+  int *sE, *nNE, *iNE, *gid;
+  double *p, *v;
+  int* iEP;
+  double *aP, *normP, *pP;
+  int* neib;
+};
+
+static int nF_of(int s) { /* polyGrid.f90:146-160 */
+  switch (s) {
+    case O_TRI: case O_QUAD: return 1;
+    case O_TET: return 4;
+    case O_HEX: return 6;
+    default: return 0;
+  }
+}
+static int nNF_of(int s, int i) { /* polyGrid.f90:163-208 */
+  switch (s) {
+    case O_TRI: return i == 1 ? 3 : 0;
+    case O_QUAD: return i == 1 ? 4 : 0;
+    case O_TET: return (i >= 1 && i <= 4) ? 3 : 0;
+    case O_HEX: return (i >= 1 && i <= 6) ? 4 : 0;
+    default: return 0;
+  }
+}
+static void getINF(int s, int i, int* ind, int len) { /* polyGrid.f90:211-278 */
+  static const int tet[4][3] = {{1, 3, 2}, {1, 2, 4}, {1, 4, 3}, {2, 3, 4}};
+  static const int hex[6][4] = {{2, 3, 7, 6}, {1, 5, 8, 4}, {3, 4, 8, 7},
+                                {1, 2, 6, 5}, {5, 6, 7, 8}, {1, 4, 3, 2}};
+  for (int k = 0; k < len; k++) ind[k] = 0;
+  switch (s) {
+    case O_TRI: if (i == 1) { ind[0] = 1; ind[1] = 2; ind[2] = 3; } break;
+    case O_QUAD: if (i == 1) { ind[0] = 1; ind[1] = 2; ind[2] = 3; ind[3] = 4; } break;
+    case O_TET: if (i >= 1 && i <= 4) for (int k = 0; k < 3; k++) ind[k] = tet[i - 1][k]; break;
+    case O_HEX: if (i >= 1 && i <= 6) for (int k = 0; k < 4; k++) ind[k] = hex[i - 1][k]; break;
+    default: break;
+  }
+}
+
+static int is_cell(int s) { return s == O_TET || s == O_HEX; }
+static int is_facet(int s) { return s == O_TRI || s == O_QUAD; }
+
+og_grid* og_grid_build(int nN, const double* pN, int nE, int m, const int* sE_in,
+                       const int* nNE_in, const int* iNE_in, const int* gid_in) {
+  og_grid* g = (og_grid*)xcalloc(1, sizeof(og_grid));
+  g->nN = nN; g->nE = nE; g->m = m;
+  g->pN = (double*)xcalloc((size_t)3 * nN, sizeof(double));
+  memcpy(g->pN, pN, sizeof(double) * 3 * (size_t)nN);
+  g->sE = (int*)xcalloc(nE, sizeof(int));
+  g->nNE = (int*)xcalloc(nE, sizeof(int));
+  g->iNE = (int*)xcalloc((size_t)m * nE, sizeof(int));
+  g->gid = (int*)xcalloc(nE, sizeof(int));
+  g->p = (double*)xcalloc((size_t)3 * nE, sizeof(double));
+  /* polyX%up: element centroid (polyX.f90:59-71) -- computed before the sort and carried */
+  double* pc = (double*)xcalloc((size_t)3 * nE, sizeof(double));
+  for (int i = 0; i < nE; i++) {
+    for (int d = 0; d < 3; d++) {
+      double s = 0.0;
+      for (int j = 0; j < nNE_in[i]; j++) s += pN[3 * (iNE_in[(size_t)m * i + j] - 1) + d];
+      pc[3 * i + d] = s / (double)nNE_in[i];
+    }
+  }
+  /* sortPolyGrid: cells first, then facets, then the rest (polyGrid.f90:88-136) */
+  int j = 0;
+  for (int pass = 0; pass < 3; pass++) {
+    for (int i = 0; i < nE; i++) {
+      int s = sE_in[i];
+      int take = pass == 0 ? is_cell(s) : pass == 1 ? is_facet(s) : !(is_cell(s) || is_facet(s));
+      if (!take) continue;
+      g->sE[j] = s;
+      g->nNE[j] = nNE_in[i];
+      memcpy(g->iNE + (size_t)m * j, iNE_in + (size_t)m * i, sizeof(int) * m);
+      memcpy(g->p + 3 * j, pc + 3 * i, 3 * sizeof(double));
+      g->gid[j] = gid_in ? gid_in[i] : 0;
+      j++;
+    }
+    if (pass == 0) g->nC = j;
+    if (pass == 1) g->nF = j - g->nC;
+  }
+  free(pc);
+  /* volumes (polyGrid.f90:72-82) */
+  g->v = (double*)xcalloc(g->nC, sizeof(double));
+  for (int i = 0; i < g->nC; i++) {
+    double q[24];
+    int nn = g->sE[i] == O_TET ? 4 : 8;
+    for (int k = 0; k < nn; k++) memcpy(q + 3 * k, g->pN + 3 * (g->iNE[(size_t)m * i + k] - 1), 3 * sizeof(double));
+    g->v[i] = g->sE[i] == O_TET ? og_v4p(q) : og_v8p(q);
+  }
+  /* getNeibPolyFvGrid (polyFvGrid.f90:60-198) */
+  int* nEN = (int*)xcalloc(nN, sizeof(int));
+  for (int i = 0; i < nE; i++)
+    for (int k = 0; k < g->nNE[i]; k++) nEN[g->iNE[(size_t)m * i + k] - 1]++;
+  int maxEN = 0;
+  for (int i = 0; i < nN; i++) if (nEN[i] > maxEN) maxEN = nEN[i];
+  int* iEN = (int*)xcalloc((size_t)maxEN * nN, sizeof(int));
+  memset(nEN, 0, sizeof(int) * nN);
+  for (int i = 0; i < nE; i++)
+    for (int k = 0; k < g->nNE[i]; k++) {
+      int nd = g->iNE[(size_t)m * i + k] - 1;
+      iEN[(size_t)maxEN * nd + nEN[nd]] = i + 1;
+      nEN[nd]++;
+    }
+  int* nFace = (int*)xcalloc(nE, sizeof(int));
+  int L = 0, maxFace = 0;
+  long tot = 0;
+  for (int i = 0; i < nE; i++) {
+    nFace[i] = nF_of(g->sE[i]);
+    tot += nFace[i];
+    if (nFace[i] > maxFace) maxFace = nFace[i];
+    for (int k = 1; k <= nFace[i]; k++) if (nNF_of(g->sE[i], k) > L) L = nNF_of(g->sE[i], k);
+  }
+  g->maxFace = maxFace;
+  int* iNF = (int*)xcalloc(L, sizeof(int));
+  int* iNF1 = (int*)xcalloc(L, sizeof(int));
+  g->neib = (int*)xcalloc((size_t)maxFace * (g->nC ? g->nC : 1), sizeof(int));
+  int* iEP = (int*)xcalloc((size_t)2 * tot, sizeof(int));
+  double* aP = (double*)xcalloc(tot, sizeof(double));
+  double* normP = (double*)xcalloc((size_t)3 * tot, sizeof(double));
+  double* pP = (double*)xcalloc((size_t)3 * tot, sizeof(double));
+  int nP = 0, nPi = 0, nPb = 0;
+  const int nC = g->nC;
+#define NEIB(jj, ii) g->neib[(size_t)maxFace * ((ii)-1) + (jj)-1]
+  for (int i = 1; i <= nC; i++) {
+    for (int jf = 1; jf <= nFace[i - 1]; jf++) {
+      if (NEIB(jf, i) != 0) continue;
+      getINF(g->sE[i - 1], jf, iNF, L);
+      for (int k = 0; k < L; k++) if (iNF[k] > 0) iNF[k] = g->iNE[(size_t)m * (i - 1) + iNF[k] - 1];
+      int nn = 0;
+      for (int k = 0; k < L; k++) nn += iNF[k] > 0;
+      int first = iNF[0] - 1;
+      for (int round = 0; round < 2; round++) {
+        for (int k = 0; k < nEN[first]; k++) {
+          int me = iEN[(size_t)maxEN * first + k];
+          if (me == i) continue;
+          if (round == 0 && !(me > nC)) continue; /* 1st round: facets only */
+          if (round == 1 && !(me <= nC)) continue; /* 2nd round: cells only */
+          for (int l = 1; l <= nFace[me - 1]; l++) {
+            getINF(g->sE[me - 1], l, iNF1, L);
+            for (int q = 0; q < L; q++)
+              if (iNF1[q] > 0) iNF1[q] = g->iNE[(size_t)m * (me - 1) + iNF1[q] - 1];
+            int all = 1;
+            for (int ii = 0; ii < L && all; ii++) {
+              int any = 0;
+              for (int q = 0; q < L; q++) if (iNF1[q] == iNF[ii]) { any = 1; break; }
+              all = any;
+            }
+            if (!all) continue;
+            NEIB(jf, i) = me;
+            if (round == 1) NEIB(l, me) = i;
+            iEP[2 * nP] = i;
+            iEP[2 * nP + 1] = me;
+            double q[12];
+            for (int c = 0; c < 4 && c < L; c++)
+              if (iNF[c] > 0) memcpy(q + 3 * c, g->pN + 3 * (iNF[c] - 1), 3 * sizeof(double));
+            if (nn == 3) {
+              aP[nP] = og_a3p(q);
+              og_n3p(q, normP + 3 * nP);
+              for (int d = 0; d < 3; d++) pP[3 * nP + d] = (q[d] + q[3 + d] + q[6 + d]) / 3.0;
+            } else if (nn == 4) {
+              aP[nP] = og_a4p(q);
+              og_n4p(q, normP + 3 * nP);
+              for (int d = 0; d < 3; d++)
+                pP[3 * nP + d] = (q[d] + q[3 + d] + q[6 + d] + q[9 + d]) / 4.0;
+            }
+            nP++;
+            if (round == 0) nPb++; else nPi++;
+            if (round == 1) break; /* 'exit' leaves the face loop of candidate me only */
+          }
+        }
+        if (round == 0 && NEIB(jf, i) != 0) break; /* found a facet: skip the cell round */
+      }
+    }
+  }
+#undef NEIB
+  g->nP = nP; g->nPi = nPi; g->nPb = nPb;
+  /* sortPolyFvGrid: order pairs by max(iEP) (polyFvGrid.f90:201-227) */
+  int* a = (int*)xcalloc(nP, sizeof(int));
+  int* perm = (int*)xcalloc(nP, sizeof(int));
+  for (int i = 0; i < nP; i++) a[i] = iEP[2 * i] > iEP[2 * i + 1] ? iEP[2 * i] : iEP[2 * i + 1];
+  og_qsort_perm(nP, a, perm);
+  g->iEP = (int*)xcalloc((size_t)2 * nP, sizeof(int));
+  g->aP = (double*)xcalloc(nP, sizeof(double));
+  g->normP = (double*)xcalloc((size_t)3 * nP, sizeof(double));
+  g->pP = (double*)xcalloc((size_t)3 * nP, sizeof(double));
+  for (int i = 0; i < nP; i++) {
+    int s = perm[i] - 1;
+    g->iEP[2 * i] = iEP[2 * s];
+    g->iEP[2 * i + 1] = iEP[2 * s + 1];
+    g->aP[i] = aP[s];
+    memcpy(g->normP + 3 * i, normP + 3 * s, 3 * sizeof(double));
+    memcpy(g->pP + 3 * i, pP + 3 * s, 3 * sizeof(double));
+  }
+  free(a); free(perm); free(iEP); free(aP); free(normP); free(pP);
+  free(nEN); free(iEN); free(nFace); free(iNF); free(iNF1);
+  return g;
+}
+
+void og_grid_free(og_grid* g) {
+  if (!g) return;
+  free(g->pN); free(g->sE); free(g->nNE); free(g->iNE); free(g->gid); free(g->p); free(g->v);
+  free(g->iEP); free(g->aP); free(g->normP); free(g->pP); free(g->neib);
+  free(g);
+}
+void og_grid_sizes(const og_grid* g, int* out) {
+  out[0] = g->nC; out[1] = g->nE; out[2] = g->nP; out[3] = g->nPi; out[4] = g->nPb;
+  out[5] = g->maxFace; out[6] = g->nF;
+}
+void og_grid_copy(const og_grid* g, int* iEP, double* aP, double* normP, double* pP, double* v,
+                  int* neib, int* gid, double* p, int* sE) {
+  if (iEP) memcpy(iEP, g->iEP, sizeof(int) * 2 * (size_t)g->nP);
+  if (aP) memcpy(aP, g->aP, sizeof(double) * (size_t)g->nP);
+  if (normP) memcpy(normP, g->normP, sizeof(double) * 3 * (size_t)g->nP);
+  if (pP) memcpy(pP, g->pP, sizeof(double) * 3 * (size_t)g->nP);
+  if (v) memcpy(v, g->v, sizeof(double) * (size_t)g->nC);
+  if (neib) memcpy(neib, g->neib, sizeof(int) * (size_t)g->maxFace * g->nC);
+  if (gid) memcpy(gid, g->gid, sizeof(int) * (size_t)g->nE);
+  if (p) memcpy(p, g->p, sizeof(double) * 3 * (size_t)g->nE);
+  if (sE) memcpy(sE, g->sE, sizeof(int) * (size_t)g->nE);
+}
+
+/* ====================================================================== Euler */
+struct oe_ctx {
+  int nC, nE, nP, nPi, nPb, maxFace, nBC, maxP, nthreads;
+  int *iEP, *neib, *iBC, *bcT;
+  double *aP, *normP, *v, *bcP;
+  double gamm, r;
+  double *rho, *rhou, *rhoE, *u, *p, *temp, *c;
+  double *dRho, *dRhou, *dRhoE;
+  double *fu, *fH, *f1c, *f2c, *f3c; /* findEuler save arrays */
+  double *JacP, *JacC, *ju_, *jH, *jc; /* findEulerJac */
+  int has_jac;
+  /* P and its ILU(0) */
+  int nnz, ierr;
+  double *pa, *alu;
+  int *pja, *pia, *jlu, *jluu, *iw;
+  double *t1, *t2;
+};
+
+static double dot3(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+static double norm2_3(const double* a) { return sqrt(dot3(a, a)); }
+
+oe_ctx* oe_new(int nC, int nE, int nPi, int nPb, const int* iEP, const double* aP,
+               const double* normP, const double* v, int maxFace, const int* neib,
+               const int* iBC, int nBC, const int* bcT, const double* bcP, int maxP,
+               double gamm, double r, const double* rho0, const double* rhou0,
+               const double* rhoE0) {
+  oe_ctx* c = (oe_ctx*)xcalloc(1, sizeof(oe_ctx));
+  int nP = nPi + nPb;
+  c->nC = nC; c->nE = nE; c->nP = nP; c->nPi = nPi; c->nPb = nPb; c->maxFace = maxFace;
+  c->nBC = nBC; c->maxP = maxP; c->gamm = gamm; c->r = r; c->nthreads = 1;
+  c->iEP = (int*)xcalloc((size_t)2 * nP, sizeof(int)); memcpy(c->iEP, iEP, sizeof(int) * 2 * (size_t)nP);
+  c->aP = (double*)xcalloc(nP, sizeof(double)); memcpy(c->aP, aP, sizeof(double) * nP);
+  c->normP = (double*)xcalloc((size_t)3 * nP, sizeof(double)); memcpy(c->normP, normP, sizeof(double) * 3 * (size_t)nP);
+  c->v = (double*)xcalloc(nC, sizeof(double)); memcpy(c->v, v, sizeof(double) * nC);
+  c->neib = (int*)xcalloc((size_t)maxFace * nC, sizeof(int));
+  if (neib) memcpy(c->neib, neib, sizeof(int) * (size_t)maxFace * nC);
+  c->iBC = (int*)xcalloc(nE, sizeof(int));
+  if (iBC) memcpy(c->iBC, iBC, sizeof(int) * nE);
+  c->bcT = (int*)xcalloc(nBC, sizeof(int));
+  if (nBC) memcpy(c->bcT, bcT, sizeof(int) * nBC);
+  c->bcP = (double*)xcalloc((size_t)maxP * nBC, sizeof(double));
+  if (nBC && maxP) memcpy(c->bcP, bcP, sizeof(double) * (size_t)maxP * nBC);
+  c->rho = (double*)xcalloc(nE, sizeof(double));
+  c->rhou = (double*)xcalloc((size_t)3 * nE, sizeof(double));
+  c->rhoE = (double*)xcalloc(nE, sizeof(double));
+  c->u = (double*)xcalloc((size_t)3 * nE, sizeof(double));
+  c->p = (double*)xcalloc(nE, sizeof(double));
+  c->temp = (double*)xcalloc(nE, sizeof(double));
+  c->c = (double*)xcalloc(nE, sizeof(double));
+  memcpy(c->rho, rho0, sizeof(double) * nE);
+  memcpy(c->rhou, rhou0, sizeof(double) * 3 * (size_t)nE);
+  memcpy(c->rhoE, rhoE0, sizeof(double) * nE);
+  /* init(): u, p, temp, c of the initial state for every element (foeuler.f90:124-140) */
+  for (int i = 0; i < nE; i++) {
+    for (int d = 0; d < 3; d++) c->u[3 * i + d] = c->rhou[3 * i + d] / c->rho[i];
+    c->p[i] = (gamm - 1.0) * (c->rhoE[i] - 0.5 * dot3(c->rhou + 3 * i, c->rhou + 3 * i) / c->rho[i]);
+    c->temp[i] = c->p[i] / c->rho[i] / r;
+    c->c[i] = sqrt(gamm * r * c->temp[i]);
+  }
+  c->dRho = (double*)xcalloc(nC, sizeof(double));
+  c->dRhou = (double*)xcalloc((size_t)3 * nC, sizeof(double));
+  c->dRhoE = (double*)xcalloc(nC, sizeof(double));
+  c->fu = (double*)xcalloc((size_t)3 * nE, sizeof(double));
+  c->fH = (double*)xcalloc(nE, sizeof(double));
+  c->f1c = (double*)xcalloc((size_t)3 * nE, sizeof(double));
+  c->f2c = (double*)xcalloc((size_t)9 * nE, sizeof(double));
+  c->f3c = (double*)xcalloc((size_t)3 * nE, sizeof(double));
+  c->t1 = (double*)xcalloc((size_t)5 * nC, sizeof(double));
+  c->t2 = (double*)xcalloc((size_t)5 * nC, sizeof(double));
+  return c;
+}
+
+void oe_free(oe_ctx* c) {
+  if (!c) return;
+  free(c->iEP); free(c->aP); free(c->normP); free(c->v); free(c->neib); free(c->iBC);
+  free(c->bcT); free(c->bcP); free(c->rho); free(c->rhou); free(c->rhoE); free(c->u);
+  free(c->p); free(c->temp); free(c->c); free(c->dRho); free(c->dRhou); free(c->dRhoE);
+  free(c->fu); free(c->fH); free(c->f1c); free(c->f2c); free(c->f3c);
+  free(c->JacP); free(c->JacC); free(c->ju_); free(c->jH); free(c->jc);
+  free(c->pa); free(c->pja); free(c->pia); free(c->alu); free(c->jlu); free(c->jluu); free(c->iw);
+  free(c->t1); free(c->t2);
+  free(c);
+}
+void oe_set_threads(oe_ctx* c, int nthreads) { c->nthreads = nthreads < 1 ? 1 : nthreads; }
+
+/* setBC (foeuler.f90:209-330); UDF variants are not supported (libmatheval absent) */
+static void oe_setBC(oe_ctx* c, const double* x) {
+  const int nC = c->nC;
+  const double g = c->gamm, r = c->r;
+  for (int i = c->nPi; i < c->nPi + c->nPb; i++) {
+    int m = c->iEP[2 * i], n = c->iEP[2 * i + 1];
+    const double* nrm = c->normP + 3 * i;
+    double xm[3] = {x[nC + m - 1], x[2 * nC + m - 1], x[3 * nC + m - 1]};
+    double* rhou_n = c->rhou + 3 * (n - 1);
+    int ib = c->iBC[n - 1];
+    int t = ib == 0 ? O_BC_WALL : c->bcT[ib - 1];
+    const double* bp = ib == 0 ? NULL : c->bcP + (size_t)c->maxP * (ib - 1);
+    double rhoGst, uGst[3], TGst, pGst;
+    switch (t) {
+      case O_BC_WALL: { /* foeuler.f90:217-228 */
+        c->rho[n - 1] = x[m - 1];
+        double dn = dot3(xm, nrm);
+        for (int d = 0; d < 3; d++) rhou_n[d] = xm[d] - 2.0 * dn * nrm[d];
+        c->rhoE[n - 1] = x[4 * nC + m - 1];
+        break;
+      }
+      case O_BC_IN_STATIC: { /* foeuler.f90:229-249 */
+        pGst = bp[0]; TGst = bp[1];
+        uGst[0] = bp[2]; uGst[1] = bp[3]; uGst[2] = bp[4];
+        double Mach = norm2_3(uGst) / sqrt(g * r * TGst);
+        rhoGst = pGst / r / TGst;
+        if (Mach < 1.0)
+          for (int d = 0; d < 3; d++) uGst[d] = xm[d] / rhoGst;
+        c->rho[n - 1] = rhoGst;
+        for (int d = 0; d < 3; d++) rhou_n[d] = rhoGst * uGst[d];
+        c->rhoE[n - 1] = rhoGst * (1.0 / (g - 1.0) * r * TGst + 0.5 * dot3(uGst, uGst));
+        break;
+      }
+      case O_BC_IN_TOTAL: { /* foeuler.f90:250-276 */
+        double ptGst = bp[0], TtGst = bp[1];
+        uGst[0] = bp[2]; uGst[1] = bp[3]; uGst[2] = bp[4];
+        TGst = TtGst - 0.5 * (g - 1.0) / g / r * dot3(uGst, uGst);
+        double Mach = norm2_3(uGst) / sqrt(g * r * TGst);
+        pGst = ptGst * pow(1.0 + 0.5 * (g - 1.0) * Mach * Mach, -g / (g - 1.0));
+        rhoGst = pGst / r / TGst;
+        if (Mach < 1.0) {
+          double ui[3] = {xm[0] / x[m - 1], xm[1] / x[m - 1], xm[2] / x[m - 1]};
+          double s = dot3(ui, uGst) / dot3(uGst, uGst);
+          for (int d = 0; d < 3; d++) uGst[d] = s * uGst[d];
+          TGst = TtGst - 0.5 * (g - 1.0) / g / r * dot3(uGst, uGst);
+          Mach = norm2_3(uGst) / sqrt(g * r * TGst);
+          pGst = ptGst * pow(1.0 + 0.5 * (g - 1.0) * Mach * Mach, -g / (g - 1.0));
+          rhoGst = pGst / r / TGst;
+        }
+        c->rho[n - 1] = rhoGst;
+        for (int d = 0; d < 3; d++) rhou_n[d] = rhoGst * uGst[d];
+        c->rhoE[n - 1] = rhoGst * (1.0 / (g - 1.0) * r * TGst + 0.5 * dot3(uGst, uGst));
+        break;
+      }
+      case O_BC_OUT: { /* foeuler.f90:277-287 */
+        pGst = bp[0];
+        c->rho[n - 1] = x[m - 1];
+        for (int d = 0; d < 3; d++) rhou_n[d] = xm[d];
+        c->rhoE[n - 1] = 1.0 / (g - 1.0) * pGst + 0.5 * dot3(xm, xm) / x[m - 1];
+        break;
+      }
+      case O_BC_OUT_EXTRAP: { /* zero-gradient outflow: not in the reference */
+        c->rho[n - 1] = x[m - 1];
+        for (int d = 0; d < 3; d++) rhou_n[d] = xm[d];
+        c->rhoE[n - 1] = x[4 * nC + m - 1];
+        break;
+      }
+      case O_BC_FAR: { /* foeuler.f90:288-325 */
+        pGst = bp[0]; TGst = bp[1];
+        uGst[0] = bp[2]; uGst[1] = bp[3]; uGst[2] = bp[4];
+        double rm = x[m - 1], Em = x[4 * nC + m - 1];
+        double charO = dot3(uGst, nrm) - 2.0 * sqrt(g * r * TGst) / (g - 1.0);
+        double ui[3] = {xm[0] / rm, xm[1] / rm, xm[2] / rm};
+        double charI = dot3(ui, nrm) + 2.0 * sqrt(g / rm / (g - 1.0) * (Em - 0.5 * dot3(ui, ui) * rm));
+        double un[3], ut[3];
+        for (int d = 0; d < 3; d++) un[d] = 0.5 * nrm[d] * (charI + charO);
+        double a = 0.25 * (g - 1.0) * (charI - charO);
+        double ptGst, Mach;
+        if (dot3(un, nrm) > 0.0) {
+          double s = dot3(nrm, ui);
+          for (int d = 0; d < 3; d++) ut[d] = ui[d] - nrm[d] * s;
+          Mach = norm2_3(ui) / sqrt(g / rm * (g - 1.0) * (Em - 0.5 * dot3(ui, ui) * rm));
+          ptGst = (g - 1.0) * (Em - 0.5 * dot3(ui, ui) * rm) *
+                  pow(1.0 + 0.5 * (g - 1.0) * Mach * Mach, g / (g - 1.0));
+        } else {
+          for (int d = 0; d < 3; d++) ut[d] = uGst[d] - un[d];
+          Mach = norm2_3(uGst) / sqrt(g * r * TGst);
+          ptGst = pGst * pow(1.0 + 0.5 * (g - 1.0) * Mach * Mach, g / (g - 1.0));
+        }
+        for (int d = 0; d < 3; d++) uGst[d] = un[d] + ut[d];
+        TGst = a * a / g / r;
+        Mach = norm2_3(uGst) / a;
+        pGst = ptGst * pow(1.0 + 0.5 * (g - 1.0) * Mach * Mach, -g / (g - 1.0));
+        rhoGst = pGst / r / TGst;
+        c->rho[n - 1] = rhoGst;
+        for (int d = 0; d < 3; d++) rhou_n[d] = rhoGst * uGst[d];
+        c->rhoE[n - 1] = rhoGst * (1.0 / (g - 1.0) * r * TGst + 0.5 * dot3(uGst, uGst));
+        break;
+      }
+      default: break;
+    }
+  }
+}
+
+/* syncState (foeuler.f90:186-206) */
+static void oe_syncState(oe_ctx* c, const double* x) {
+  const int nC = c->nC, nE = c->nE;
+  const double g = c->gamm, r = c->r;
+#pragma omp parallel for num_threads(c->nthreads) if (c->nthreads > 1)
+  for (int i = 0; i < nC; i++) {
+    c->rho[i] = x[i];
+    c->rhou[3 * i] = x[nC + i];
+    c->rhou[3 * i + 1] = x[2 * nC + i];
+    c->rhou[3 * i + 2] = x[3 * nC + i];
+    c->rhoE[i] = x[4 * nC + i];
+  }
+#pragma omp parallel for num_threads(c->nthreads) if (c->nthreads > 1)
+  for (int i = 0; i < nE; i++) {
+    const double* ru = c->rhou + 3 * i;
+    for (int d = 0; d < 3; d++) c->u[3 * i + d] = ru[d] / c->rho[i];
+    c->p[i] = (g - 1.0) * (c->rhoE[i] - 0.5 * dot3(ru, ru) / c->rho[i]);
+    c->temp[i] = c->p[i] / c->rho[i] / r;
+    c->c[i] = sqrt(g * r * c->temp[i]);
+  }
+}
+
+/* findEulerPoly (Euler.f90:25-156) */
+static void oe_findEuler(oe_ctx* c) {
+  const int nC = c->nC, k = c->nE, nP = c->nP;
+  const double g = c->gamm;
+  const double *rho = c->rho, *rhou = c->rhou, *rhoE = c->rhoE, *p = c->p;
+  double *dRho = c->dRho, *dRhou = c->dRhou, *dRhoE = c->dRhoE;
+  double *u = c->fu, *H = c->fH, *f1c = c->f1c, *f2c = c->f2c, *f3c = c->f3c;
+  memset(dRho, 0, sizeof(double) * nC);
+  memset(dRhou, 0, sizeof(double) * 3 * (size_t)nC);
+  memset(dRhoE, 0, sizeof(double) * nC);
+  const int nt = c->nthreads;
+#pragma omp parallel num_threads(nt) if (nt > 1)
+  {
+#pragma omp for
+    for (int i = 0; i < k; i++) { /* Euler.f90:73-81 */
+      for (int d = 0; d < 3; d++) u[3 * i + d] = rhou[3 * i + d] / rho[i];
+      H[i] = (rhoE[i] + p[i]) / rho[i];
+      for (int d = 0; d < 3; d++) f1c[3 * i + d] = rhou[3 * i + d];
+      for (int col = 0; col < 3; col++)
+        for (int d = 0; d < 3; d++)
+          f2c[9 * i + 3 * col + d] = rhou[3 * i + col] * u[3 * i + d] + (d == col ? p[i] : 0.0);
+      for (int d = 0; d < 3; d++) f3c[3 * i + d] = (rhoE[i] + p[i]) * u[3 * i + d];
+    }
+#pragma omp for
+    for (int i = 0; i < nP; i++) { /* Euler.f90:86-153 */
+      int m = c->iEP[2 * i] - 1, n = c->iEP[2 * i + 1] - 1;
+      if (!(m < k && n < k)) continue;
+      const double* nr = c->normP + 3 * i;
+      const double *um = u + 3 * m, *un = u + 3 * n;
+      double sm = sqrt(rho[m]), sn = sqrt(rho[n]);
+      double rhoAvg = sqrt(rho[m] * rho[n]);
+      double uAvg[3];
+      for (int d = 0; d < 3; d++) uAvg[d] = (sm * um[d] + sn * un[d]) / (sm + sn);
+      double uNormAvg = dot3(uAvg, nr);
+      double HAvg = (sm * H[m] + sn * H[n]) / (sm + sn);
+      double cAvg = sqrt((g - 1.0) * (HAvg - 0.5 * dot3(uAvg, uAvg)));
+      double rhoJump = rho[n] - rho[m];
+      double pJump = p[n] - p[m];
+      double uJump[3] = {un[0] - um[0], un[1] - um[1], un[2] - um[2]};
+      double uNormJump = dot3(uJump, nr);
+      double c2 = cAvg * cAvg;
+      double dFE[5], dFA1[5], dFA2[5];
+      /* abs(uNormAvg)*((rhoJump-pJump/cAvg**2)*vec1 + rhoAvg*vec2), same grouping */
+      {
+        double w = rhoJump - pJump / c2;
+        double au = fabs(uNormAvg);
+        double v1[5] = {1.0, uAvg[0], uAvg[1], uAvg[2], 0.5 * dot3(uAvg, uAvg)};
+        double v2[5] = {0.0, uJump[0] - nr[0] * uNormJump, uJump[1] - nr[1] * uNormJump,
+                        uJump[2] - nr[2] * uNormJump, dot3(uAvg, uJump) - uNormAvg * uNormJump};
+        for (int q = 0; q < 5; q++) dFE[q] = au * (w * v1[q] + rhoAvg * v2[q]);
+      }
+      double s1 = fabs(uNormAvg - cAvg) * (0.5 * (pJump - rhoAvg * cAvg * uNormJump) / c2);
+      dFA1[0] = s1 * 1.0;
+      for (int d = 0; d < 3; d++) dFA1[1 + d] = s1 * (uAvg[d] - nr[d] * cAvg);
+      dFA1[4] = s1 * (HAvg - uNormAvg * cAvg);
+      double s2 = fabs(uNormAvg + cAvg) * (0.5 * (pJump + rhoAvg * cAvg * uNormJump) / c2);
+      dFA2[0] = s2 * 1.0;
+      for (int d = 0; d < 3; d++) dFA2[1 + d] = s2 * (uAvg[d] + nr[d] * cAvg);
+      dFA2[4] = s2 * (HAvg + uNormAvg * cAvg);
+      double cen[5];
+      {
+        double t = 0.0;
+        for (int d = 0; d < 3; d++) t += 0.5 * (f1c[3 * m + d] + f1c[3 * n + d]) * nr[d];
+        cen[0] = t;
+        for (int col = 0; col < 3; col++) {
+          t = 0.0;
+          for (int d = 0; d < 3; d++) t += 0.5 * (f2c[9 * m + 3 * col + d] + f2c[9 * n + 3 * col + d]) * nr[d];
+          cen[1 + col] = t;
+        }
+        t = 0.0;
+        for (int d = 0; d < 3; d++) t += 0.5 * (f3c[3 * m + d] + f3c[3 * n + d]) * nr[d];
+        cen[4] = t;
+      }
+      double flow[5];
+      for (int q = 0; q < 5; q++) flow[q] = c->aP[i] * (cen[q] - 0.5 * (dFE[q] + dFA1[q] + dFA2[q]));
+      if (nt > 1) {
+        if (n < nC) {
+#pragma omp atomic
+          dRho[m] -= flow[0];
+#pragma omp atomic
+          dRho[n] += flow[0];
+          for (int d = 0; d < 3; d++) {
+#pragma omp atomic
+            dRhou[3 * m + d] -= flow[1 + d];
+#pragma omp atomic
+            dRhou[3 * n + d] += flow[1 + d];
+          }
+#pragma omp atomic
+          dRhoE[m] -= flow[4];
+#pragma omp atomic
+          dRhoE[n] += flow[4];
+        } else {
+#pragma omp atomic
+          dRho[m] -= flow[0];
+          for (int d = 0; d < 3; d++) {
+#pragma omp atomic
+            dRhou[3 * m + d] -= flow[1 + d];
+          }
+#pragma omp atomic
+          dRhoE[m] -= flow[4];
+        }
+      } else {
+        dRho[m] -= flow[0];
+        for (int d = 0; d < 3; d++) dRhou[3 * m + d] -= flow[1 + d];
+        dRhoE[m] -= flow[4];
+        if (n < nC) {
+          dRho[n] += flow[0];
+          for (int d = 0; d < 3; d++) dRhou[3 * n + d] += flow[1 + d];
+          dRhoE[n] += flow[4];
+        }
+      }
+    }
+  }
+}
+
+/* rhs (foeuler.f90:349-375) */
+int oe_rhs(double t, const double* y, double* ydot, void* ud) {
+  (void)t;
+  oe_ctx* c = (oe_ctx*)ud;
+  const int nC = c->nC;
+  oe_setBC(c, y);
+  oe_syncState(c, y);
+  oe_findEuler(c);
+  int bad = 0;
+#pragma omp parallel for num_threads(c->nthreads) if (c->nthreads > 1) reduction(| : bad)
+  for (int i = 0; i < nC; i++) {
+    ydot[i] = c->dRho[i] / c->v[i];
+    ydot[nC + i] = c->dRhou[3 * i] / c->v[i];
+    ydot[2 * nC + i] = c->dRhou[3 * i + 1] / c->v[i];
+    ydot[3 * nC + i] = c->dRhou[3 * i + 2] / c->v[i];
+    ydot[4 * nC + i] = c->dRhoE[i] / c->v[i];
+    for (int q = 0; q < 5; q++) bad |= !isfinite(ydot[q * nC + i]);
+  }
+  /* the reference always returns 0; a non-finite residual is reported as recoverable (>0) */
+  return bad ? 1 : 0;
+}
+
+void oe_elem_state(const oe_ctx* c, double* rho, double* rhou, double* rhoE) {
+  if (rho) memcpy(rho, c->rho, sizeof(double) * c->nE);
+  if (rhou) memcpy(rhou, c->rhou, sizeof(double) * 3 * (size_t)c->nE);
+  if (rhoE) memcpy(rhoE, c->rhoE, sizeof(double) * c->nE);
+}
+
+/* eulerNFJ (Euler.f90:252-276); out 5x5 column-major */
+void oe_nfj(const double* norm, const double* u, double H, double gamm, double* out) {
+  double v = norm2_3(u), vn = dot3(u, norm), tmp[9];
+  memset(tmp, 0, sizeof(tmp));
+  for (int j = 0; j < 3; j++)
+    for (int i = 0; i < 3; i++) tmp[i + 3 * j] += 1.0 * u[i] * norm[j];          /* dger */
+  for (int j = 0; j < 3; j++)
+    for (int i = 0; i < 3; i++) tmp[i + 3 * j] += (1.0 - gamm) * norm[i] * u[j]; /* dger */
+  for (int i = 0; i < 3; i++) tmp[i + 3 * i] += vn;
+#define F(i, j) out[((i)-1) + 5 * ((j)-1)]
+  memset(out, 0, 25 * sizeof(double));
+  for (int i = 0; i < 3; i++) F(2 + i, 1) = 0.5 * (gamm - 1.0) * v * v * norm[i] - u[i] * vn;
+  F(5, 1) = (0.5 * (gamm - 1.0) * v * v - H) * vn;
+  for (int j = 0; j < 3; j++) F(1, 2 + j) = norm[j];
+  for (int j = 0; j < 3; j++)
+    for (int i = 0; i < 3; i++) F(2 + i, 2 + j) = tmp[i + 3 * j];
+  for (int j = 0; j < 3; j++) F(5, 2 + j) = H * norm[j] - (gamm - 1.0) * u[j] * vn;
+  for (int i = 0; i < 3; i++) F(2 + i, 5) = (gamm - 1.0) * norm[i];
+  F(5, 5) = gamm * vn;
+#undef F
+}
+
+/* eulerANFJ (Euler.f90:279-333) */
+void oe_anfj(const double* norm, const double* u, double H, double cc, double gamm, double* out) {
+  double v = norm2_3(u), vn = dot3(u, norm), M = v / cc, Mn = vn / cc;
+  double tmp1[9], tmp2[25];
+#define T2(i, j) tmp2[((i)-1) + 5 * ((j)-1)]
+  memset(out, 0, 25 * sizeof(double));
+  memset(tmp1, 0, sizeof(tmp1));
+  for (int j = 0; j < 3; j++)
+    for (int i = 0; i < 3; i++) tmp1[i + 3 * j] += (gamm - 1.0) / (cc * cc) * u[i] * u[j];
+  for (int j = 0; j < 3; j++)
+    for (int i = 0; i < 3; i++) tmp1[i + 3 * j] += -1.0 * norm[i] * norm[j];
+  for (int i = 0; i < 3; i++) tmp1[i + 3 * i] += 1.0;
+  T2(1, 1) = 1.0 - 0.5 * (gamm - 1.0) * M * M;
+  for (int i = 0; i < 3; i++) T2(2 + i, 1) = -(1.0 + 0.5 * (gamm - 1.0) * M * M) * u[i] + vn * norm[i];
+  T2(5, 1) = vn * vn - 0.5 * v * v * (1.0 + 0.5 * (gamm - 1.0) * M * M);
+  for (int j = 0; j < 3; j++) T2(1, 2 + j) = (gamm - 1.0) / (cc * cc) * u[j];
+  for (int j = 0; j < 3; j++)
+    for (int i = 0; i < 3; i++) T2(2 + i, 2 + j) = tmp1[i + 3 * j];
+  for (int j = 0; j < 3; j++) T2(5, 2 + j) = (1.0 + 0.5 * (gamm - 1.0) * M * M) * u[j] - vn * norm[j];
+  T2(1, 5) = -(gamm - 1.0) / (cc * cc);
+  for (int i = 0; i < 3; i++) T2(2 + i, 5) = -(gamm - 1.0) / (cc * cc) * u[i];
+  T2(5, 5) = -0.5 * (gamm - 1.0) * M * M;
+  for (int q = 0; q < 25; q++) out[q] = fabs(vn) * tmp2[q];
+  for (int sgn = -1; sgn <= 1; sgn += 2) { /* the (vn - c) then the (vn + c) acoustic projector */
+    double a[3], b[3];
+    for (int i = 0; i < 3; i++) {
+      a[i] = u[i] + sgn * cc * norm[i];
+      b[i] = -0.5 * (gamm - 1.0) / (cc * cc) * u[i] + sgn * 0.5 * norm[i] / cc;
+    }
+    memset(tmp1, 0, sizeof(tmp1));
+    for (int j = 0; j < 3; j++)
+      for (int i = 0; i < 3; i++) tmp1[i + 3 * j] += 1.0 * a[i] * b[j];
+    double hh = H + sgn * vn * cc;
+    T2(1, 1) = 0.25 * (gamm - 1.0) * M * M - sgn * 0.5 * Mn;
+    for (int i = 0; i < 3; i++) T2(2 + i, 1) = a[i] * T2(1, 1);
+    T2(5, 1) = hh * T2(1, 1);
+    for (int j = 0; j < 3; j++) T2(1, 2 + j) = b[j];
+    for (int j = 0; j < 3; j++)
+      for (int i = 0; i < 3; i++) T2(2 + i, 2 + j) = tmp1[i + 3 * j];
+    for (int j = 0; j < 3; j++) T2(5, 2 + j) = hh * T2(1, 2 + j);
+    T2(1, 5) = 0.5 * (gamm - 1.0) / (cc * cc);
+    for (int i = 0; i < 3; i++) T2(2 + i, 5) = a[i] * T2(1, 5);
+    T2(5, 5) = hh * T2(1, 5);
+    double lam = fabs(vn + sgn * cc);
+    for (int q = 0; q < 25; q++) out[q] += lam * tmp2[q];
+  }
+#undef T2
+}
+
+/* findEulerJacPoly (Euler.f90:159-249) on the current element state */
+static void oe_findEulerJac(oe_ctx* c) {
+  const int nC = c->nC, k = c->nE, nP = c->nP, mf = c->maxFace;
+  const double g = c->gamm;
+  const int ncol = 5 * mf + 5;
+  if (!c->JacP) c->JacP = (double*)xcalloc((size_t)100 * nP, sizeof(double));
+  if (!c->JacC) c->JacC = (double*)xcalloc((size_t)5 * ncol * nC, sizeof(double));
+  if (!c->ju_) {
+    c->ju_ = (double*)xcalloc((size_t)3 * k, sizeof(double));
+    c->jH = (double*)xcalloc(k, sizeof(double));
+    c->jc = (double*)xcalloc(k, sizeof(double));
+  }
+  memset(c->JacP, 0, sizeof(double) * 100 * (size_t)nP);
+  memset(c->JacC, 0, sizeof(double) * 5 * (size_t)ncol * nC);
+  double *u = c->ju_, *H = c->jH, *cs = c->jc;
+  for (int i = 0; i < k; i++) { /* Euler.f90:195-199 */
+    for (int d = 0; d < 3; d++) u[3 * i + d] = c->rhou[3 * i + d] / c->rho[i];
+    H[i] = (c->rhoE[i] + c->p[i]) / c->rho[i];
+    cs[i] = sqrt((g - 1.0) * (H[i] - 0.5 * dot3(u + 3 * i, u + 3 * i)));
+  }
+#define JP(a, b, i) c->JacP[((a)-1) + 10 * ((b)-1) + (size_t)100 * (i)]
+  for (int i = 0; i < nP; i++) { /* Euler.f90:203-221 */
+    int m = c->iEP[2 * i] - 1, n = c->iEP[2 * i + 1] - 1;
+    if (!(m < k && n < k)) continue;
+    const double* nr = c->normP + 3 * i;
+    double sm = sqrt(c->rho[m]), sn = sqrt(c->rho[n]), uAvg[3];
+    for (int d = 0; d < 3; d++) uAvg[d] = (sm * u[3 * m + d] + sn * u[3 * n + d]) / (sm + sn);
+    double HAvg = (sm * H[m] + sn * H[n]) / (sm + sn);
+    double cAvg = sqrt((g - 1.0) * (HAvg - 0.5 * dot3(uAvg, uAvg)));
+    double A[25], Am[25], An[25];
+    oe_anfj(nr, uAvg, HAvg, cAvg, g, A);
+    oe_nfj(nr, u + 3 * m, H[m], g, Am);
+    for (int b = 1; b <= 5; b++)
+      for (int a = 1; a <= 5; a++) JP(a, b, i) = -0.5 * c->aP[i] * (Am[(a - 1) + 5 * (b - 1)] + A[(a - 1) + 5 * (b - 1)]);
+    if (n < nC) {
+      oe_nfj(nr, u + 3 * n, H[n], g, An);
+      for (int b = 1; b <= 5; b++)
+        for (int a = 1; a <= 5; a++)
+          JP(a, 5 + b, i) = -0.5 * c->aP[i] * (An[(a - 1) + 5 * (b - 1)] - A[(a - 1) + 5 * (b - 1)]);
+      for (int b = 1; b <= 10; b++)
+        for (int a = 1; a <= 5; a++) JP(5 + a, b, i) = -JP(a, b, i);
+    }
+  }
+  /* copy Jacobian to cell (Euler.f90:225-248) */
+#define JC(a, col, cell) c->JacC[((a)-1) + 5 * ((size_t)((col)-1) + (size_t)ncol * (cell))]
+  for (int i = 0; i < nP; i++) {
+    int m = c->iEP[2 * i] - 1, n = c->iEP[2 * i + 1] - 1;
+    if (m < nC)
+      for (int b = 1; b <= 5; b++)
+        for (int a = 1; a <= 5; a++) JC(a, b, m) += JP(a, b, i);
+    if (n < nC)
+      for (int b = 1; b <= 5; b++)
+        for (int a = 1; a <= 5; a++) JC(a, b, n) += JP(5 + a, 5 + b, i);
+    if (m < nC && n < nC) {
+      for (int j = 1; j <= mf; j++)
+        if (c->neib[(size_t)mf * m + j - 1] == n + 1) {
+          for (int b = 1; b <= 5; b++)
+            for (int a = 1; a <= 5; a++) JC(a, 5 * j + b, m) += JP(a, 5 + b, i);
+          break;
+        }
+      for (int j = 1; j <= mf; j++)
+        if (c->neib[(size_t)mf * n + j - 1] == m + 1) {
+          for (int b = 1; b <= 5; b++)
+            for (int a = 1; a <= 5; a++) JC(a, 5 * j + b, n) += JP(5 + a, b, i);
+          break;
+        }
+    }
+  }
+#undef JP
+#undef JC
+  c->has_jac = 1;
+}
+
+const double* oe_jac(oe_ctx* c, const double* y) {
+  oe_setBC(c, y);
+  oe_syncState(c, y);
+  oe_findEulerJac(c);
+  return c->JacC;
+}
+
+/* ====================================================================== SPARSKIT */
+void o_coocsr(int nrow, int nnz, const double* a, const int* ir, const int* jc, double* ao,
+              int* jao, int* iao) { /* FORMATS/formats.f:164-230 */
+  for (int k = 0; k <= nrow; k++) iao[k] = 0;
+  for (int k = 0; k < nnz; k++) iao[ir[k] - 1]++;
+  int k = 1;
+  for (int j = 0; j <= nrow; j++) {
+    int k0 = iao[j];
+    iao[j] = k;
+    k += k0;
+  }
+  for (int q = 0; q < nnz; q++) {
+    int i = ir[q], iad = iao[i - 1];
+    ao[iad - 1] = a[q];
+    jao[iad - 1] = jc[q];
+    iao[i - 1] = iad + 1;
+  }
+  for (int j = nrow; j >= 1; j--) iao[j] = iao[j - 1];
+  iao[0] = 1;
+}
+void o_csrsort(int n, double* a, int* ja, const int* ia) { /* per-row insertion sort by column */
+  for (int i = 0; i < n; i++) {
+    for (int k = ia[i]; k < ia[i + 1] - 1; k++) {
+      int kk = k;
+      while (kk >= ia[i] && ja[kk - 1] > ja[kk]) {
+        int tj = ja[kk - 1]; ja[kk - 1] = ja[kk]; ja[kk] = tj;
+        double ta = a[kk - 1]; a[kk - 1] = a[kk]; a[kk] = ta;
+        kk--;
+      }
+    }
+  }
+}
+void o_amux(int n, const double* x, double* y, const double* a, const int* ja, const int* ia) {
+  for (int i = 0; i < n; i++) { /* BLASSM/matvec.f:34-75 */
+    double t = 0.0;
+    for (int k = ia[i]; k < ia[i + 1]; k++) t += a[k - 1] * x[ja[k - 1] - 1];
+    y[i] = t;
+  }
+}
+int o_ilu0(int n, const double* a, const int* ja, const int* ia, double* alu, int* jlu, int* ju,
+           int* iw) { /* ITSOL/ilut.f:1793-1917; all arrays 1-based in content */
+#define ALU(k) alu[(k)-1]
+#define JLU(k) jlu[(k)-1]
+#define JU(k) ju[(k)-1]
+#define IW(k) iw[(k)-1]
+  int ju0 = n + 2;
+  JLU(1) = ju0;
+  for (int i = 1; i <= n; i++) IW(i) = 0;
+  for (int ii = 1; ii <= n; ii++) {
+    int js = ju0;
+    for (int j = ia[ii - 1]; j <= ia[ii] - 1; j++) {
+      int jcol = ja[j - 1];
+      if (jcol == ii) {
+        ALU(ii) = a[j - 1];
+        IW(jcol) = ii;
+        JU(ii) = ju0;
+      } else {
+        ALU(ju0) = a[j - 1];
+        JLU(ju0) = ja[j - 1];
+        IW(jcol) = ju0;
+        ju0++;
+      }
+    }
+    JLU(ii + 1) = ju0;
+    int jf = ju0 - 1, jm = JU(ii) - 1;
+    for (int j = js; j <= jm; j++) {
+      int jrow = JLU(j);
+      double tl = ALU(j) * ALU(jrow);
+      ALU(j) = tl;
+      for (int jj = JU(jrow); jj <= JLU(jrow + 1) - 1; jj++) {
+        int jw = IW(JLU(jj));
+        if (jw != 0) ALU(jw) = ALU(jw) - tl * ALU(jj);
+      }
+    }
+    if (ALU(ii) == 0.0) return ii;
+    ALU(ii) = 1.0 / ALU(ii);
+    IW(ii) = 0;
+    for (int i = js; i <= jf; i++) IW(JLU(i)) = 0;
+  }
+  return 0;
+#undef ALU
+#undef JLU
+#undef JU
+#undef IW
+}
+void o_lusol(int n, const double* y, double* x, const double* alu, const int* jlu, const int* ju) {
+  for (int i = 1; i <= n; i++) { /* ITSOL/ilut.f:2272-2320 */
+    double s = y[i - 1];
+    for (int k = jlu[i - 1]; k <= ju[i - 1] - 1; k++) s -= alu[k - 1] * x[jlu[k - 1] - 1];
+    x[i - 1] = s;
+  }
+  for (int i = n; i >= 1; i--) {
+    double s = x[i - 1];
+    for (int k = ju[i - 1]; k <= jlu[i] - 1; k++) s -= alu[k - 1] * x[jlu[k - 1] - 1];
+    x[i - 1] = alu[i - 1] * s;
+  }
+}
+
+/* ====================================================================== pset / psol
+ * The reference pset/psol are stubs (foeuler.f90:378-437); the comment at :401-402 states the
+ * intent: rescale the Jacobian with gamma and factor.  This follows the fopbc wiring
+ * (modPbc.f90:676-711: COO -> setCOO/coocsr -> fact -> solve/lusol) with ilu0 in place of
+ * ilut, on P = I - gamma*diag(1/v)*JacC in interleaved (cell-major) scalar ordering. */
+static void oe_build_P(oe_ctx* c, double gamma) {
+  const int nC = c->nC, mf = c->maxFace, ncol = 5 * mf + 5, n = 5 * nC;
+  /* count entries */
+  long nnz = 0;
+  for (int cc = 0; cc < nC; cc++) {
+    int nb = 1;
+    for (int j = 1; j <= mf; j++) {
+      int k = c->neib[(size_t)mf * cc + j - 1];
+      if (k >= 1 && k <= nC) nb++;
+    }
+    nnz += 25L * nb;
+  }
+  if (!c->pa) {
+    c->pa = (double*)xcalloc(nnz, sizeof(double));
+    c->pja = (int*)xcalloc(nnz, sizeof(int));
+    c->pia = (int*)xcalloc(n + 1, sizeof(int));
+    c->alu = (double*)xcalloc(nnz + 2, sizeof(double));
+    c->jlu = (int*)xcalloc(nnz + 2, sizeof(int));
+    c->jluu = (int*)xcalloc(n, sizeof(int));
+    c->iw = (int*)xcalloc(n, sizeof(int));
+  }
+  c->nnz = (int)nnz;
+  int* ir = (int*)xcalloc(nnz, sizeof(int));
+  int* jcv = (int*)xcalloc(nnz, sizeof(int));
+  double* av = (double*)xcalloc(nnz, sizeof(double));
+  long q = 0;
+  for (int cc = 0; cc < nC; cc++) {
+    int blk[16], col[16], nb = 0;
+    blk[nb] = 0; col[nb] = cc + 1; nb++;
+    for (int j = 1; j <= mf; j++) {
+      int k = c->neib[(size_t)mf * cc + j - 1];
+      if (k >= 1 && k <= nC) { blk[nb] = j; col[nb] = k; nb++; }
+    }
+    for (int x = 1; x < nb; x++) /* blocks by increasing column: lower part first (ilut.f:1835) */
+      for (int y = x; y > 0 && col[y - 1] > col[y]; y--) {
+        int t = col[y]; col[y] = col[y - 1]; col[y - 1] = t;
+        t = blk[y]; blk[y] = blk[y - 1]; blk[y - 1] = t;
+      }
+    double s = gamma / c->v[cc];
+    for (int a = 1; a <= 5; a++)
+      for (int bI = 0; bI < nb; bI++)
+        for (int b = 1; b <= 5; b++) {
+          double jv = c->JacC[(a - 1) + 5 * ((size_t)(5 * blk[bI] + b - 1) + (size_t)ncol * cc)];
+          ir[q] = 5 * cc + a;
+          jcv[q] = 5 * (col[bI] - 1) + b;
+          av[q] = (blk[bI] == 0 && a == b ? 1.0 : 0.0) - s * jv;
+          q++;
+        }
+  }
+  o_coocsr(n, (int)nnz, av, ir, jcv, c->pa, c->pja, c->pia);
+  o_csrsort(n, c->pa, c->pja, c->pia);
+  free(ir); free(jcv); free(av);
+}
+
+int oe_pset(double t, const double* y, const double* fy, int jok, int* jcur, double gamma,
+            void* ud) {
+  (void)t; (void)fy;
+  oe_ctx* c = (oe_ctx*)ud;
+  if (jok == 0 || !c->has_jac) {
+    oe_jac(c, y);
+    if (jcur) *jcur = 1;
+  } else if (jcur) {
+    *jcur = 0;
+  }
+  oe_build_P(c, gamma);
+  c->ierr = o_ilu0(5 * c->nC, c->pa, c->pja, c->pia, c->alu, c->jlu, c->jluu, c->iw);
+  return c->ierr ? 1 : 0; /* zero pivot: recoverable */
+}
+
+int oe_psol(double t, const double* y, const double* fy, const double* r, double* z,
+            double gamma, double delta, int lr, void* ud) {
+  (void)t; (void)y; (void)fy; (void)gamma; (void)delta; (void)lr;
+  oe_ctx* c = (oe_ctx*)ud;
+  const int nC = c->nC;
+  for (int i = 0; i < nC; i++)
+    for (int a = 0; a < 5; a++) c->t1[5 * i + a] = r[a * nC + i];
+  o_lusol(5 * nC, c->t1, c->t2, c->alu, c->jlu, c->jluu);
+  for (int i = 0; i < nC; i++)
+    for (int a = 0; a < 5; a++) z[a * nC + i] = c->t2[5 * i + a];
+  return 0;
+}
+int oe_pmat(const oe_ctx* c, const double** a, const int** ja, const int** ia) {
+  *a = c->pa; *ja = c->pja; *ia = c->pia;
+  return c->nnz;
+}
+int oe_ilu_ierr(const oe_ctx* c) { return c->ierr; }
+
+/* ====================================================================== Newton-Krylov
+ * Fixed-step BDF with Newton--GMRES.  SUNDIALS (CVODE, SPGMR) is not vendored in the
+ * reference; this restates the published algorithms with the contract CVODE drives the
+ * callbacks by (SUNDIALS.f90:745-845; foeuler.f90:171-174,450):
+ *   G(y) = y - gamma f(t,y) - h,  gamma = beta*dt, h = history combination
+ *   J_G v ~ v - gamma (f(y + s v) - f(y))/s,  s = jv_eps (1 + ||y||_2)/||v||_2
+ *   right-preconditioned restarted GMRES(maxl), classical Gram-Schmidt with one
+ *   re-orthogonalisation (CGS2), Givens least squares, stop at ||r|| <= lin_rtol ||b||
+ *   Newton stops when ||G(y_k)||_WRMS <= 1, weights 1/(rtol |y_n| + atol). */
+typedef struct {
+  int n;
+  o_rhs_fn f;
+  o_psol_fn psol;
+  void* ud;
+  double t, gamma, a_coef, b_coef, ynorm, eps;
+  const double *y, *fy;
+  double *ytmp, *ftmp;
+  o_bdf_stats* st;
+  int use_prec;
+} nk_op;
+
+static double vdot(int n, const double* a, const double* b) {
+  double s = 0.0;
+  for (int i = 0; i < n; i++) s += a[i] * b[i];
+  return s;
+}
+static int nk_matvec(nk_op* op, const double* v, double* out) {
+  const int n = op->n;
+  double nv = sqrt(vdot(n, v, v));
+  if (nv == 0.0) {
+    memset(out, 0, sizeof(double) * n);
+    return 0;
+  }
+  double s = op->eps * (1.0 + op->ynorm) / nv;
+  for (int i = 0; i < n; i++) op->ytmp[i] = op->y[i] + s * v[i];
+  int rc = op->f(op->t, op->ytmp, op->ftmp, op->ud);
+  op->st->n_rhs++;
+  op->st->n_jv++;
+  for (int i = 0; i < n; i++) out[i] = op->a_coef * v[i] + op->b_coef * ((op->ftmp[i] - op->fy[i]) / s);
+  return rc;
+}
+static int nk_prec(nk_op* op, const double* r, double* z, double delta) {
+  if (!op->use_prec) {
+    memcpy(z, r, sizeof(double) * op->n);
+    return 0;
+  }
+  op->st->n_psol++;
+  return op->psol(op->t, op->y, op->fy, r, z, op->gamma, delta, 2, op->ud);
+}
+
+/* GMRES(m) on J_G x = b, x starts at 0; returns 0 ok, 1 not converged, <0 callback failure */
+static int nk_gmres(nk_op* op, const double* b, double* x, int m, int max_restarts, double rtol,
+                    int* iters) {
+  const int n = op->n;
+  double* V = (double*)xcalloc((size_t)n * (m + 1), sizeof(double));
+  double* Z = (double*)xcalloc((size_t)n * m, sizeof(double));
+  double* w = (double*)xcalloc(n, sizeof(double));
+  double* H = (double*)xcalloc((size_t)(m + 1) * m, sizeof(double));
+  double *cs = (double*)xcalloc(m, sizeof(double)), *sn = (double*)xcalloc(m, sizeof(double));
+  double *g = (double*)xcalloc(m + 1, sizeof(double)), *h = (double*)xcalloc(m + 1, sizeof(double));
+  double *h2 = (double*)xcalloc(m + 1, sizeof(double)), *yv = (double*)xcalloc(m, sizeof(double));
+  memset(x, 0, sizeof(double) * n);
+  double bnorm = sqrt(vdot(n, b, b));
+  int status = 1, it = 0;
+  if (bnorm == 0.0) { status = 0; goto done; }
+  memcpy(w, b, sizeof(double) * n);
+  double beta = bnorm;
+  for (int cyc = 0; cyc <= max_restarts; cyc++) {
+    for (int i = 0; i < n; i++) V[i] = w[i] / beta;
+    memset(g, 0, sizeof(double) * (m + 1));
+    g[0] = beta;
+    int j, kend = 0;
+    int conv = 0;
+    for (j = 0; j < m; j++) {
+      double* vj = V + (size_t)n * j;
+      double* zj = Z + (size_t)n * j;
+      int rc = nk_prec(op, vj, zj, rtol * bnorm);
+      if (rc) { status = rc < 0 ? rc : -1; goto done; }
+      rc = nk_matvec(op, zj, w);
+      if (rc) { status = rc < 0 ? rc : -2; goto done; }
+      it++;
+      /* CGS2 */
+      for (int l = 0; l <= j; l++) h[l] = vdot(n, V + (size_t)n * l, w);
+      for (int l = 0; l <= j; l++) { const double* vl = V + (size_t)n * l; for (int i = 0; i < n; i++) w[i] -= h[l] * vl[i]; }
+      for (int l = 0; l <= j; l++) h2[l] = vdot(n, V + (size_t)n * l, w);
+      for (int l = 0; l <= j; l++) { const double* vl = V + (size_t)n * l; for (int i = 0; i < n; i++) w[i] -= h2[l] * vl[i]; }
+      for (int l = 0; l <= j; l++) h[l] += h2[l];
+      double hn = sqrt(vdot(n, w, w));
+      for (int l = 0; l <= j; l++) H[l + (size_t)(m + 1) * j] = h[l];
+      H[j + 1 + (size_t)(m + 1) * j] = hn;
+      if (hn > 0.0) { double* vn = V + (size_t)n * (j + 1); for (int i = 0; i < n; i++) vn[i] = w[i] / hn; }
+      /* Givens */
+      double* col = H + (size_t)(m + 1) * j;
+      for (int l = 0; l < j; l++) {
+        double t0 = cs[l] * col[l] + sn[l] * col[l + 1];
+        col[l + 1] = -sn[l] * col[l] + cs[l] * col[l + 1];
+        col[l] = t0;
+      }
+      double den = sqrt(col[j] * col[j] + col[j + 1] * col[j + 1]);
+      if (den == 0.0) { cs[j] = 1.0; sn[j] = 0.0; }
+      else { cs[j] = col[j] / den; sn[j] = col[j + 1] / den; }
+      col[j] = cs[j] * col[j] + sn[j] * col[j + 1];
+      col[j + 1] = 0.0;
+      g[j + 1] = -sn[j] * g[j];
+      g[j] = cs[j] * g[j];
+      kend = j + 1;
+      if (fabs(g[j + 1]) <= rtol * bnorm) { conv = 1; break; }
+      if (hn == 0.0) { conv = 1; break; }
+    }
+    /* back substitution */
+    for (int l = kend - 1; l >= 0; l--) {
+      double s = g[l];
+      for (int q = l + 1; q < kend; q++) s -= H[l + (size_t)(m + 1) * q] * yv[q];
+      yv[l] = s / H[l + (size_t)(m + 1) * l];
+    }
+    for (int l = 0; l < kend; l++) { const double* zl = Z + (size_t)n * l; for (int i = 0; i < n; i++) x[i] += yv[l] * zl[i]; }
+    if (conv) { status = 0; break; }
+    if (cyc == max_restarts) break;
+    /* true residual for the restart */
+    int rc = nk_matvec(op, x, w);
+    if (rc) { status = -2; goto done; }
+    for (int i = 0; i < n; i++) w[i] = b[i] - w[i];
+    beta = sqrt(vdot(n, w, w));
+    if (beta <= rtol * bnorm) { status = 0; break; }
+  }
+done:
+  if (iters) *iters = it;
+  free(V); free(Z); free(w); free(H); free(cs); free(sn); free(g); free(h); free(h2); free(yv);
+  return status;
+}
+
+void o_bdf_defaults(o_bdf_opts* o) {
+  o->order = 1; o->dt = 1e-3; o->nsteps = 1;
+  o->newton_rtol = 1e-8; o->newton_atol = 1e-12; o->max_newton = 10;
+  o->maxl = 30; o->max_restarts = 4; o->lin_rtol = 1e-3;
+  o->jv_eps = 1.4901161193847656e-08; o->use_prec = 1;
+}
+
+static double wrms(int n, const double* v, const double* yref, double rtol, double atol) {
+  double s = 0.0;
+  for (int i = 0; i < n; i++) {
+    double w = v[i] / (rtol * fabs(yref[i]) + atol);
+    s += w * w;
+  }
+  return sqrt(s / n);
+}
+
+int o_bdf_run(int n, o_rhs_fn rhs, o_pset_fn pset, o_psol_fn psol, void* ud, double t0,
+              double* y, const o_bdf_opts* opts, o_bdf_stats* st) {
+  o_bdf_stats dummy;
+  if (!st) st = &dummy;
+  memset(st, 0, sizeof(*st));
+  double *yn = (double*)xcalloc(n, sizeof(double)), *ynm1 = (double*)xcalloc(n, sizeof(double));
+  double *hist = (double*)xcalloc(n, sizeof(double)), *f = (double*)xcalloc(n, sizeof(double));
+  double *G = (double*)xcalloc(n, sizeof(double)), *d = (double*)xcalloc(n, sizeof(double));
+  double *ytmp = (double*)xcalloc(n, sizeof(double)), *ftmp = (double*)xcalloc(n, sizeof(double));
+  double t = t0;
+  int status = 0;
+  memcpy(yn, y, sizeof(double) * n);
+  for (int s = 0; s < opts->nsteps; s++) {
+    int q = (opts->order == 2 && s >= 1) ? 2 : 1;
+    double gamma;
+    if (q == 1) {
+      gamma = opts->dt;
+      memcpy(hist, yn, sizeof(double) * n);
+    } else {
+      gamma = 2.0 * opts->dt / 3.0;
+      for (int i = 0; i < n; i++) hist[i] = (4.0 / 3.0) * yn[i] - (1.0 / 3.0) * ynm1[i];
+    }
+    double tn = t + opts->dt;
+    memcpy(y, yn, sizeof(double) * n); /* predictor: previous state */
+    int conv = 0;
+    for (int k = 0; k <= opts->max_newton; k++) {
+      int rc = rhs(tn, y, f, ud);
+      st->n_rhs++;
+      if (rc) { status = 2; break; }
+      for (int i = 0; i < n; i++) G[i] = y[i] - gamma * f[i] - hist[i];
+      double gn = wrms(n, G, yn, opts->newton_rtol, opts->newton_atol);
+      st->last_gnorm = gn;
+      if (gn <= 1.0) { conv = 1; break; }
+      if (k == opts->max_newton) break;
+      if (k == 0 && opts->use_prec) {
+        int jcur = 0;
+        rc = pset(tn, y, f, 0, &jcur, gamma, ud);
+        st->n_pset++;
+        if (rc) { status = 3; break; }
+      }
+      nk_op op = {n, rhs, psol, ud, tn, gamma, 1.0, -gamma, sqrt(vdot(n, y, y)), opts->jv_eps,
+                  y, f, ytmp, ftmp, st, opts->use_prec};
+      for (int i = 0; i < n; i++) G[i] = -G[i];
+      int its = 0;
+      rc = nk_gmres(&op, G, d, opts->maxl, opts->max_restarts, opts->lin_rtol, &its);
+      st->n_lin_iters += its;
+      st->n_newton++;
+      if (rc < 0) { status = 4; break; }
+      for (int i = 0; i < n; i++) y[i] += d[i];
+    }
+    if (!conv) {
+      st->fails++;
+      if (!status) status = 1;
+      break;
+    }
+    memcpy(ynm1, yn, sizeof(double) * n);
+    memcpy(yn, y, sizeof(double) * n);
+    t = tn;
+    st->n_steps++;
+  }
+  free(yn); free(ynm1); free(hist); free(f); free(G); free(d); free(ytmp); free(ftmp);
+  return status;
+}
+
+int o_newton_solve(int n, o_rhs_fn Gf, void* ud, double* x, double rtol, double atol,
+                   int max_newton, int maxl, double lin_rtol, o_bdf_stats* st) {
+  o_bdf_stats dummy;
+  if (!st) st = &dummy;
+  memset(st, 0, sizeof(*st));
+  double *G = (double*)xcalloc(n, sizeof(double)), *d = (double*)xcalloc(n, sizeof(double));
+  double *xt = (double*)xcalloc(n, sizeof(double)), *ft = (double*)xcalloc(n, sizeof(double));
+  double* xref = (double*)xcalloc(n, sizeof(double));
+  memcpy(xref, x, sizeof(double) * n);
+  int status = 1;
+  for (int k = 0; k <= max_newton; k++) {
+    Gf(0.0, x, G, ud);
+    st->n_rhs++;
+    double gn = 0.0;
+    for (int i = 0; i < n; i++) gn += G[i] * G[i];
+    gn = sqrt(gn / n) / atol;
+    (void)rtol;
+    st->last_gnorm = gn;
+    if (gn <= 1.0) { status = 0; break; }
+    if (k == max_newton) break;
+    nk_op op = {n, Gf, NULL, ud, 0.0, 0.0, 0.0, 1.0, sqrt(vdot(n, x, x)),
+                1.4901161193847656e-08, x, G, xt, ft, st, 0};
+    double* b = (double*)xcalloc(n, sizeof(double));
+    for (int i = 0; i < n; i++) b[i] = -G[i];
+    int its = 0;
+    int rc = nk_gmres(&op, b, d, maxl, 4, lin_rtol, &its);
+    free(b);
+    st->n_lin_iters += its;
+    st->n_newton++;
+    if (rc < 0) { status = 4; break; }
+    for (int i = 0; i < n; i++) x[i] += d[i];
+  }
+  free(G); free(d); free(xt); free(ft); free(xref);
+  return status;
+}

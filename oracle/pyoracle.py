@@ -1,0 +1,217 @@
+"""ctypes binding of the CPU oracle (liboracle.so) -- TEST INFRASTRUCTURE ONLY.
+
+Loaded by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as the
+checker / baseline; never by the fosolvers_gb300 package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_vp = C.c_void_p
+
+RHS_FN = C.CFUNCTYPE(C.c_int, C.c_double, _dp, _dp, _vp)
+PSET_FN = C.CFUNCTYPE(C.c_int, C.c_double, _dp, _dp, C.c_int, _ip, C.c_double, _vp)
+PSOL_FN = C.CFUNCTYPE(C.c_int, C.c_double, _dp, _dp, _dp, _dp, C.c_double, C.c_double, C.c_int, _vp)
+
+
+class BdfOpts(C.Structure):
+    _fields_ = [("order", C.c_int), ("dt", C.c_double), ("nsteps", C.c_int),
+                ("newton_rtol", C.c_double), ("newton_atol", C.c_double),
+                ("max_newton", C.c_int), ("maxl", C.c_int), ("max_restarts", C.c_int),
+                ("lin_rtol", C.c_double), ("jv_eps", C.c_double), ("use_prec", C.c_int)]
+
+
+class BdfStats(C.Structure):
+    _fields_ = [("n_rhs", C.c_long), ("n_jv", C.c_long), ("n_psol", C.c_long),
+                ("n_pset", C.c_long), ("n_newton", C.c_long), ("n_lin_iters", C.c_long),
+                ("n_steps", C.c_long), ("fails", C.c_long), ("last_gnorm", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_SIGS = {
+    "og_grid_build": (_vp, [C.c_int, _dp, C.c_int, C.c_int, _ip, _ip, _ip, _ip]),
+    "og_grid_free": (None, [_vp]),
+    "og_grid_sizes": (None, [_vp, _ip]),
+    "og_grid_copy": (None, [_vp, _ip, _dp, _dp, _dp, _dp, _ip, _ip, _dp, _ip]),
+    "og_a3p": (C.c_double, [_dp]),
+    "og_v4p": (C.c_double, [_dp]),
+    "og_v8p": (C.c_double, [_dp]),
+    "og_n3p": (None, [_dp, _dp]),
+    "og_qsort_perm": (None, [C.c_int, _ip, _ip]),
+    "oe_new": (_vp, [C.c_int, C.c_int, C.c_int, C.c_int, _ip, _dp, _dp, _dp, C.c_int, _ip, _ip,
+                     C.c_int, _ip, _dp, C.c_int, C.c_double, C.c_double, _dp, _dp, _dp]),
+    "oe_free": (None, [_vp]),
+    "oe_set_threads": (None, [_vp, C.c_int]),
+    "oe_rhs": (C.c_int, [C.c_double, _dp, _dp, _vp]),
+    "oe_pset": (C.c_int, [C.c_double, _dp, _dp, C.c_int, _ip, C.c_double, _vp]),
+    "oe_psol": (C.c_int, [C.c_double, _dp, _dp, _dp, _dp, C.c_double, C.c_double, C.c_int, _vp]),
+    "oe_jac": (_dp, [_vp, _dp]),
+    "oe_pmat": (C.c_int, [_vp, C.POINTER(_dp), C.POINTER(_ip), C.POINTER(_ip)]),
+    "oe_ilu_ierr": (C.c_int, [_vp]),
+    "oe_elem_state": (None, [_vp, _dp, _dp, _dp]),
+    "oe_nfj": (None, [_dp, _dp, C.c_double, C.c_double, _dp]),
+    "oe_anfj": (None, [_dp, _dp, C.c_double, C.c_double, C.c_double, _dp]),
+    "o_coocsr": (None, [C.c_int, C.c_int, _dp, _ip, _ip, _dp, _ip, _ip]),
+    "o_csrsort": (None, [C.c_int, _dp, _ip, _ip]),
+    "o_amux": (None, [C.c_int, _dp, _dp, _dp, _ip, _ip]),
+    "o_ilu0": (C.c_int, [C.c_int, _dp, _ip, _ip, _dp, _ip, _ip, _ip]),
+    "o_lusol": (None, [C.c_int, _dp, _dp, _dp, _ip, _ip]),
+    "o_bdf_defaults": (None, [C.POINTER(BdfOpts)]),
+    "o_bdf_run": (C.c_int, [C.c_int, _vp, _vp, _vp, _vp, C.c_double, _dp, C.POINTER(BdfOpts),
+                            C.POINTER(BdfStats)]),
+    "o_newton_solve": (C.c_int, [C.c_int, _vp, _vp, _dp, C.c_double, C.c_double, C.c_int, C.c_int,
+                                 C.c_double, C.POINTER(BdfStats)]),
+}
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        l = C.CDLL(str(path))
+        for name, (res, args) in _SIGS.items():
+            f = getattr(l, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = l
+    return _lib
+
+
+def dp(a):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+def ip(a):
+    assert a.dtype == np.int32 and a.flags.c_contiguous
+    return a.ctypes.data_as(_ip)
+
+
+def grid_build(mesh) -> dict:
+    """Reference face construction (polyGrid%up + getNeib + sort) on a Mesh."""
+    L = lib()
+    pN = np.ascontiguousarray(mesh.pN, np.float64)
+    iNE = np.ascontiguousarray(mesh.iNE, np.int32)
+    g = L.og_grid_build(mesh.nN, dp(pN), mesh.nE, iNE.shape[1],
+                        ip(np.ascontiguousarray(mesh.sE, np.int32)),
+                        ip(np.ascontiguousarray(mesh.nNE, np.int32)), ip(iNE),
+                        ip(np.ascontiguousarray(mesh.gid, np.int32)))
+    try:
+        sz = np.zeros(7, np.int32)
+        L.og_grid_sizes(g, ip(sz))
+        nC, nE, nP, nPi, nPb, mf, nF = (int(x) for x in sz)
+        out = dict(nC=nC, nE=nE, nP=nP, nPi=nPi, nPb=nPb, maxFace=mf, nF=nF,
+                   iEP=np.zeros((nP, 2), np.int32), aP=np.zeros(nP), normP=np.zeros((nP, 3)),
+                   pP=np.zeros((nP, 3)), v=np.zeros(nC), neib=np.zeros((nC, mf), np.int32),
+                   gid=np.zeros(nE, np.int32), p=np.zeros((nE, 3)), sE=np.zeros(nE, np.int32))
+        L.og_grid_copy(g, ip(out["iEP"]), dp(out["aP"]), dp(out["normP"]), dp(out["pP"]),
+                       dp(out["v"]), ip(out["neib"]), ip(out["gid"]), dp(out["p"]), ip(out["sE"]))
+    finally:
+        L.og_grid_free(g)
+    return out
+
+
+class Euler:
+    """oe_ctx: the reference foeuler module state restated on the CPU."""
+
+    def __init__(self, grid, iBC, bc_type, bc_param, gamm, r, elem_state, threads=1):
+        L = lib()
+        self.nC, self.nE = grid["nC"] if isinstance(grid, dict) else grid.nC, \
+            grid["nE"] if isinstance(grid, dict) else grid.nE
+        gg = grid if isinstance(grid, dict) else grid.__dict__
+        rho, ru, rv, rw, rE = (np.ascontiguousarray(x, np.float64) for x in elem_state)
+        rhou = np.ascontiguousarray(np.stack([ru, rv, rw], axis=1))
+        nBC = int(len(bc_type))
+        bcp = np.ascontiguousarray(np.asarray(bc_param, np.float64).reshape(max(nBC, 1), -1)) \
+            if nBC else np.zeros((1, 5))
+        self._keep = [np.ascontiguousarray(gg["iEP"], np.int32), np.ascontiguousarray(gg["aP"]),
+                      np.ascontiguousarray(gg["normP"]), np.ascontiguousarray(gg["v"]),
+                      np.ascontiguousarray(gg["neib"], np.int32),
+                      np.ascontiguousarray(iBC, np.int32),
+                      np.ascontiguousarray(bc_type, np.int32) if nBC else np.zeros(1, np.int32),
+                      bcp, rho, rhou, rE]
+        k = self._keep
+        self.h = L.oe_new(self.nC, self.nE, gg["nPi"], gg["nPb"], ip(k[0]), dp(k[1]), dp(k[2]),
+                          dp(k[3]), gg["maxFace"], ip(k[4]), ip(k[5]), nBC, ip(k[6]), dp(k[7]),
+                          int(bcp.shape[1]), gamm, r, dp(rho), dp(rhou), dp(rE))
+        self.set_threads(threads)
+
+    def set_threads(self, n):
+        lib().oe_set_threads(self.h, int(n))
+
+    def close(self):
+        if self.h:
+            lib().oe_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def rhs(self, t, y, ydot):
+        return lib().oe_rhs(t, dp(y), dp(ydot), self.h)
+
+    def pset(self, t, y, fy, jok, gamma):
+        jc = C.c_int(0)
+        rc = lib().oe_pset(t, dp(y), dp(fy) if fy is not None else None, jok, C.byref(jc), gamma,
+                           self.h)
+        return rc, jc.value
+
+    def psol(self, t, y, fy, r, z, gamma, delta=0.0, lr=1):
+        return lib().oe_psol(t, None, None, dp(r), dp(z), gamma, delta, lr, self.h)
+
+    def jac(self, y, maxFace):
+        ptr = lib().oe_jac(self.h, dp(y))
+        n = 5 * (5 * maxFace + 5) * self.nC
+        a = np.ctypeslib.as_array(ptr, shape=(n,)).copy()
+        # Fortran JacC(5, 5*(maxFace+1), nC) column-major -> [cell, block col, row]
+        return a.reshape(self.nC, 5 * maxFace + 5, 5)
+
+    def pmat(self):
+        a, ja, ia = _dp(), _ip(), _ip()
+        nnz = lib().oe_pmat(self.h, C.byref(a), C.byref(ja), C.byref(ia))
+        n = 5 * self.nC
+        return (np.ctypeslib.as_array(a, shape=(nnz,)).copy(),
+                np.ctypeslib.as_array(ja, shape=(nnz,)).copy(),
+                np.ctypeslib.as_array(ia, shape=(n + 1,)).copy())
+
+    def elem_state(self):
+        rho = np.zeros(self.nE)
+        rhou = np.zeros(3 * self.nE)
+        rE = np.zeros(self.nE)
+        lib().oe_elem_state(self.h, dp(rho), dp(rhou), dp(rE))
+        return rho, rhou.reshape(-1, 3), rE
+
+    def callbacks(self):
+        L = lib()
+        return (C.cast(L.oe_rhs, _vp), C.cast(L.oe_pset, _vp), C.cast(L.oe_psol, _vp))
+
+
+def bdf_defaults(**kw) -> BdfOpts:
+    o = BdfOpts()
+    lib().o_bdf_defaults(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def bdf_run(n, rhs, pset, psol, ud, y, opts, t0=0.0):
+    """rhs/pset/psol: raw C function pointers (c_void_p) or ctypes CFUNCTYPE objects."""
+    st = BdfStats()
+    as_vp = lambda f: f if isinstance(f, (C.c_void_p, int)) or f is None else C.cast(f, _vp)
+    rc = lib().o_bdf_run(n, as_vp(rhs), as_vp(pset), as_vp(psol), ud, t0, dp(y), C.byref(opts),
+                         C.byref(st))
+    return rc, st.as_dict()

@@ -1,0 +1,64 @@
+"""Shared set-up for the parity tests: one workload -> reference face arrays, oracle
+context and GPU context on the same mesh and initial state."""
+from __future__ import annotations
+
+import numpy as np
+
+from fosolvers_gb300 import mesh as M
+from fosolvers_gb300.euler import FOEuler, PolyFvGrid
+from oracle import pyoracle as O
+
+
+class Case:
+    def __init__(self, wl: M.Workload, flags: int = 0, grid_from: str = "product"):
+        self.wl = wl
+        self.grid = PolyFvGrid.from_mesh(wl.mesh)
+        self.g = self.grid.__dict__
+        self.nC = self.grid.nC
+        self.N = 5 * self.nC
+        self.iBC = M.ibc_for(wl.mesh, wl.bc_gid)
+        self.y0 = M.soa(wl.elem_state, self.nC)
+        self.flags = flags
+        self._oracle = None
+        self._gpu = None
+
+    @property
+    def oracle(self) -> O.Euler:
+        if self._oracle is None:
+            self._oracle = O.Euler(self.g, self.iBC, self.wl.bc_type, self.wl.bc_param,
+                                   self.wl.gamm, self.wl.r, self.wl.elem_state)
+        return self._oracle
+
+    @property
+    def gpu(self) -> FOEuler:
+        if self._gpu is None:
+            self._gpu = FOEuler(self.grid, self.iBC, self.wl.bc_type, self.wl.bc_param,
+                                self.wl.gamm, self.wl.r, flags=self.flags)
+        return self._gpu
+
+    def oracle_rhs(self, y):
+        f = np.zeros_like(y)
+        rc = self.oracle.rhs(0.0, np.ascontiguousarray(y), f)
+        assert rc == 0
+        return f
+
+
+def perturbed(y: np.ndarray, nC: int, seed: int, amp: float = 0.05) -> np.ndarray:
+    """Smooth-ish random perturbation that keeps rho and p positive."""
+    rng = np.random.default_rng(seed)
+    y = y.copy().reshape(5, nC)
+    rho = y[0] * (1.0 + amp * rng.uniform(-1, 1, nC))
+    u = y[1:4] / y[0] + amp * rng.uniform(-1, 1, (3, nC))
+    p = (0.4) * (y[4] - 0.5 * (y[1:4] ** 2).sum(0) / y[0]) * (1.0 + amp * rng.uniform(-1, 1, nC))
+    out = np.empty_like(y)
+    out[0] = rho
+    out[1:4] = rho * u
+    out[4] = p / 0.4 + 0.5 * rho * (u ** 2).sum(0)
+    return out.reshape(-1)
+
+
+def rel_err(a: np.ndarray, b: np.ndarray) -> float:
+    """max |a - b| / max |b| per conserved block, maximum over the 5 blocks."""
+    a = a.reshape(5, -1)
+    b = b.reshape(5, -1)
+    return float(max(np.abs(a[q] - b[q]).max() / max(np.abs(b[q]).max(), 1e-300) for q in range(5)))
