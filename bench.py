@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--mode", choices=["fp64", "fp32"], default="fp64",
                     help="fp64: FP64 flux + FP64 ILU(0); fp32: FP32 flux + FP32 ILU(0) apply")
     ap.add_argument("--precond", choices=["ilu", "none"], default="ilu")
+    ap.add_argument("--ilu-order", choices=["rcm", "color"], default="color",
+                    help="ILU(0) elimination order: internal RCM order or greedy colouring")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-oracle baseline")
     ap.add_argument("--no-ops", action="store_true", help="skip the per-operation timing")
     ap.add_argument("--no-e2e", action="store_true")
@@ -218,7 +220,7 @@ def main():
     from __graft_entry__ import build
     build()
     from fosolvers_gb300 import mesh as M
-    from fosolvers_gb300.euler import FLUX_FP32, ILU_FP32, FOEuler, PolyFvGrid
+    from fosolvers_gb300.euler import FLUX_FP32, ILU_COLOR, ILU_FP32, FOEuler, PolyFvGrid
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
@@ -227,6 +229,8 @@ def main():
     grid = PolyFvGrid.from_mesh(wl.mesh)
     ibc = M.ibc_for(wl.mesh, wl.bc_gid)
     flags = (FLUX_FP32 | ILU_FP32) if args.mode == "fp32" else 0
+    if args.ilu_order == "color":
+        flags |= ILU_COLOR
     stream = torch.cuda.current_stream(dev)
     ctx = FOEuler(grid, ibc, wl.bc_type, wl.bc_param, wl.gamm, wl.r, flags=flags, stream=stream)
     nC, nF = grid.nC, grid.nP
@@ -359,6 +363,8 @@ def main():
             "config": {"workload": workload_desc(args.workload) if args.scale is None else
                        f"{args.workload} at scale {args.scale}",
                        "cells": nC, "faces": nF, "mode": args.mode, "precond": args.precond,
+                       "ilu_order": args.ilu_order, "ilu_levels": [ctx.info()["nlev_fwd"],
+                                                                  ctx.info()["nlev_bwd"]],
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
                        "l2": "inputs larger than L2 (state 0.2 GB, ILU factors ~5 GB); no flush",
                        "setup_s": round(setup_s, 2)},

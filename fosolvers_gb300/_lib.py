@@ -51,6 +51,7 @@ _SIGS = {
     "fos_ctx_info": (None, [_vp, _lp]),
     "fos_ctx_permute_dev": (C.c_int, [_vp, _vp, _vp, C.c_int]),
     "fos_ctx_renumbering": (C.c_int, [_vp, _ip]),
+    "fos_ctx_ilu_order": (C.c_int, [_vp, _ip]),
     "fos_last_error": (C.c_char_p, []),
     "fos_euler_rhs": (C.c_int, [C.c_double, _dp, _dp, _vp]),
     "fos_euler_pset": (C.c_int, [C.c_double, _dp, _dp, C.c_int, _ip, C.c_double, _vp]),

@@ -5,7 +5,7 @@
 // (the workloads prescribe fixed-step BDF1/BDF2) and keeps every vector in HBM:
 //   BDF1: G(y) = y - dt f(y) - y_n                      gamma = dt
 //   BDF2: G(y) = y - 2/3 dt f(y) - (4/3 y_n - 1/3 y_{n-1})  gamma = 2/3 dt (first step BDF1)
-//   Newton: y_0 = y_n; stop when ||G(y_k)||_WRMS <= 1, w_i = 1/(rtol |y_n,i| + atol)
+//   Newton: y_0 = y_n; stop when ||G(y_k)||_2 <= rtol ||y_n||_2 + atol sqrt(N), in FP64
 //   linear: right-preconditioned restarted GMRES(maxl) on J_G d = -G, Arnoldi by classical
 //           Gram--Schmidt with one re-orthogonalisation (CGS2) in FP64, Givens least
 //           squares on the host, stop at ||r|| <= lin_rtol ||G||
@@ -144,21 +144,18 @@ __global__ void k_hist(long n, int q, const double* __restrict__ yn, const doubl
   if (i >= n) return;
   h[i] = q == 1 ? yn[i] : (4.0 / 3.0) * yn[i] - (1.0 / 3.0) * ym[i];
 }
-// G = y - gamma f - hist; b = -G; part0 <- sum (G w)^2, part1 <- sum y^2
+// G = y - gamma f - hist; b = -G; part0 <- sum G^2, part1 <- sum y^2
 __global__ void __launch_bounds__(kT) k_newton_res(long n, const double* __restrict__ y,
                                                    const double* __restrict__ f,
                                                    const double* __restrict__ hist,
-                                                   const double* __restrict__ yn, double gamma,
-                                                   double rtol, double atol,
-                                                   double* __restrict__ b,
+                                                   double gamma, double* __restrict__ b,
                                                    double* __restrict__ part) {
   double acc[2] = {0.0, 0.0};
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     const double yi = y[i];
     const double G = yi - gamma * f[i] - hist[i];
     b[i] = -G;
-    const double wg = G / (rtol * fabs(yn[i]) + atol);
-    acc[0] += wg * wg;
+    acc[0] += G * G;
     acc[1] += yi * yi;
   }
   block_reduce_store<2>(acc, 2, part);
@@ -379,22 +376,24 @@ extern "C" int fos_bdf_run(fos_ctx* c, double t0, double* y, const fos_bdf_opts*
     fos_launch(c, k_hist, nb(N), kT, N, q, wk.yn, wk.ym, wk.hist);
     FOS_CUDA(cudaMemcpyAsync(y, wk.yn, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
     bool conv = false;
+    double gtol = 0.0;
     for (int k = 0; k <= opts->max_newton; k++) {
       FOS_CUDA(cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream));
       int rc = fos_residual_launch(c, y, nullptr, nullptr, nullptr, wk.f, 0.0, 0.0, 0);
       if (rc) return rc;
       st.n_rhs++;
-      fos_launch(c, k_newton_res, kRedBlocks, kT, N, y, wk.f, wk.hist, wk.yn, gamma,
-                                                      opts->newton_rtol, opts->newton_atol, wk.b,
-                                                      wk.part);
+      fos_launch(c, k_newton_res, kRedBlocks, kT, N, (const double*)y, (const double*)wk.f,
+                 (const double*)wk.hist, gamma, wk.b, wk.part);
       if ((rc = dr.reduce(2, wk.sc))) return rc;
       FOS_CUDA(cudaMemcpyAsync(hb, wk.sc, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
       FOS_CUDA(cudaMemcpyAsync(c->h_scal, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
       FOS_CUDA(cudaStreamSynchronize(c->stream));
       if (*(int*)c->h_scal) { status = 2; break; }  // non-finite residual
-      const double gn = std::sqrt(hb[0] / (double)N);
-      st.last_gnorm = gn;
-      if (gn <= 1.0) { conv = true; break; }
+      // y_0 = y_n, so the first pass also gives ||y_n||
+      if (k == 0) gtol = opts->newton_rtol * std::sqrt(hb[1]) + opts->newton_atol * std::sqrt((double)N);
+      const double gn = std::sqrt(hb[0]);
+      st.last_gnorm = gn / gtol;
+      if (gn <= gtol) { conv = true; break; }
       if (k == opts->max_newton) break;
       if (k == 0 && opts->precond) {
         int jcur = 0;

@@ -447,7 +447,7 @@ extern "C" int fos_euler_psol_dev(fos_ctx* c, const double* r, double* z) {
     fos_set_error("fos_euler_psol_dev: bad arguments");
     return -1;
   }
-  if (!c->d_LU) {
+  if (!c->has_factor) {
     fos_set_error("fos_euler_psol_dev: no factorisation (call pset first)");
     return -2;
   }

@@ -93,6 +93,9 @@ struct fos_ctx {
   int* d_upd_ptr = nullptr;   // [nC+1] per row
   int3* d_upd = nullptr;      // updates
   int ilu_ierr = 0;
+  int ilu_colors = 0;            // > 0: ILU order is colour-major (FOS_ILU_COLOR)
+  bool has_factor = false;
+  std::vector<int> h_ilu_pos;     // ILU position of every internal row
   double* d_ilu_tmp = nullptr;  // [5*nC]
   fos_bdf_work* bdf = nullptr;  // driver workspace, kept between calls
   long n_launch = 0;            // kernels launched through fos_launch

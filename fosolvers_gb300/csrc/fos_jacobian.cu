@@ -43,10 +43,8 @@ __device__ __forceinline__ void load_prim(const double* __restrict__ W, int c, P
 
 // eulerNFJ entry (a, b) -- normal flux Jacobian dF.n/dU
 __device__ __forceinline__ double nfj(int a, int b, const double n[3], const double u[3], double H,
-                                      double g) {
+                                      double g, double v2, double vn) {
   const double g1 = g - 1.0;
-  const double v2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
-  const double vn = u[0] * n[0] + u[1] * n[1] + u[2] * n[2];
   if (a == 0) return (b >= 1 && b <= 3) ? n[b - 1] : 0.0;
   if (a == 4) {
     if (b == 0) return (0.5 * g1 * v2 - H) * vn;
@@ -140,19 +138,23 @@ __global__ void __launch_bounds__(kT) k_jac_face(int nFi, int nF, int nC,
   double Ab[25];
   anfj(n, ua, Ha, ca, g, Ab);
   const double uL[3] = {L.u, L.v, L.w}, uR[3] = {R.u, R.v, R.w};
+  const double v2L = uL[0] * uL[0] + uL[1] * uL[1] + uL[2] * uL[2];
+  const double vnL = uL[0] * n[0] + uL[1] * n[1] + uL[2] * n[2];
+  const double v2R = uR[0] * uR[0] + uR[1] * uR[1] + uR[2] * uR[2];
+  const double vnR = uR[0] * n[0] + uR[1] * n[1] + uR[2] * n[2];
   const double h = 0.5 * aP;
   if (f < nFi) {
     double* oLR = J + 25 * (size_t)fslot[2 * f];      // block (L, R) = JacP(1:5,6:10)
     double* oRL = J + 25 * (size_t)fslot[2 * f + 1];  // block (R, L) = JacP(6:10,1:5)
     for (int a = 0; a < 5; a++)
       for (int b = 0; b < 5; b++) {
-        oLR[5 * a + b] = -h * (nfj(a, b, n, uR, R.H, g) - Ab[5 * a + b]);
-        oRL[5 * a + b] = h * (nfj(a, b, n, uL, L.H, g) + Ab[5 * a + b]);
+        oLR[5 * a + b] = -h * (nfj(a, b, n, uR, R.H, g, v2R, vnR) - Ab[5 * a + b]);
+        oRL[5 * a + b] = h * (nfj(a, b, n, uL, L.H, g, v2L, vnL) + Ab[5 * a + b]);
       }
   } else {
     double* d = Jb + 25 * (size_t)(f - nFi);  // boundary pair's diagonal term
     for (int a = 0; a < 5; a++)
-      for (int b = 0; b < 5; b++) d[5 * a + b] = -h * (nfj(a, b, n, uL, L.H, g) + Ab[5 * a + b]);
+      for (int b = 0; b < 5; b++) d[5 * a + b] = -h * (nfj(a, b, n, uL, L.H, g, v2L, vnL) + Ab[5 * a + b]);
   }
 }
 
@@ -185,53 +187,29 @@ __global__ void __launch_bounds__(kT) k_jac_diag(int nC, int nFi, const int* __r
   for (int k = 0; k < 25; k++) dst[k] = D[k];
 }
 
-// LU = P = I - gamma/v J
-__global__ void k_ilu_copy(int nC, const int* __restrict__ rowptr, const int* __restrict__ diag,
-                           const double* __restrict__ invV, double gamma,
-                           const double* __restrict__ J, double* __restrict__ LU) {
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long nnz25 = 25L * rowptr[nC];
-  if (t >= nnz25) return;
-  const int slot = (int)(t / 25), k = (int)(t % 25);
-  // row of the slot by binary search
-  int lo = 0, hi = nC;
-  while (hi - lo > 1) {
-    int mid = (lo + hi) >> 1;
-    if (rowptr[mid] <= slot) lo = mid; else hi = mid;
-  }
-  const double s = gamma * invV[lo];
-  double val = -s * J[t];
-  if (slot == diag[lo] && (k / 5) == (k % 5)) val += 1.0;
-  LU[t] = val;
-}
-
-__device__ __forceinline__ void ld25(const double* __restrict__ p, double a[25]) {
+// invert a 5x5 block in place (Gauss--Jordan, partial pivoting); false on a zero pivot
+template <typename T>
+__device__ bool inv5(T a[25]) {
+  T b[25];
 #pragma unroll
-  for (int k = 0; k < 25; k++) a[k] = p[k];
-}
-
-// invert a 5x5 block in place (Gauss--Jordan, partial pivoting); returns false on a zero pivot
-__device__ bool inv5(double a[25]) {
-  double b[25];
-#pragma unroll
-  for (int k = 0; k < 25; k++) b[k] = (k / 5 == k % 5) ? 1.0 : 0.0;
+  for (int k = 0; k < 25; k++) b[k] = (k / 5 == k % 5) ? T(1) : T(0);
   for (int col = 0; col < 5; col++) {
     int piv = col;
-    double best = fabs(a[5 * col + col]);
+    T best = fabs(a[5 * col + col]);
     for (int rr = col + 1; rr < 5; rr++)
       if (fabs(a[5 * rr + col]) > best) { best = fabs(a[5 * rr + col]); piv = rr; }
-    if (!(best > 0.0)) return false;
+    if (!(best > T(0))) return false;
     if (piv != col)
       for (int k = 0; k < 5; k++) {
-        double t = a[5 * col + k]; a[5 * col + k] = a[5 * piv + k]; a[5 * piv + k] = t;
+        T t = a[5 * col + k]; a[5 * col + k] = a[5 * piv + k]; a[5 * piv + k] = t;
         t = b[5 * col + k]; b[5 * col + k] = b[5 * piv + k]; b[5 * piv + k] = t;
       }
-    const double ip = 1.0 / a[5 * col + col];
+    const T ip = T(1) / a[5 * col + col];
     for (int k = 0; k < 5; k++) { a[5 * col + k] *= ip; b[5 * col + k] *= ip; }
     for (int rr = 0; rr < 5; rr++) {
       if (rr == col) continue;
-      const double f = a[5 * rr + col];
-      if (f == 0.0) continue;
+      const T f = a[5 * rr + col];
+      if (f == T(0)) continue;
       for (int k = 0; k < 5; k++) { a[5 * rr + k] -= f * a[5 * col + k]; b[5 * rr + k] -= f * b[5 * col + k]; }
     }
   }
@@ -240,42 +218,49 @@ __device__ bool inv5(double a[25]) {
   return true;
 }
 
-// one level of the block ILU(0) factorisation: thread per row
-__global__ void __launch_bounds__(kT) k_ilu_factor_level(int n, const int* __restrict__ rows,
-                                                         const int* __restrict__ upd_ptr,
-                                                         const int3* __restrict__ upd,
-                                                         const int* __restrict__ diag,
-                                                         double* __restrict__ LU,
-                                                         int* __restrict__ ierr) {
+// One level of the block ILU(0) factorisation, one thread per block row i:
+//   LU_i* = P_i* = delta - gamma/v_i J_i*          (copy of the row, fused)
+//   for k in lower(i) (ILU order): LU_ik = LU_ik inv(D_k); LU_ij -= LU_ik LU_kj (j in row i)
+//   D_i = LU_ii -> stored inverted
+// Rows of one level only read finished rows of earlier levels and write their own row.
+template <typename TF>
+__global__ void __launch_bounds__(kT) k_ilu_factor_level(
+    int n, const int* __restrict__ rows, const int* __restrict__ rowptr,
+    const int* __restrict__ diag, const double* __restrict__ invV, double gamma,
+    const double* __restrict__ J, const int* __restrict__ upd_ptr, const int3* __restrict__ upd,
+    TF* __restrict__ LU, int* __restrict__ ierr) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   const int i = rows[t];
+  const double s = gamma * invV[i];
+  for (int sl = rowptr[i]; sl < rowptr[i + 1]; sl++) {
+    const double* src = J + 25 * (size_t)sl;
+    TF* dst = LU + 25 * (size_t)sl;
+    const bool dg = sl == diag[i];
+#pragma unroll
+    for (int k = 0; k < 25; k++) dst[k] = (TF)(((dg && k / 5 == k % 5) ? 1.0 : 0.0) - s * src[k]);
+  }
   for (int o = upd_ptr[i]; o < upd_ptr[i + 1]; o++) {
     const int3 op = upd[o];
-    double A[25], B[25];
-    ld25(LU + 25 * (size_t)op.x, A);
-    ld25(LU + 25 * (size_t)op.y, B);
-    if (op.z < 0) {  // L_ik = A_ik * inv(D_k)
-      double* dst = LU + 25 * (size_t)op.x;
-      for (int a = 0; a < 5; a++)
-        for (int b = 0; b < 5; b++) {
-          double s = 0.0;
-          for (int k = 0; k < 5; k++) s += A[5 * a + k] * B[5 * k + b];
-          dst[5 * a + b] = s;
-        }
-    } else {  // A_ij -= L_ik U_kj
-      double* dst = LU + 25 * (size_t)op.z;
-      for (int a = 0; a < 5; a++)
-        for (int b = 0; b < 5; b++) {
-          double s = dst[5 * a + b];
-          for (int k = 0; k < 5; k++) s -= A[5 * a + k] * B[5 * k + b];
-          dst[5 * a + b] = s;
-        }
-    }
+    TF A[25], B[25];
+#pragma unroll
+    for (int k = 0; k < 25; k++) { A[k] = LU[25 * (size_t)op.x + k]; B[k] = LU[25 * (size_t)op.y + k]; }
+    TF* dst = LU + 25 * (size_t)(op.z < 0 ? op.x : op.z);
+#pragma unroll
+    for (int a = 0; a < 5; a++)
+#pragma unroll
+      for (int b = 0; b < 5; b++) {
+        TF acc = op.z < 0 ? TF(0) : dst[5 * a + b];
+        TF p = 0;
+#pragma unroll
+        for (int k = 0; k < 5; k++) p += A[5 * a + k] * B[5 * k + b];
+        dst[5 * a + b] = op.z < 0 ? p : acc - p;
+      }
   }
-  double D[25];
-  double* dd = LU + 25 * (size_t)diag[i];
-  ld25(dd, D);
+  TF D[25];
+  TF* dd = LU + 25 * (size_t)diag[i];
+#pragma unroll
+  for (int k = 0; k < 25; k++) D[k] = dd[k];
   if (!inv5(D)) {
     atomicMin(ierr, i + 1);
     return;
@@ -284,74 +269,49 @@ __global__ void __launch_bounds__(kT) k_ilu_factor_level(int n, const int* __res
   for (int k = 0; k < 25; k++) dd[k] = D[k];
 }
 
-__global__ void k_to_f32(long n, const double* __restrict__ a, float* __restrict__ b) {
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < n) b[t] = (float)a[t];
-}
-
-// forward sweep of one level: y_i = r_i - sum_{k<i} L_ik y_k  (unit block diagonal)
-template <typename TF>
-__global__ void __launch_bounds__(kT) k_ilu_fwd(int n, int nC, const int* __restrict__ rows,
-                                                const int* __restrict__ rowptr,
-                                                const int* __restrict__ col,
-                                                const int* __restrict__ diag,
-                                                const TF* __restrict__ LU,
-                                                const double* __restrict__ r,
-                                                double* __restrict__ yv) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  const int i = rows[t];
-  TF acc[5];
+// Triangular sweeps, five lanes per block row (lane a owns component a and reads row a
+// of every 5x5 block: 40 contiguous bytes per lane, 200 per row).
+//   forward:  y_i = r_i - sum_{k in lower(i)} L_ik y_k           (unit block diagonal)
+//   backward: z_i = inv(D_i) (y_i - sum_{j in upper(i)} U_ij z_j)
+template <typename TF, bool FWD>
+__global__ void __launch_bounds__(kT) k_ilu_sweep(int n, int nC, const int* __restrict__ rows,
+                                                  const int* __restrict__ rowptr,
+                                                  const int* __restrict__ col,
+                                                  const int* __restrict__ diag,
+                                                  const TF* __restrict__ LU,
+                                                  const double* __restrict__ in,
+                                                  double* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int sub = lane / 5, a = lane - 5 * sub;  // 6 rows per warp, lanes 30, 31 idle
+  const int t = (blockIdx.x * blockDim.x + threadIdx.x) / 32 * 6 + sub;
+  const bool active = sub < 6 && t < n;
+  const int i = active ? rows[t] : 0;
+  TF acc = active ? (TF)in[(size_t)a * nC + i] : TF(0);
+  if (active) {
+    const int s0 = FWD ? rowptr[i] : diag[i] + 1;
+    const int s1 = FWD ? diag[i] : rowptr[i + 1];
+    for (int s = s0; s < s1; s++) {
+      const int k = col[s];
+      const TF* B = LU + 25 * (size_t)s + 5 * a;
 #pragma unroll
-  for (int q = 0; q < 5; q++) acc[q] = (TF)r[(size_t)q * nC + i];
-  for (int s = rowptr[i]; s < diag[i]; s++) {
-    const int k = col[s];
-    TF yk[5];
-#pragma unroll
-    for (int q = 0; q < 5; q++) yk[q] = (TF)yv[(size_t)q * nC + k];
-    const TF* B = LU + 25 * (size_t)s;
-#pragma unroll
-    for (int a = 0; a < 5; a++)
-#pragma unroll
-      for (int b = 0; b < 5; b++) acc[a] -= B[5 * a + b] * yk[b];
+      for (int b = 0; b < 5; b++) acc -= __ldg(B + b) * (TF)out[(size_t)b * nC + k];
+    }
   }
-#pragma unroll
-  for (int q = 0; q < 5; q++) yv[(size_t)q * nC + i] = (double)acc[q];
-}
-
-// backward sweep of one level: z_i = inv(D_i) (y_i - sum_{j>i} U_ij z_j)
-template <typename TF>
-__global__ void __launch_bounds__(kT) k_ilu_bwd(int n, int nC, const int* __restrict__ rows,
-                                                const int* __restrict__ rowptr,
-                                                const int* __restrict__ col,
-                                                const int* __restrict__ diag,
-                                                const TF* __restrict__ LU,
-                                                const double* __restrict__ yv,
-                                                double* __restrict__ z) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  const int i = rows[t];
-  TF acc[5];
-#pragma unroll
-  for (int q = 0; q < 5; q++) acc[q] = (TF)yv[(size_t)q * nC + i];
-  for (int s = diag[i] + 1; s < rowptr[i + 1]; s++) {
-    const int j = col[s];
-    TF zj[5];
-#pragma unroll
-    for (int q = 0; q < 5; q++) zj[q] = (TF)z[(size_t)q * nC + j];
-    const TF* B = LU + 25 * (size_t)s;
-#pragma unroll
-    for (int a = 0; a < 5; a++)
-#pragma unroll
-      for (int b = 0; b < 5; b++) acc[a] -= B[5 * a + b] * zj[b];
+  if (FWD) {
+    if (active) out[(size_t)a * nC + i] = (double)acc;
+    return;
   }
-  const TF* Di = LU + 25 * (size_t)diag[i];
+  // z_i = inv(D_i) acc: exchange the five components of the row through shuffles
+  TF comp[5];
+  const int base = lane - a;
 #pragma unroll
-  for (int a = 0; a < 5; a++) {
-    TF s = 0;
+  for (int b = 0; b < 5; b++) comp[b] = __shfl_sync(0xffffffffu, acc, base + b < 32 ? base + b : 0);
+  if (active) {
+    const TF* D = LU + 25 * (size_t)diag[i] + 5 * a;
+    TF z = 0;
 #pragma unroll
-    for (int b = 0; b < 5; b++) s += Di[5 * a + b] * acc[b];
-    z[(size_t)a * nC + i] = (double)s;
+    for (int b = 0; b < 5; b++) z += __ldg(D + b) * comp[b];
+    out[(size_t)a * nC + i] = (double)z;
   }
 }
 
@@ -359,6 +319,7 @@ __global__ void __launch_bounds__(kT) k_ilu_bwd(int n, int nC, const int* __rest
 
 namespace {
 inline int nb(long n, int t = kT) { return (int)((n + t - 1) / t); }
+inline int nb_rows5(long rows) { return (int)((rows + 6 * (kT / 32) - 1) / (6 * (kT / 32))); }
 template <typename T>
 int up(T** dst, const std::vector<T>& v) {
   FOS_CUDA(cudaMalloc((void**)dst, std::max<size_t>(v.size(), 1) * sizeof(T)));
@@ -367,23 +328,61 @@ int up(T** dst, const std::vector<T>& v) {
 }
 }  // namespace
 
-// Block sparsity, level sets and factor update lists (once per context).
+// Block sparsity, ILU order, level sets and factor update lists (once per context).
+// Each block row holds its columns sorted by ILU position, so lower(i) = [rowptr, diag)
+// and upper(i) = (diag, rowptr+1) in the ILU order (identity = the internal RCM order;
+// FOS_ILU_COLOR = greedy colouring of the cell graph, colour-major).
 int fos_jac_setup(fos_ctx* c) {
   if (c->d_rowptr) return 0;
   const int nC = c->nC, nFi = c->nFi;
-  std::vector<std::vector<int>> nbr(nC);
+  std::vector<int> deg(nC + 1, 0);
   for (int f = 0; f < nFi; f++) {
-    nbr[c->h_faceL[f]].push_back(c->h_faceR[f]);
-    nbr[c->h_faceR[f]].push_back(c->h_faceL[f]);
+    deg[c->h_faceL[f] + 1]++;
+    deg[c->h_faceR[f] + 1]++;
   }
+  for (int i = 0; i < nC; i++) deg[i + 1] += deg[i];
+  std::vector<int> adj(deg[nC]);
+  {
+    std::vector<int> pos(deg.begin(), deg.end() - 1);
+    for (int f = 0; f < nFi; f++) {
+      adj[pos[c->h_faceL[f]]++] = c->h_faceR[f];
+      adj[pos[c->h_faceR[f]]++] = c->h_faceL[f];
+    }
+  }
+  // ILU position of every internal row
+  std::vector<int> ipos(nC);
+  c->ilu_colors = 0;
+  if (c->flags & FOS_ILU_COLOR) {
+    std::vector<int> color(nC, -1);
+    int ncol = 0;
+    for (int i = 0; i < nC; i++) {
+      unsigned used = 0;
+      for (int e = deg[i]; e < deg[i + 1]; e++)
+        if (color[adj[e]] >= 0 && color[adj[e]] < 32) used |= 1u << color[adj[e]];
+      int k = 0;
+      while (used & (1u << k)) k++;
+      color[i] = k;
+      ncol = std::max(ncol, k + 1);
+    }
+    std::vector<int> cnt(ncol + 1, 0);
+    for (int i = 0; i < nC; i++) cnt[color[i] + 1]++;
+    for (int k = 0; k < ncol; k++) cnt[k + 1] += cnt[k];
+    for (int i = 0; i < nC; i++) ipos[i] = cnt[color[i]]++;
+    c->ilu_colors = ncol;
+  } else {
+    for (int i = 0; i < nC; i++) ipos[i] = i;
+  }
+  c->h_ilu_pos = ipos;
   std::vector<int> rowptr(nC + 1, 0), col, diag(nC);
   col.reserve((size_t)nC + 2 * (size_t)nFi);
+  std::vector<int> tmp;
   for (int i = 0; i < nC; i++) {
-    auto& v = nbr[i];
-    v.push_back(i);
-    std::sort(v.begin(), v.end());
-    v.erase(std::unique(v.begin(), v.end()), v.end());
-    for (int j : v) {
+    tmp.assign(adj.begin() + deg[i], adj.begin() + deg[i + 1]);
+    tmp.push_back(i);
+    std::sort(tmp.begin(), tmp.end());
+    tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+    std::sort(tmp.begin(), tmp.end(), [&](int a, int b) { return ipos[a] < ipos[b]; });
+    for (int j : tmp) {
       if (j == i) diag[i] = (int)col.size();
       col.push_back(j);
     }
@@ -391,25 +390,29 @@ int fos_jac_setup(fos_ctx* c) {
   }
   c->nnzb = (long)col.size();
   auto slot_of = [&](int i, int j) -> int {
-    auto b = col.begin() + rowptr[i], e = col.begin() + rowptr[i + 1];
-    auto it = std::lower_bound(b, e, j);
-    return (it != e && *it == j) ? (int)(it - col.begin()) : -1;
+    for (int s = rowptr[i]; s < rowptr[i + 1]; s++)
+      if (col[s] == j) return s;
+    return -1;
   };
   std::vector<int> fslot(2 * (size_t)nFi);
   for (int f = 0; f < nFi; f++) {
     fslot[2 * f] = slot_of(c->h_faceL[f], c->h_faceR[f]);
     fslot[2 * f + 1] = slot_of(c->h_faceR[f], c->h_faceL[f]);
   }
-  // level sets
+  // level sets in the ILU order
+  std::vector<int> order(nC);
+  for (int i = 0; i < nC; i++) order[ipos[i]] = i;
   std::vector<int> lf(nC, 0), lb(nC, 0);
   int nlf = 0, nlb = 0;
-  for (int i = 0; i < nC; i++) {
+  for (int q = 0; q < nC; q++) {
+    const int i = order[q];
     int l = 0;
     for (int s = rowptr[i]; s < diag[i]; s++) l = std::max(l, lf[col[s]] + 1);
     lf[i] = l;
     nlf = std::max(nlf, l + 1);
   }
-  for (int i = nC - 1; i >= 0; i--) {
+  for (int q = nC - 1; q >= 0; q--) {
+    const int i = order[q];
     int l = 0;
     for (int s = diag[i] + 1; s < rowptr[i + 1]; s++) l = std::max(l, lb[col[s]] + 1);
     lb[i] = l;
@@ -428,10 +431,11 @@ int fos_jac_setup(fos_ctx* c) {
   group(lb, nlb, c->lev_b, rows_b);
   c->ilu_nlev_f = nlf;
   c->ilu_nlev_b = nlb;
-  // factor update lists (IKJ order): for k in lower(i) ascending: scale L_ik, then
-  // A_ij -= L_ik U_kj for every j > k in row k that is also in row i's pattern
+  // factor update lists (IKJ): for k in lower(i) in ILU order: scale L_ik, then
+  // A_ij -= L_ik U_kj for every j in upper(k) that is also in row i
   std::vector<int> upd_ptr(nC + 1, 0);
   std::vector<int3> upd;
+  upd.reserve((size_t)nC * 8);
   for (int i = 0; i < nC; i++) {
     for (int s = rowptr[i]; s < diag[i]; s++) {
       const int k = col[s];
@@ -450,12 +454,13 @@ int fos_jac_setup(fos_ctx* c) {
       up(&c->d_upd_ptr, upd_ptr) || up(&c->d_upd, upd))
     return -100;
   FOS_CUDA(cudaMalloc((void**)&c->d_J, 25 * sizeof(double) * (size_t)c->nnzb));
-  FOS_CUDA(cudaMalloc((void**)&c->d_LU, 25 * sizeof(double) * (size_t)c->nnzb));
   FOS_CUDA(cudaMalloc((void**)&c->d_Jb, 25 * sizeof(double) * (size_t)std::max(c->nFb, 1)));
   FOS_CUDA(cudaMalloc((void**)&c->d_ilu_tmp, 5 * sizeof(double) * (size_t)nC));
   FOS_CUDA(cudaMalloc((void**)&c->d_ierr, sizeof(int)));
   if (c->flags & FOS_ILU_FP32)
     FOS_CUDA(cudaMalloc((void**)&c->d_LU32, 25 * sizeof(float) * (size_t)c->nnzb));
+  else
+    FOS_CUDA(cudaMalloc((void**)&c->d_LU, 25 * sizeof(double) * (size_t)c->nnzb));
   return 0;
 }
 
@@ -463,33 +468,37 @@ int fos_jac_assemble(fos_ctx* c, const double* y) {
   int rc = fos_prim_launch(c, y);
   if (rc) return rc;
   fos_launch(c, k_jac_face, nb(c->nF), kT, c->nFi, c->nF, c->nC, c->d_faceLR, c->d_faceNA,
-                                               c->d_W, y, c->d_fslot, c->d_bcT, c->d_bcP,
-                                               c->maxP, c->gamm, c->r, c->d_J, c->d_Jb);
-  fos_launch(c, k_jac_diag, nb(c->nC), kT, c->nC, c->nFi, c->d_crow, c->d_cent, c->d_fslot,
-                                               c->d_diag, c->d_Jb, c->d_J);
+             (const double*)c->d_W, y, (const int*)c->d_fslot, (const int*)c->d_bcT,
+             (const double*)c->d_bcP, c->maxP, c->gamm, c->r, c->d_J, c->d_Jb);
+  fos_launch(c, k_jac_diag, nb(c->nC), kT, c->nC, c->nFi, (const int*)c->d_crow,
+             (const int*)c->d_cent, (const int*)c->d_fslot, (const int*)c->d_diag,
+             (const double*)c->d_Jb, c->d_J);
   FOS_LAUNCH_CHECK();
   c->has_jac = true;
   return 0;
 }
 
 int fos_ilu_factor(fos_ctx* c, double gamma) {
-  const long n25 = 25L * c->nnzb;
-  fos_launch(c, k_ilu_copy, nb(n25, 256), 256, c->nC, c->d_rowptr, c->d_diag, c->d_invV,
-                                                   gamma, c->d_J, c->d_LU);
   const int big = 0x7fffffff;
   FOS_CUDA(cudaMemcpyAsync(c->d_ierr, &big, sizeof(int), cudaMemcpyHostToDevice, c->stream));
   for (int l = 0; l < c->ilu_nlev_f; l++) {
     const int n = c->lev_f[l + 1] - c->lev_f[l];
-    fos_launch(c, k_ilu_factor_level, nb(n), kT, n, c->d_lrows_f + c->lev_f[l], c->d_upd_ptr,
-                                                     c->d_upd, c->d_diag, c->d_LU, c->d_ierr);
+    const int* rows = c->d_lrows_f + c->lev_f[l];
+    if (c->flags & FOS_ILU_FP32)
+      fos_launch(c, k_ilu_factor_level<float>, nb(n), kT, n, rows, (const int*)c->d_rowptr,
+                 (const int*)c->d_diag, (const double*)c->d_invV, gamma, (const double*)c->d_J,
+                 (const int*)c->d_upd_ptr, (const int3*)c->d_upd, c->d_LU32, c->d_ierr);
+    else
+      fos_launch(c, k_ilu_factor_level<double>, nb(n), kT, n, rows, (const int*)c->d_rowptr,
+                 (const int*)c->d_diag, (const double*)c->d_invV, gamma, (const double*)c->d_J,
+                 (const int*)c->d_upd_ptr, (const int3*)c->d_upd, c->d_LU, c->d_ierr);
   }
   FOS_LAUNCH_CHECK();
-  if (c->flags & FOS_ILU_FP32)
-    fos_launch(c, k_to_f32, nb(n25, 256), 256, n25, c->d_LU, c->d_LU32);
   int* h = (int*)c->h_scal;
   FOS_CUDA(cudaMemcpyAsync(h, c->d_ierr, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   FOS_CUDA(cudaStreamSynchronize(c->stream));
   c->ilu_ierr = (*h == big) ? 0 : *h;  // 1-based internal row of the first zero pivot
+  c->has_factor = true;
   if (c->ilu_ierr) fos_set_error("block ILU(0): zero pivot");
   return 0;
 }
@@ -499,25 +508,27 @@ int fos_ilu_apply(fos_ctx* c, const double* r, double* z) {
   const bool f32 = (c->flags & FOS_ILU_FP32) != 0;
   for (int l = 0; l < c->ilu_nlev_f; l++) {
     const int n = c->lev_f[l + 1] - c->lev_f[l];
+    const int* rows = c->d_lrows_f + c->lev_f[l];
     if (f32)
-      fos_launch(c, k_ilu_fwd<float>, nb(n), kT, n, c->nC, c->d_lrows_f + c->lev_f[l],
-                                                    c->d_rowptr, c->d_col, c->d_diag, c->d_LU32,
-                                                    r, tmp);
+      fos_launch(c, k_ilu_sweep<float, true>, nb_rows5(n), kT, n, c->nC, rows,
+                 (const int*)c->d_rowptr, (const int*)c->d_col, (const int*)c->d_diag,
+                 (const float*)c->d_LU32, r, tmp);
     else
-      fos_launch(c, k_ilu_fwd<double>, nb(n), kT, n, c->nC, c->d_lrows_f + c->lev_f[l],
-                                                     c->d_rowptr, c->d_col, c->d_diag, c->d_LU,
-                                                     r, tmp);
+      fos_launch(c, k_ilu_sweep<double, true>, nb_rows5(n), kT, n, c->nC, rows,
+                 (const int*)c->d_rowptr, (const int*)c->d_col, (const int*)c->d_diag,
+                 (const double*)c->d_LU, r, tmp);
   }
   for (int l = 0; l < c->ilu_nlev_b; l++) {
     const int n = c->lev_b[l + 1] - c->lev_b[l];
+    const int* rows = c->d_lrows_b + c->lev_b[l];
     if (f32)
-      fos_launch(c, k_ilu_bwd<float>, nb(n), kT, n, c->nC, c->d_lrows_b + c->lev_b[l],
-                                                    c->d_rowptr, c->d_col, c->d_diag, c->d_LU32,
-                                                    tmp, z);
+      fos_launch(c, k_ilu_sweep<float, false>, nb_rows5(n), kT, n, c->nC, rows,
+                 (const int*)c->d_rowptr, (const int*)c->d_col, (const int*)c->d_diag,
+                 (const float*)c->d_LU32, (const double*)tmp, z);
     else
-      fos_launch(c, k_ilu_bwd<double>, nb(n), kT, n, c->nC, c->d_lrows_b + c->lev_b[l],
-                                                     c->d_rowptr, c->d_col, c->d_diag, c->d_LU,
-                                                     tmp, z);
+      fos_launch(c, k_ilu_sweep<double, false>, nb_rows5(n), kT, n, c->nC, rows,
+                 (const int*)c->d_rowptr, (const int*)c->d_col, (const int*)c->d_diag,
+                 (const double*)c->d_LU, (const double*)tmp, z);
   }
   FOS_LAUNCH_CHECK();
   return 0;
@@ -541,4 +552,13 @@ extern "C" long fos_euler_jac_copy(fos_ctx* c, int* rowptr, int* col, double* va
     }
   }
   return c->nnzb;
+}
+
+extern "C" int fos_ctx_ilu_order(const fos_ctx* c, int* old2pos) {
+  if (!c || !old2pos || c->h_ilu_pos.empty()) {
+    fos_set_error("fos_ctx_ilu_order: no factorisation set up yet");
+    return -1;
+  }
+  for (int o = 0; o < c->nC; o++) old2pos[o] = c->h_ilu_pos[c->old2new[o]];
+  return c->ilu_colors;
 }

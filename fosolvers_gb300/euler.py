@@ -141,6 +141,12 @@ class FOEuler:
         check(_lib.lib().fos_ctx_renumbering(self._h, iptr(o2n)), "fos_ctx_renumbering")
         return o2n
 
+    def ilu_order(self) -> np.ndarray:
+        """Position of every reference cell in the ILU(0) elimination order (after pset)."""
+        pos = np.zeros(self.nC, np.int32)
+        check(_lib.lib().fos_ctx_ilu_order(self._h, iptr(pos)), "fos_ctx_ilu_order")
+        return pos
+
     # ---------------------------------------------------------------- CVODE callbacks (host)
     def rhs(self, t: float, y: np.ndarray, ydot: np.ndarray) -> int:
         return check(_lib.lib().fos_euler_rhs(t, dptr(y), dptr(ydot), self._h), "rhs")

@@ -92,6 +92,9 @@ void fos_ctx_info(const fos_ctx* ctx, long* out);
 int fos_ctx_permute_dev(fos_ctx* ctx, const double* in, double* out, int dir);
 /* internal cell id of every reference cell (old2new, 0-based), length nC */
 int fos_ctx_renumbering(const fos_ctx* ctx, int* old2new);
+/* position of every reference cell in the ILU(0) elimination order (0-based), after the
+ * first pset; returns the number of colours (FOS_ILU_COLOR) or 0 (internal order) */
+int fos_ctx_ilu_order(const fos_ctx* ctx, int* old2pos);
 const char* fos_last_error(void);
 
 /* ------------------------------------------------------------------ CVODE callbacks (host) */
@@ -131,7 +134,7 @@ typedef struct {
   int order;          /* 1 = BDF1; 2 = BDF2 (first step BDF1) */
   int nsteps;
   double dt;
-  double newton_rtol; /* Newton: ||G(y)||_WRMS <= 1 with w = 1/(rtol |y_n| + atol) */
+  double newton_rtol; /* Newton: ||G(y)||_2 <= rtol ||y_n||_2 + atol sqrt(5 nC), FP64 */
   double newton_atol;
   int max_newton;
   int maxl;           /* (F)GMRES restart length */

@@ -360,6 +360,7 @@ struct oe_ctx {
   double *pa, *alu;
   int *pja, *pia, *jlu, *jluu, *iw;
   double *t1, *t2;
+  int* perm; /* ILU cell order: old -> new (NULL = natural) */
 };
 
 static double dot3(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
@@ -424,10 +425,18 @@ void oe_free(oe_ctx* c) {
   free(c->fu); free(c->fH); free(c->f1c); free(c->f2c); free(c->f3c);
   free(c->JacP); free(c->JacC); free(c->ju_); free(c->jH); free(c->jc);
   free(c->pa); free(c->pja); free(c->pia); free(c->alu); free(c->jlu); free(c->jluu); free(c->iw);
-  free(c->t1); free(c->t2);
+  free(c->t1); free(c->t2); free(c->perm);
   free(c);
 }
 void oe_set_threads(oe_ctx* c, int nthreads) { c->nthreads = nthreads < 1 ? 1 : nthreads; }
+void oe_set_ilu_order(oe_ctx* c, const int* old2new) {
+  free(c->perm);
+  c->perm = NULL;
+  if (!old2new) return;
+  c->perm = (int*)xcalloc(c->nC, sizeof(int));
+  memcpy(c->perm, old2new, sizeof(int) * c->nC);
+}
+static int pnew(const oe_ctx* c, int cell) { return c->perm ? c->perm[cell] : cell; }
 
 /* setBC (foeuler.f90:209-330); UDF variants are not supported (libmatheval absent) */
 static void oe_setBC(oe_ctx* c, const double* x) {
@@ -995,8 +1004,8 @@ static void oe_build_P(oe_ctx* c, double gamma) {
       for (int bI = 0; bI < nb; bI++)
         for (int b = 1; b <= 5; b++) {
           double jv = c->JacC[(a - 1) + 5 * ((size_t)(5 * blk[bI] + b - 1) + (size_t)ncol * cc)];
-          ir[q] = 5 * cc + a;
-          jcv[q] = 5 * (col[bI] - 1) + b;
+          ir[q] = 5 * pnew(c, cc) + a;
+          jcv[q] = 5 * pnew(c, col[bI] - 1) + b;
           av[q] = (blk[bI] == 0 && a == b ? 1.0 : 0.0) - s * jv;
           q++;
         }
@@ -1027,10 +1036,10 @@ int oe_psol(double t, const double* y, const double* fy, const double* r, double
   oe_ctx* c = (oe_ctx*)ud;
   const int nC = c->nC;
   for (int i = 0; i < nC; i++)
-    for (int a = 0; a < 5; a++) c->t1[5 * i + a] = r[a * nC + i];
+    for (int a = 0; a < 5; a++) c->t1[5 * pnew(c, i) + a] = r[a * nC + i];
   o_lusol(5 * nC, c->t1, c->t2, c->alu, c->jlu, c->jluu);
   for (int i = 0; i < nC; i++)
-    for (int a = 0; a < 5; a++) z[a * nC + i] = c->t2[5 * i + a];
+    for (int a = 0; a < 5; a++) z[a * nC + i] = c->t2[5 * pnew(c, i) + a];
   return 0;
 }
 int oe_pmat(const oe_ctx* c, const double** a, const int** ja, const int** ia) {
@@ -1047,7 +1056,7 @@ int oe_ilu_ierr(const oe_ctx* c) { return c->ierr; }
  *   J_G v ~ v - gamma (f(y + s v) - f(y))/s,  s = jv_eps (1 + ||y||_2)/||v||_2
  *   right-preconditioned restarted GMRES(maxl), classical Gram-Schmidt with one
  *   re-orthogonalisation (CGS2), Givens least squares, stop at ||r|| <= lin_rtol ||b||
- *   Newton stops when ||G(y_k)||_WRMS <= 1, weights 1/(rtol |y_n| + atol). */
+ *   Newton stops when ||G(y_k)||_2 <= rtol ||y_n||_2 + atol sqrt(n) (FP64 residual norm). */
 typedef struct {
   int n;
   o_rhs_fn f;
@@ -1177,14 +1186,6 @@ void o_bdf_defaults(o_bdf_opts* o) {
   o->jv_eps = 1.4901161193847656e-08; o->use_prec = 1;
 }
 
-static double wrms(int n, const double* v, const double* yref, double rtol, double atol) {
-  double s = 0.0;
-  for (int i = 0; i < n; i++) {
-    double w = v[i] / (rtol * fabs(yref[i]) + atol);
-    s += w * w;
-  }
-  return sqrt(s / n);
-}
 
 int o_bdf_run(int n, o_rhs_fn rhs, o_pset_fn pset, o_psol_fn psol, void* ud, double t0,
               double* y, const o_bdf_opts* opts, o_bdf_stats* st) {
@@ -1210,15 +1211,16 @@ int o_bdf_run(int n, o_rhs_fn rhs, o_pset_fn pset, o_psol_fn psol, void* ud, dou
     }
     double tn = t + opts->dt;
     memcpy(y, yn, sizeof(double) * n); /* predictor: previous state */
+    const double gtol = opts->newton_rtol * sqrt(vdot(n, yn, yn)) + opts->newton_atol * sqrt((double)n);
     int conv = 0;
     for (int k = 0; k <= opts->max_newton; k++) {
       int rc = rhs(tn, y, f, ud);
       st->n_rhs++;
       if (rc) { status = 2; break; }
       for (int i = 0; i < n; i++) G[i] = y[i] - gamma * f[i] - hist[i];
-      double gn = wrms(n, G, yn, opts->newton_rtol, opts->newton_atol);
-      st->last_gnorm = gn;
-      if (gn <= 1.0) { conv = 1; break; }
+      double gn = sqrt(vdot(n, G, G));
+      st->last_gnorm = gn / gtol;
+      if (gn <= gtol) { conv = 1; break; }
       if (k == opts->max_newton) break;
       if (k == 0 && opts->use_prec) {
         int jcur = 0;

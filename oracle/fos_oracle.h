@@ -67,6 +67,10 @@ void oe_free(oe_ctx* c);
 /* number of OpenMP threads used by oe_rhs: 1 = reference pair order, serial (parity mode);
  * >1 = parallel pair loop with atomic scatter, the reference's own OpenMP structure */
 void oe_set_threads(oe_ctx* c, int nthreads);
+/* cell order of the ILU(0) factorisation in pset/psol: old2new[c] = position of reference
+ * cell c (0-based); NULL = the reference's natural order.  ILU(0) depends on the order, so
+ * parity with a renumbered GPU factorisation uses the GPU's order here. */
+void oe_set_ilu_order(oe_ctx* c, const int* old2new);
 /* the three CVODE callbacks (foeuler.f90:349-437) with N_Vector data as raw arrays;
  * ud is the oe_ctx*.  pset assembles findEulerJac, P = I - gamma*diag(1/v)*JacC in
  * interleaved (cell-major) scalar COO, coocsr, sorted rows, ilu0; psol = lusol. */
@@ -107,7 +111,7 @@ typedef struct {
   int order;          /* 1 = BDF1, 2 = BDF2 (first step BDF1) */
   double dt;
   int nsteps;
-  double newton_rtol; /* Newton: ||G(y)||_WRMS <= 1 with w = 1/(rtol*|y_n|+atol) */
+  double newton_rtol; /* Newton: ||G(y)||_2 <= rtol*||y_n||_2 + atol*sqrt(n) */
   double newton_atol;
   int max_newton;
   int maxl;           /* GMRES restart length */

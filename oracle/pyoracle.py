@@ -51,6 +51,7 @@ _SIGS = {
                      C.c_int, _ip, _dp, C.c_int, C.c_double, C.c_double, _dp, _dp, _dp]),
     "oe_free": (None, [_vp]),
     "oe_set_threads": (None, [_vp, C.c_int]),
+    "oe_set_ilu_order": (None, [_vp, _ip]),
     "oe_rhs": (C.c_int, [C.c_double, _dp, _dp, _vp]),
     "oe_pset": (C.c_int, [C.c_double, _dp, _dp, C.c_int, _ip, C.c_double, _vp]),
     "oe_psol": (C.c_int, [C.c_double, _dp, _dp, _dp, _dp, C.c_double, C.c_double, C.c_int, _vp]),
@@ -149,6 +150,14 @@ class Euler:
 
     def set_threads(self, n):
         lib().oe_set_threads(self.h, int(n))
+
+    def set_ilu_order(self, old2new):
+        """ILU(0) cell order (old -> new, 0-based); None = natural reference order."""
+        if old2new is None:
+            lib().oe_set_ilu_order(self.h, None)
+        else:
+            self._perm = np.ascontiguousarray(old2new, np.int32)
+            lib().oe_set_ilu_order(self.h, ip(self._perm))
 
     def close(self):
         if self.h:

@@ -21,6 +21,7 @@ class Case:
         self.flags = flags
         self._oracle = None
         self._gpu = None
+        self._gpu_has_factor = False
 
     @property
     def oracle(self) -> O.Euler:
@@ -35,6 +36,14 @@ class Case:
             self._gpu = FOEuler(self.grid, self.iBC, self.wl.bc_type, self.wl.bc_param,
                                 self.wl.gamm, self.wl.r, flags=self.flags)
         return self._gpu
+
+    def match_ilu_order(self):
+        """ILU(0) depends on the cell order: factor the oracle in the GPU's order (the GPU
+        sets its order up at the first pset, so run one on the initial state first)."""
+        if not self._gpu_has_factor:
+            self.gpu.pset(0.0, self.y0, None, 0, 1e-3)
+            self._gpu_has_factor = True
+        self.oracle.set_ilu_order(self.gpu.ilu_order())
 
     def oracle_rhs(self, y):
         f = np.zeros_like(y)

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from fosolvers_gb300 import mesh as M
-from fosolvers_gb300.euler import FLUX_FP32, ILU_FP32
+from fosolvers_gb300.euler import FLUX_FP32, ILU_COLOR, ILU_FP32
 from helpers import Case, rel_err
 from oracle import pyoracle as O
 
@@ -19,6 +19,7 @@ def oracle_run(c: Case, nsteps=None, use_prec=1):
     wl = c.wl
     opts = O.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=nsteps or wl.nsteps, use_prec=use_prec)
     y = c.y0.copy()
+    c.match_ilu_order()
     rhs, pset, psol = c.oracle.callbacks()
     rc, st = O.bdf_run(c.N, rhs, pset, psol, c.oracle.h, y, opts)
     assert rc == 0, st
@@ -51,8 +52,9 @@ def test_sod16_twenty_steps_matches_oracle(cuda):
     assert err <= 1e-10
 
 
-def test_sine_bdf2_matches_oracle(cuda):
-    c = Case(M.make_workload("sine96", scale=10, seed=2))
+@pytest.mark.parametrize("flags", [0, ILU_COLOR])
+def test_sine_bdf2_matches_oracle(cuda, flags):
+    c = Case(M.make_workload("sine96", scale=10, seed=2), flags=flags)
     y_ref, st_ref = oracle_run(c, nsteps=5)
     y, st = gpu_run(c, nsteps=5)
     assert rel_err(y, y_ref) <= 1e-10
@@ -88,10 +90,11 @@ def test_dropin_callbacks_under_reference_driver(cuda):
     assert rel_err(y, y_ref) <= 1e-10
 
 
-def test_fp32_form_within_1e6(cuda):
-    """FP32 Roe flux + FP32 ILU(0) apply, FP64 Newton/orthogonalisation: state within 1e-6
-    of the FP64 oracle after the Sod workload's 20 steps."""
-    c = Case(M.make_workload("sod16"), flags=FLUX_FP32 | ILU_FP32)
+@pytest.mark.parametrize("extra", [0, ILU_COLOR])
+def test_fp32_form_within_1e6(cuda, extra):
+    """FP32 Roe flux + FP32 ILU(0) factors/apply, FP64 Newton/orthogonalisation: state within
+    1e-6 of the FP64 oracle after the Sod workload's 20 steps."""
+    c = Case(M.make_workload("sod16"), flags=FLUX_FP32 | ILU_FP32 | extra)
     y_ref, _ = oracle_run(c)
     y, st = gpu_run(c)
     err = rel_err(y, y_ref)

@@ -4,21 +4,24 @@ J: every 5x5 block of the GPU block-CSR (internal order) equals the oracle's Jac
 (findEulerJac, reference order) within 1e-12 of the largest entry.  ILU: z = P^-1 r
 from the GPU's level-scheduled block ILU(0) equals SPARSKIT ilu0 + lusol on the scalar
 interleaved matrix within 1e-10 (block ILU(0) with dense diagonal blocks is scalar ILU(0)
-of the interleaved matrix)."""
+of the interleaved matrix), with the oracle factoring in the GPU's cell order (ILU(0)
+depends on the order)."""
 import numpy as np
 import pytest
 
 from fosolvers_gb300 import mesh as M
-from fosolvers_gb300.euler import ILU_FP32
+from fosolvers_gb300.euler import ILU_COLOR, ILU_FP32
 from helpers import Case, perturbed, rel_err
 
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(scope="module", params=["sine8", "bump16"])
+@pytest.fixture(scope="module", params=["sine8", "bump16", "sine8-colour"])
 def case(request, cuda):
     if request.param == "sine8":
         return Case(M.make_workload("sine96", scale=8, seed=1))
+    if request.param == "sine8-colour":
+        return Case(M.make_workload("sine96", scale=8, seed=1), flags=ILU_COLOR)
     return Case(M.make_workload("bump192", scale=16))
 
 
@@ -39,8 +42,7 @@ def test_jacobian_blocks_match_oracle(case):
         blocks = [(cell, 0)] + [(k - 1, j + 1) for j, k in enumerate(c.grid.neib[cell]) if 1 <= k <= c.nC]
         assert len(blocks) == len(cols)
         for other, j in blocks:
-            s = rowptr[i] + int(np.searchsorted(cols, o2n[other]))
-            assert cols[s - rowptr[i]] == o2n[other]
+            s = rowptr[i] + list(cols).index(o2n[other])
             want = ref[cell, 5 * j:5 * j + 5, :].T
             assert np.abs(val[s] - want).max() <= 1e-12 * scale
             nblk += 1
@@ -51,6 +53,7 @@ def test_ilu_apply_matches_sparskit(case):
     c = case
     y = perturbed(c.y0, c.nC, 4)
     gamma = 5e-3
+    c.match_ilu_order()
     assert c.oracle.pset(0.0, y, None, 0, gamma) == (0, 1)
     rc, _ = c.gpu.pset(0.0, y, None, 0, gamma)
     assert rc == 0
@@ -64,12 +67,15 @@ def test_ilu_apply_matches_sparskit(case):
         assert rel_err(z, z_ref) <= 1e-10
     info = c.gpu.info()
     assert info["nlev_fwd"] >= 2 and info["nlev_bwd"] >= 2
+    if c.flags & ILU_COLOR:
+        assert info["nlev_fwd"] <= 6 and info["nlev_bwd"] <= 6
 
 
 def test_pset_jok_reuses_jacobian(case):
     """jok = 1 keeps J and only re-scales by the new gamma (CVODE pset contract)."""
     c = case
     y = perturbed(c.y0, c.nC, 6)
+    c.match_ilu_order()
     c.gpu.pset(0.0, y, None, 0, 1e-3)
     rc, jcur = c.gpu.pset(0.0, 2.0 * y, None, 1, 2e-3)
     assert rc == 0 and jcur == 0
@@ -85,6 +91,7 @@ def test_pset_jok_reuses_jacobian(case):
 def test_fp32_ilu_apply(cuda):
     c = Case(M.make_workload("sine96", scale=8, seed=1), flags=ILU_FP32)
     y = perturbed(c.y0, c.nC, 4)
+    c.match_ilu_order()
     c.oracle.pset(0.0, y, None, 0, 5e-3)
     c.gpu.pset(0.0, y, None, 0, 5e-3)
     r = np.random.default_rng(2).normal(size=c.N)
