@@ -52,52 +52,52 @@ __device__ __forceinline__ void block_reduce_store(double (&acc)[NV], int nv, do
   }
 }
 
-// h[l] = V_l . w,  l < nv
-__global__ void __launch_bounds__(kT) k_mdot(long n, int nv, const double* __restrict__ V,
-                                             long ldv, const double* __restrict__ w,
+// h[l] = V_l . w for l < NV (NV fixed at compile time: accumulators stay in registers)
+template <int NV>
+__global__ void __launch_bounds__(kT) k_mdot(long n, const double* __restrict__ V, long ldv,
+                                             const double* __restrict__ w,
                                              double* __restrict__ part) {
-  double acc[kMaxVec];
+  double acc[NV];
 #pragma unroll
-  for (int l = 0; l < kMaxVec; l++) acc[l] = 0.0;
+  for (int l = 0; l < NV; l++) acc[l] = 0.0;
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     const double wi = w[i];
 #pragma unroll
-    for (int l = 0; l < kMaxVec; l++)
-      if (l < nv) acc[l] += V[(size_t)l * ldv + i] * wi;
+    for (int l = 0; l < NV; l++) acc[l] += V[(size_t)l * ldv + i] * wi;
   }
-  block_reduce_store<kMaxVec>(acc, nv, part);
+  block_reduce_store<NV>(acc, NV, part);
 }
 
-// w -= sum_l h[l] V_l ; then part <- V_l . w (mode 0) or ||w||^2 (mode 1)
-__global__ void __launch_bounds__(kT) k_update(long n, int nv, const double* __restrict__ V,
-                                               long ldv, const double* __restrict__ h,
-                                               double* __restrict__ w, int mode,
+// w -= sum_l h[l] V_l ; then part <- V_l . w (MODE 0, CGS2 second pass) or ||w||^2 (MODE 1)
+template <int NV, int MODE>
+__global__ void __launch_bounds__(kT) k_update(long n, const double* __restrict__ V, long ldv,
+                                               const double* __restrict__ h,
+                                               double* __restrict__ w,
                                                double* __restrict__ part) {
-  __shared__ double hs[kMaxVec];
-  if (threadIdx.x < kMaxVec) hs[threadIdx.x] = threadIdx.x < nv ? h[threadIdx.x] : 0.0;
+  __shared__ double hs[NV];
+  if (threadIdx.x < NV) hs[threadIdx.x] = h[threadIdx.x];
   __syncthreads();
-  double acc[kMaxVec];
+  constexpr int NA = MODE == 0 ? NV : 1;
+  double acc[NA];
 #pragma unroll
-  for (int l = 0; l < kMaxVec; l++) acc[l] = 0.0;
+  for (int l = 0; l < NA; l++) acc[l] = 0.0;
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    double vv[kMaxVec];
+    double vv[NV];
     double wi = w[i];
 #pragma unroll
-    for (int l = 0; l < kMaxVec; l++)
-      if (l < nv) {
-        vv[l] = V[(size_t)l * ldv + i];
-        wi -= hs[l] * vv[l];
-      }
+    for (int l = 0; l < NV; l++) {
+      vv[l] = V[(size_t)l * ldv + i];
+      wi -= hs[l] * vv[l];
+    }
     w[i] = wi;
-    if (mode == 0) {
+    if (MODE == 0) {
 #pragma unroll
-      for (int l = 0; l < kMaxVec; l++)
-        if (l < nv) acc[l] += vv[l] * wi;
+      for (int l = 0; l < NA; l++) acc[l] += vv[l] * wi;
     } else {
       acc[0] += wi * wi;
     }
   }
-  block_reduce_store<kMaxVec>(acc, mode == 0 ? nv : 1, part);
+  block_reduce_store<NA>(acc, NA, part);
 }
 
 // out[l] = sum of part[l * np ...]
@@ -238,6 +238,37 @@ struct Driver {
     FOS_LAUNCH_CHECK();
     return 0;
   }
+  int mdot(int nv, const double* V, long ldv, const double* w) {
+    switch (nv) {
+#define FOS_MDOT(K) \
+  case K: fos_launch(c, k_mdot<K>, kRedBlocks, kT, wk.N, V, ldv, w, wk.part); break;
+      FOS_MDOT(1) FOS_MDOT(2) FOS_MDOT(3) FOS_MDOT(4) FOS_MDOT(5) FOS_MDOT(6) FOS_MDOT(7)
+      FOS_MDOT(8) FOS_MDOT(9) FOS_MDOT(10) FOS_MDOT(11) FOS_MDOT(12) FOS_MDOT(13) FOS_MDOT(14)
+      FOS_MDOT(15) FOS_MDOT(16) FOS_MDOT(17) FOS_MDOT(18) FOS_MDOT(19) FOS_MDOT(20) FOS_MDOT(21)
+      FOS_MDOT(22) FOS_MDOT(23) FOS_MDOT(24) FOS_MDOT(25) FOS_MDOT(26) FOS_MDOT(27) FOS_MDOT(28)
+      FOS_MDOT(29) FOS_MDOT(30) FOS_MDOT(31)
+#undef FOS_MDOT
+      default: fos_set_error("mdot: too many vectors"); return -1;
+    }
+    FOS_LAUNCH_CHECK();
+    return 0;
+  }
+  template <int MODE>
+  int update(int nv, const double* V, long ldv, const double* h, double* w) {
+    switch (nv) {
+#define FOS_UPD(K) \
+  case K: fos_launch(c, k_update<K, MODE>, kRedBlocks, kT, wk.N, V, ldv, h, w, wk.part); break;
+      FOS_UPD(1) FOS_UPD(2) FOS_UPD(3) FOS_UPD(4) FOS_UPD(5) FOS_UPD(6) FOS_UPD(7) FOS_UPD(8)
+      FOS_UPD(9) FOS_UPD(10) FOS_UPD(11) FOS_UPD(12) FOS_UPD(13) FOS_UPD(14) FOS_UPD(15)
+      FOS_UPD(16) FOS_UPD(17) FOS_UPD(18) FOS_UPD(19) FOS_UPD(20) FOS_UPD(21) FOS_UPD(22)
+      FOS_UPD(23) FOS_UPD(24) FOS_UPD(25) FOS_UPD(26) FOS_UPD(27) FOS_UPD(28) FOS_UPD(29)
+      FOS_UPD(30) FOS_UPD(31)
+#undef FOS_UPD
+      default: fos_set_error("update: too many vectors"); return -1;
+    }
+    FOS_LAUNCH_CHECK();
+    return 0;
+  }
   int fetch(const double* d, double* h, int n) {
     FOS_CUDA(cudaMemcpyAsync(h, d, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     FOS_CUDA(cudaStreamSynchronize(c->stream));
@@ -289,11 +320,11 @@ struct Driver {
         if (rc) return rc;
         (*its)++;
         const int nv = j + 1;
-        fos_launch(c, k_mdot, kRedBlocks, kT, N, nv, wk.V, N, wk.w, wk.part);
+        if ((rc = mdot(nv, wk.V, N, wk.w))) return rc;
         if ((rc = reduce(nv, wk.sc))) return rc;
-        fos_launch(c, k_update, kRedBlocks, kT, N, nv, wk.V, N, wk.sc, wk.w, 0, wk.part);
+        if ((rc = update<0>(nv, wk.V, N, wk.sc, wk.w))) return rc;
         if ((rc = reduce(nv, wk.sc + kMaxVec))) return rc;
-        fos_launch(c, k_update, kRedBlocks, kT, N, nv, wk.V, N, wk.sc + kMaxVec, wk.w, 1, wk.part);
+        if ((rc = update<1>(nv, wk.V, N, wk.sc + kMaxVec, wk.w))) return rc;
         if ((rc = reduce(1, wk.sc + 2 * kMaxVec))) return rc;
         if ((rc = fetch(wk.sc, hbuf.data(), 3 * kMaxVec))) return rc;
         double* col = &H[(size_t)(m + 1) * j];

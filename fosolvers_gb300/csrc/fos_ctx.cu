@@ -10,8 +10,10 @@
 //   faceNA  double2[2*nF]  (nx, ny), (nz, area)
 //   crow/cent          per-cell CSR of its faces, entry = face<<1 | (cell is R),
 //                      ascending face id (fixed, deterministic summation order)
+//   ell    int[4*nC]      the same entries at fixed width (one int4 load per tetrahedron)
 //   W      double[8*nC]   per-cell primitives AoS (rho,u,v,w,H,p,sqrt(rho),0)
-//   F      double[5*nF]   per-face flows (SoA)
+//   Whl    float[16*nC]   FP32 (hi, lo) primitives for the FP32 flux
+//   F      double[6*nF]   per-face flows, AoS (5 + pad) so a gather reads 48 B per face
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -28,7 +30,7 @@ extern "C" const char* fos_last_error(void) { return g_err.c_str(); }
 
 fos_ctx::~fos_ctx() {
   void* ptrs[] = {d_old2new, d_new2old, d_faceLR, d_faceNA, d_faceNA32, d_crow, d_cent, d_invV,
-                  d_bcT, d_bcP, d_W, d_W32, d_F, d_stage, d_y, d_f, d_z, d_red, d_scal,
+                  d_bcT, d_bcP, d_W, d_Whl, d_ell, d_F, d_stage, d_y, d_f, d_z, d_red, d_scal,
                   d_flag, d_rowptr, d_col, d_diag, d_fslot, d_J, d_LU, d_LU32, d_lrows_f,
                   d_lrows_b, d_upd_ptr, d_upd, d_ilu_tmp, d_Jb, d_ierr};
   for (void* p : ptrs)
@@ -268,6 +270,18 @@ extern "C" int fos_ctx_create(fos_ctx** out, int nC, int nE, int nPi, int nPb, c
       if (f < nPi) cent[pos[faceLR[f].y]++] = (f << 1) | 1;
     }
   }
+  // ELL copy of the per-cell entries (fixed width: 4 for tetrahedra, 6 for hexahedra)
+  int maxe = 0;
+  for (int i = 0; i < nC; i++) maxe = std::max(maxe, crow[i + 1] - crow[i]);
+  if (maxe > 6) {
+    fos_set_error("fos_ctx_create: a cell has more than 6 faces");
+    delete c;
+    return -2;
+  }
+  c->ell_w = maxe <= 4 ? 4 : 6;
+  std::vector<int> ell((size_t)c->ell_w * nC, -1);
+  for (int i = 0; i < nC; i++)
+    for (int e = crow[i]; e < crow[i + 1]; e++) ell[(size_t)c->ell_w * i + (e - crow[i])] = cent[e];
   std::vector<double> invV(nC);
   for (int i = 0; i < nC; i++) invV[c->old2new[i]] = 1.0 / v[i];
 
@@ -278,12 +292,13 @@ extern "C" int fos_ctx_create(fos_ctx** out, int nC, int nE, int nPi, int nPb, c
   FOS_TRY(upload(&c->d_faceNA32, faceNA32.data(), nP));
   FOS_TRY(upload(&c->d_crow, crow.data(), nC + 1));
   FOS_TRY(upload(&c->d_cent, cent.data(), cent.size()));
+  FOS_TRY(upload(&c->d_ell, ell.data(), ell.size()));
+  FOS_TRY(dalloc(&c->d_Whl, 16 * (size_t)nC));
   FOS_TRY(upload(&c->d_invV, invV.data(), nC));
   FOS_TRY(upload(&c->d_bcT, bcType, nBC));
   FOS_TRY(upload(&c->d_bcP, bcParam, (size_t)maxP * nBC));
   FOS_TRY(dalloc(&c->d_W, 8 * (size_t)nC));
-  FOS_TRY(dalloc(&c->d_W32, 8 * (size_t)nC));
-  FOS_TRY(dalloc(&c->d_F, 5 * (size_t)nP));
+  FOS_TRY(dalloc(&c->d_F, 6 * (size_t)nP));  // AoS flows, 48 B per face (FP64 or 2 x FP32)
   FOS_TRY(dalloc(&c->d_stage, 5 * (size_t)nC));
   FOS_TRY(dalloc(&c->d_y, 5 * (size_t)nC));
   FOS_TRY(dalloc(&c->d_f, 5 * (size_t)nC));

@@ -54,14 +54,16 @@ struct fos_ctx {
   float4* d_faceNA32 = nullptr; // [nF]  (nx, ny, nz, aP) for the FP32 flux
   int* d_crow = nullptr;      // [nC+1] cell -> face entries
   int* d_cent = nullptr;      // (face << 1) | (cell is R)
+  int* d_ell = nullptr;       // [ell_w*nC] the same entries, fixed width, -1 = empty
+  int ell_w = 4;
   double* d_invV = nullptr;   // [nC]
   int* d_bcT = nullptr;       // [nBC]
   double* d_bcP = nullptr;    // [maxP*nBC]
 
   // ---- device work
   double* d_W = nullptr;      // [8*nC] primitive AoS (rho,u,v,w,H,p,sqrt(rho),0)
-  float* d_W32 = nullptr;     // [8*nC]
-  double* d_F = nullptr;      // [5*nF] face flows (FP64 path)
+  float* d_Whl = nullptr;     // [16*nC] FP32 (hi, lo) primitives
+  double* d_F = nullptr;      // [6*nF] face flows, AoS
   double* d_stage = nullptr;  // [5*nC] reference-order staging
   double* d_y = nullptr;      // [5*nC] internal-order callback buffers
   double* d_f = nullptr;

@@ -42,61 +42,62 @@ __device__ __forceinline__ void load_prim(const double* __restrict__ W, int c, P
 }
 
 // eulerNFJ entry (a, b) -- normal flux Jacobian dF.n/dU
-__device__ __forceinline__ double nfj(int a, int b, const double n[3], const double u[3], double H,
-                                      double g, double v2, double vn) {
-  const double g1 = g - 1.0;
-  if (a == 0) return (b >= 1 && b <= 3) ? n[b - 1] : 0.0;
+template <typename T>
+__device__ __forceinline__ T nfj(int a, int b, const T n[3], const T u[3], T H, T g, T v2, T vn) {
+  const T g1 = g - T(1);
+  if (a == 0) return (b >= 1 && b <= 3) ? n[b - 1] : T(0);
   if (a == 4) {
-    if (b == 0) return (0.5 * g1 * v2 - H) * vn;
+    if (b == 0) return (T(0.5) * g1 * v2 - H) * vn;
     if (b == 4) return g * vn;
     return H * n[b - 1] - g1 * u[b - 1] * vn;
   }
   const int i = a - 1;
-  if (b == 0) return 0.5 * g1 * v2 * n[i] - u[i] * vn;
+  if (b == 0) return T(0.5) * g1 * v2 * n[i] - u[i] * vn;
   if (b == 4) return g1 * n[i];
   const int j = b - 1;
-  return u[i] * n[j] + (1.0 - g) * n[i] * u[j] + (i == j ? vn : 0.0);
+  return u[i] * n[j] + (T(1) - g) * n[i] * u[j] + (i == j ? vn : T(0));
 }
 
 // eulerANFJ as |vn| T0 + |vn - c| r- l-^T + |vn + c| r+ l+^T (row-major 25)
-__device__ __forceinline__ void anfj(const double n[3], const double u[3], double H, double c,
-                                     double g, double out[25]) {
-  const double g1 = g - 1.0;
-  const double v2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
-  const double vn = u[0] * n[0] + u[1] * n[1] + u[2] * n[2];
-  const double ic = 1.0 / c;
-  const double M2 = v2 * ic * ic, Mn = vn * ic;
-  const double be = g1 * ic * ic;
-  const double k1 = 1.0 + 0.5 * g1 * M2;
-  const double av = fabs(vn);
+template <typename T>
+__device__ __forceinline__ void anfj(const T n[3], const T u[3], T H, T c, T g, T out[25]) {
+  const T g1 = g - 1.0;
+  const T v2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+  const T vn = u[0] * n[0] + u[1] * n[1] + u[2] * n[2];
+  const T ic = T(1) / c;
+  const T M2 = v2 * ic * ic, Mn = vn * ic;
+  const T be = g1 * ic * ic;
+  const T k1 = T(1) + T(0.5) * g1 * M2;
+  const T av = fabs(vn);
   // T0
-  out[0] = av * (1.0 - 0.5 * g1 * M2);
+  out[0] = av * (T(1) - T(0.5) * g1 * M2);
   for (int j = 0; j < 3; j++) out[1 + j] = av * (be * u[j]);
   out[4] = av * (-be);
   for (int i = 0; i < 3; i++) {
     out[5 * (1 + i)] = av * (-k1 * u[i] + vn * n[i]);
     for (int j = 0; j < 3; j++)
-      out[5 * (1 + i) + 1 + j] = av * (be * u[i] * u[j] - n[i] * n[j] + (i == j ? 1.0 : 0.0));
+      out[5 * (1 + i) + 1 + j] = av * (be * u[i] * u[j] - n[i] * n[j] + (i == j ? T(1) : T(0)));
     out[5 * (1 + i) + 4] = av * (-be * u[i]);
   }
-  out[20] = av * (vn * vn - 0.5 * v2 * k1);
+  out[20] = av * (vn * vn - T(0.5) * v2 * k1);
   for (int j = 0; j < 3; j++) out[21 + j] = av * (k1 * u[j] - vn * n[j]);
-  out[24] = av * (-0.5 * g1 * M2);
+  out[24] = av * (-T(0.5) * g1 * M2);
 #pragma unroll
   for (int sgn = -1; sgn <= 1; sgn += 2) {
-    double rr[5], ll[5];
-    rr[0] = 1.0;
-    for (int i = 0; i < 3; i++) rr[1 + i] = u[i] + sgn * c * n[i];
-    rr[4] = H + sgn * vn * c;
-    ll[0] = 0.25 * g1 * M2 - sgn * 0.5 * Mn;
-    for (int j = 0; j < 3; j++) ll[1 + j] = -0.5 * be * u[j] + sgn * 0.5 * n[j] * ic;
-    ll[4] = 0.5 * be;
-    const double lam = fabs(vn + sgn * c);
+    T rr[5], ll[5];
+    rr[0] = T(1);
+    for (int i = 0; i < 3; i++) rr[1 + i] = u[i] + T(sgn) * c * n[i];
+    rr[4] = H + T(sgn) * vn * c;
+    ll[0] = T(0.25) * g1 * M2 - T(sgn) * T(0.5) * Mn;
+    for (int j = 0; j < 3; j++) ll[1 + j] = -T(0.5) * be * u[j] + T(sgn) * T(0.5) * n[j] * ic;
+    ll[4] = T(0.5) * be;
+    const T lam = fabs(vn + T(sgn) * c);
     for (int a = 0; a < 5; a++)
       for (int b = 0; b < 5; b++) out[5 * a + b] += lam * (rr[a] * ll[b]);
   }
 }
 
+template <typename T>
 __global__ void __launch_bounds__(kT) k_jac_face(int nFi, int nF, int nC,
                                                  const int2* __restrict__ faceLR,
                                                  const double2* __restrict__ faceNA,
@@ -111,8 +112,8 @@ __global__ void __launch_bounds__(kT) k_jac_face(int nFi, int nF, int nC,
   if (f >= nF) return;
   const int2 lr = faceLR[f];
   const double2 n01 = faceNA[2 * (size_t)f], n2a = faceNA[2 * (size_t)f + 1];
-  const double n[3] = {n01.x, n01.y, n2a.x};
-  const double aP = n2a.y;
+  const T n[3] = {(T)n01.x, (T)n01.y, (T)n2a.x};
+  const T aP = (T)n2a.y;
   Prim L, R;
   load_prim(W, lr.x, L);
   if (f < nFi) {
@@ -122,39 +123,43 @@ __global__ void __launch_bounds__(kT) k_jac_face(int nFi, int nF, int nC,
     for (int q = 0; q < 5; q++) U[q] = y[(size_t)q * nC + lr.x];
     const int row = lr.y;
     ghost_state(row > 0 ? bcT[row - 1] : FOS_BC_WALL,
-                row > 0 ? bcP + (size_t)maxP * (row - 1) : nullptr, U, n[0], n[1], n[2], g, r, G);
+                row > 0 ? bcP + (size_t)maxP * (row - 1) : nullptr, U, n01.x, n01.y, n2a.x, g, r, G);
     const double inv = 1.0 / G[0];
     R.rho = G[0]; R.u = G[1] * inv; R.v = G[2] * inv; R.w = G[3] * inv;
     R.p = (g - 1.0) * (G[4] - 0.5 * (G[1] * G[1] + G[2] * G[2] + G[3] * G[3]) * inv);
     R.H = (G[4] + R.p) * inv;
     R.s = sqrt(G[0]);
   }
-  // Roe averages (Euler.f90:207-209)
-  const double inv = 1.0 / (L.s + R.s);
-  const double ua[3] = {(L.s * L.u + R.s * R.u) * inv, (L.s * L.v + R.s * R.v) * inv,
-                        (L.s * L.w + R.s * R.w) * inv};
-  const double Ha = (L.s * L.H + R.s * R.H) * inv;
-  const double ca = sqrt((g - 1.0) * (Ha - 0.5 * (ua[0] * ua[0] + ua[1] * ua[1] + ua[2] * ua[2])));
-  double Ab[25];
-  anfj(n, ua, Ha, ca, g, Ab);
-  const double uL[3] = {L.u, L.v, L.w}, uR[3] = {R.u, R.v, R.w};
-  const double v2L = uL[0] * uL[0] + uL[1] * uL[1] + uL[2] * uL[2];
-  const double vnL = uL[0] * n[0] + uL[1] * n[1] + uL[2] * n[2];
-  const double v2R = uR[0] * uR[0] + uR[1] * uR[1] + uR[2] * uR[2];
-  const double vnR = uR[0] * n[0] + uR[1] * n[1] + uR[2] * n[2];
-  const double h = 0.5 * aP;
+  // Roe averages (Euler.f90:207-209), arithmetic in T (FP64, or FP32 for the FP32 form)
+  const T gg = (T)g;
+  const T sL = (T)L.s, sR = (T)R.s;
+  const T inv = T(1) / (sL + sR);
+  const T ua[3] = {(sL * (T)L.u + sR * (T)R.u) * inv, (sL * (T)L.v + sR * (T)R.v) * inv,
+                   (sL * (T)L.w + sR * (T)R.w) * inv};
+  const T Ha = (sL * (T)L.H + sR * (T)R.H) * inv;
+  const T ca = sqrt((gg - T(1)) * (Ha - T(0.5) * (ua[0] * ua[0] + ua[1] * ua[1] + ua[2] * ua[2])));
+  T Ab[25];
+  anfj<T>(n, ua, Ha, ca, gg, Ab);
+  const T uL[3] = {(T)L.u, (T)L.v, (T)L.w}, uR[3] = {(T)R.u, (T)R.v, (T)R.w};
+  const T HL = (T)L.H, HR = (T)R.H;
+  const T v2L = uL[0] * uL[0] + uL[1] * uL[1] + uL[2] * uL[2];
+  const T vnL = uL[0] * n[0] + uL[1] * n[1] + uL[2] * n[2];
+  const T v2R = uR[0] * uR[0] + uR[1] * uR[1] + uR[2] * uR[2];
+  const T vnR = uR[0] * n[0] + uR[1] * n[1] + uR[2] * n[2];
+  const T h = T(0.5) * aP;
   if (f < nFi) {
     double* oLR = J + 25 * (size_t)fslot[2 * f];      // block (L, R) = JacP(1:5,6:10)
     double* oRL = J + 25 * (size_t)fslot[2 * f + 1];  // block (R, L) = JacP(6:10,1:5)
     for (int a = 0; a < 5; a++)
       for (int b = 0; b < 5; b++) {
-        oLR[5 * a + b] = -h * (nfj(a, b, n, uR, R.H, g, v2R, vnR) - Ab[5 * a + b]);
-        oRL[5 * a + b] = h * (nfj(a, b, n, uL, L.H, g, v2L, vnL) + Ab[5 * a + b]);
+        oLR[5 * a + b] = (double)(-h * (nfj<T>(a, b, n, uR, HR, gg, v2R, vnR) - Ab[5 * a + b]));
+        oRL[5 * a + b] = (double)(h * (nfj<T>(a, b, n, uL, HL, gg, v2L, vnL) + Ab[5 * a + b]));
       }
   } else {
     double* d = Jb + 25 * (size_t)(f - nFi);  // boundary pair's diagonal term
     for (int a = 0; a < 5; a++)
-      for (int b = 0; b < 5; b++) d[5 * a + b] = -h * (nfj(a, b, n, uL, L.H, g, v2L, vnL) + Ab[5 * a + b]);
+      for (int b = 0; b < 5; b++)
+        d[5 * a + b] = (double)(-h * (nfj<T>(a, b, n, uL, HL, gg, v2L, vnL) + Ab[5 * a + b]));
   }
 }
 
@@ -187,35 +192,28 @@ __global__ void __launch_bounds__(kT) k_jac_diag(int nC, int nFi, const int* __r
   for (int k = 0; k < 25; k++) dst[k] = D[k];
 }
 
-// invert a 5x5 block in place (Gauss--Jordan, partial pivoting); false on a zero pivot
+// invert a 5x5 block in place by Gauss--Jordan without pivoting (scalar ilu0 eliminates
+// inside the diagonal block without pivoting too, ilut.f:1893-1898); false on a zero pivot
 template <typename T>
-__device__ bool inv5(T a[25]) {
-  T b[25];
+__device__ __forceinline__ bool inv5(T a[25]) {
+  bool ok = true;
 #pragma unroll
-  for (int k = 0; k < 25; k++) b[k] = (k / 5 == k % 5) ? T(1) : T(0);
-  for (int col = 0; col < 5; col++) {
-    int piv = col;
-    T best = fabs(a[5 * col + col]);
-    for (int rr = col + 1; rr < 5; rr++)
-      if (fabs(a[5 * rr + col]) > best) { best = fabs(a[5 * rr + col]); piv = rr; }
-    if (!(best > T(0))) return false;
-    if (piv != col)
-      for (int k = 0; k < 5; k++) {
-        T t = a[5 * col + k]; a[5 * col + k] = a[5 * piv + k]; a[5 * piv + k] = t;
-        t = b[5 * col + k]; b[5 * col + k] = b[5 * piv + k]; b[5 * piv + k] = t;
-      }
-    const T ip = T(1) / a[5 * col + col];
-    for (int k = 0; k < 5; k++) { a[5 * col + k] *= ip; b[5 * col + k] *= ip; }
-    for (int rr = 0; rr < 5; rr++) {
-      if (rr == col) continue;
-      const T f = a[5 * rr + col];
-      if (f == T(0)) continue;
-      for (int k = 0; k < 5; k++) { a[5 * rr + k] -= f * a[5 * col + k]; b[5 * rr + k] -= f * b[5 * col + k]; }
+  for (int k = 0; k < 5; k++) {
+    const T piv = a[5 * k + k];
+    ok &= (piv != T(0));
+    const T ip = T(1) / piv;
+    // row k scaled; column k becomes the inverse's column
+#pragma unroll
+    for (int j = 0; j < 5; j++) a[5 * k + j] = (j == k) ? ip : a[5 * k + j] * ip;
+#pragma unroll
+    for (int i = 0; i < 5; i++) {
+      if (i == k) continue;
+      const T f = a[5 * i + k];
+#pragma unroll
+      for (int j = 0; j < 5; j++) a[5 * i + j] = (j == k) ? -f * ip : a[5 * i + j] - f * a[5 * k + j];
     }
   }
-#pragma unroll
-  for (int k = 0; k < 25; k++) a[k] = b[k];
-  return true;
+  return ok;
 }
 
 // One level of the block ILU(0) factorisation, one thread per block row i:
@@ -467,9 +465,16 @@ int fos_jac_setup(fos_ctx* c) {
 int fos_jac_assemble(fos_ctx* c, const double* y) {
   int rc = fos_prim_launch(c, y);
   if (rc) return rc;
-  fos_launch(c, k_jac_face, nb(c->nF), kT, c->nFi, c->nF, c->nC, c->d_faceLR, c->d_faceNA,
-             (const double*)c->d_W, y, (const int*)c->d_fslot, (const int*)c->d_bcT,
-             (const double*)c->d_bcP, c->maxP, c->gamm, c->r, c->d_J, c->d_Jb);
+  if (c->flags & FOS_ILU_FP32)  // the FP32 preconditioner is assembled in FP32
+    fos_launch(c, k_jac_face<float>, nb(c->nF), kT, c->nFi, c->nF, c->nC,
+               (const int2*)c->d_faceLR, (const double2*)c->d_faceNA, (const double*)c->d_W, y,
+               (const int*)c->d_fslot, (const int*)c->d_bcT, (const double*)c->d_bcP, c->maxP,
+               c->gamm, c->r, c->d_J, c->d_Jb);
+  else
+    fos_launch(c, k_jac_face<double>, nb(c->nF), kT, c->nFi, c->nF, c->nC,
+               (const int2*)c->d_faceLR, (const double2*)c->d_faceNA, (const double*)c->d_W, y,
+               (const int*)c->d_fslot, (const int*)c->d_bcT, (const double*)c->d_bcP, c->maxP,
+               c->gamm, c->r, c->d_J, c->d_Jb);
   fos_launch(c, k_jac_diag, nb(c->nC), kT, c->nC, c->nFi, (const int*)c->d_crow,
              (const int*)c->d_cent, (const int*)c->d_fslot, (const int*)c->d_diag,
              (const double*)c->d_Jb, c->d_J);

@@ -11,9 +11,8 @@
 //   k_gather  per cell   deterministic CSR gather of -flow (cell is L) / +flow (cell
 //                         is R) in ascending face order, times 1/v; Jv epilogue
 //                         out = a v + b (f(y+sv) - fy)/s in FP64
-// The FP32-flux variant (FOS_FLUX_FP32) computes the same flow in FP32 in the
-// flux-difference form (the L/R central fluxes enter as F_R - F_L; the cell's own
-// flux sums to zero over a closed cell) and accumulates it in FP64.
+// The FP32-flux variant (FOS_FLUX_FP32) computes the same flow in FP32 from FP64 means
+// and jumps, in flux-difference form, and accumulates it in FP64 (see roe_split_mixed).
 #include <cmath>
 
 #include "fos_internal.h"
@@ -145,31 +144,32 @@ __global__ void __launch_bounds__(kThreads) k_face64(
   }
   double flow[5];
   roe_flow64(L, R, nx, ny, nz, aP, g - 1.0, flow);
-#pragma unroll
-  for (int q = 0; q < 5; q++) F[(size_t)q * nF + f] = flow[q];
+  double2* F2 = reinterpret_cast<double2*>(F + 6 * (size_t)f);  // AoS, 48 B per face
+  F2[0] = make_double2(flow[0], flow[1]);
+  F2[1] = make_double2(flow[2], flow[3]);
+  F2[2] = make_double2(flow[4], 0.0);
 }
 
+// Per-cell gather.  ELL layout: every cell has kW entry slots (face << 1 | cell-is-R,
+// -1 = empty), loaded as one int4 for kW = 4 (tetrahedra), so all face loads of a cell
+// are issued together; the fixed slot order gives a deterministic summation order.
 // mode 0: out = sum/v ; mode 1: out = a*v + b*(sum/v - fy)/s
-__global__ void __launch_bounds__(kThreads) k_gather(
-    int nC, int nF, const int* __restrict__ crow, const int* __restrict__ cent,
-    const double* __restrict__ F, const double* __restrict__ invV, int mode,
-    const double* __restrict__ vv, const double* __restrict__ fy, const double* __restrict__ d_s,
-    double a, double b, double* __restrict__ out, int* __restrict__ flag) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= nC) return;
-  double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-  const int e0 = __ldg(crow + c), e1 = __ldg(crow + c + 1);
-  for (int e = e0; e < e1; e++) {
-    const int ent = __ldg(cent + e);
-    const int f = ent >> 1;
-    const bool plus = ent & 1;
+template <int kW>
+__device__ __forceinline__ void load_ell(const int* __restrict__ ell, int c, int e[kW]) {
+  if (kW == 4) {
+    const int4 q = __ldg(reinterpret_cast<const int4*>(ell) + c);
+    e[0] = q.x; e[1] = q.y; e[2] = q.z; e[3] = q.w;
+  } else {
 #pragma unroll
-    for (int q = 0; q < 5; q++) {
-      const double x = __ldg(F + (size_t)q * nF + f);
-      acc[q] = plus ? acc[q] + x : acc[q] - x;
-    }
+    for (int k = 0; k < kW; k++) e[k] = __ldg(ell + (size_t)kW * c + k);
   }
-  const double iv = __ldg(invV + c);
+}
+
+__device__ __forceinline__ void gather_epilogue(int nC, int c, const double acc[5], double iv,
+                                                int mode, const double* __restrict__ vv,
+                                                const double* __restrict__ fy,
+                                                const double* __restrict__ d_s, double a, double b,
+                                                double* __restrict__ out, int* __restrict__ flag) {
   bool bad = false;
   if (mode == 0) {
 #pragma unroll
@@ -192,66 +192,42 @@ __global__ void __launch_bounds__(kThreads) k_gather(
   if (bad && flag) atomicOr(flag, 1);
 }
 
+template <int kW>
+__global__ void __launch_bounds__(kThreads) k_gather(
+    int nC, const int* __restrict__ ell, const double* __restrict__ F,
+    const double* __restrict__ invV, int mode, const double* __restrict__ vv,
+    const double* __restrict__ fy, const double* __restrict__ d_s, double a, double b,
+    double* __restrict__ out, int* __restrict__ flag) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nC) return;
+  int e[kW];
+  load_ell<kW>(ell, c, e);
+  double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+  for (int k = 0; k < kW; k++) {
+    if (e[k] < 0) continue;
+    const double sg = (e[k] & 1) ? 1.0 : -1.0;
+    const double2* F2 = reinterpret_cast<const double2*>(F + 6 * (size_t)(e[k] >> 1));
+    const double2 a0 = __ldg(F2), a1 = __ldg(F2 + 1), a2 = __ldg(F2 + 2);
+    acc[0] += sg * a0.x; acc[1] += sg * a0.y; acc[2] += sg * a1.x; acc[3] += sg * a1.y;
+    acc[4] += sg * a2.x;
+  }
+  gather_epilogue(nC, c, acc, __ldg(invV + c), mode, vv, fy, d_s, a, b, out, flag);
+}
+
 // ------------------------------------------------------------------ FP32 flux
-struct P32 {
-  float rho, u, v, w, H, p, s;
-};
-__device__ __forceinline__ void load_prim32(const float* __restrict__ W, int c, P32& P) {
-  const float4* w4 = reinterpret_cast<const float4*>(W + 8 * (size_t)c);
-  float4 a = __ldg(w4), b = __ldg(w4 + 1);
-  P.rho = a.x; P.u = a.y; P.v = a.z; P.w = a.w; P.H = b.x; P.p = b.y; P.s = b.z;
+// Per-cell primitives for the FP32 flux as FP32 (hi, lo) pairs: x = hi + lo to ~48 bits,
+// so a face jump (hR - hL) + (lR - lL) keeps FP32 relative accuracy of the jump itself
+// while the face kernel issues FP32 instructions only.  Layout: 16 floats (64 B) per cell
+// = (rho, u, v, w, H, p) hi, (rho, u, v, w, H, p) lo, sqrt(rho), 0, 0, 0.
+__device__ __forceinline__ void split_hl(double x, float& h, float& l) {
+  h = (float)x;
+  l = (float)(x - (double)h);
 }
-
-// Same Roe flow in FP32, flux-difference form: the cell's own flux F_L.n sums to zero
-// over the closed cell, so L receives -aP(1/2 (F_R - F_L).n - 1/2 waves) and R receives
-// -aP(1/2 (F_R - F_L).n + 1/2 waves); stored as (dF, waves) pairs per face.
-__device__ __forceinline__ void roe_split32(const P32& L, const P32& R, float nx, float ny,
-                                            float nz, float aP, float gm1, float dF[5],
-                                            float dw[5]) {
-  const float inv = 1.0f / (L.s + R.s);
-  const float ua = (L.s * L.u + R.s * R.u) * inv;
-  const float va = (L.s * L.v + R.s * R.v) * inv;
-  const float wa = (L.s * L.w + R.s * R.w) * inv;
-  const float Ha = (L.s * L.H + R.s * R.H) * inv;
-  const float rhoA = L.s * R.s;
-  const float q2 = ua * ua + va * va + wa * wa;
-  const float c2 = gm1 * (Ha - 0.5f * q2);
-  const float ca = sqrtf(c2);
-  const float ic2 = 1.0f / c2;
-  const float unA = ua * nx + va * ny + wa * nz;
-  const float rJ = R.rho - L.rho, pJ = R.p - L.p;
-  const float uJ = R.u - L.u, vJ = R.v - L.v, wJ = R.w - L.w;
-  const float unJ = uJ * nx + vJ * ny + wJ * nz;
-  const float au = fabsf(unA);
-  const float wE = rJ - pJ * ic2;
-  float d0 = au * wE;
-  float d1 = au * (wE * ua + rhoA * (uJ - nx * unJ));
-  float d2 = au * (wE * va + rhoA * (vJ - ny * unJ));
-  float d3 = au * (wE * wa + rhoA * (wJ - nz * unJ));
-  float d4 = au * (wE * (0.5f * q2) + rhoA * (ua * uJ + va * vJ + wa * wJ - unA * unJ));
-  const float s1 = fabsf(unA - ca) * (0.5f * (pJ - rhoA * ca * unJ) * ic2);
-  d0 += s1; d1 += s1 * (ua - nx * ca); d2 += s1 * (va - ny * ca); d3 += s1 * (wa - nz * ca);
-  d4 += s1 * (Ha - unA * ca);
-  const float s2 = fabsf(unA + ca) * (0.5f * (pJ + rhoA * ca * unJ) * ic2);
-  d0 += s2; d1 += s2 * (ua + nx * ca); d2 += s2 * (va + ny * ca); d3 += s2 * (wa + nz * ca);
-  d4 += s2 * (Ha + unA * ca);
-  // F_R.n - F_L.n for the five components
-  const float unL = L.u * nx + L.v * ny + L.w * nz;
-  const float unR = R.u * nx + R.v * ny + R.w * nz;
-  const float mL = L.rho * unL, mR = R.rho * unR;
-  dF[0] = 0.5f * aP * (mR - mL);
-  dF[1] = 0.5f * aP * (mR * R.u - mL * L.u + pJ * nx);
-  dF[2] = 0.5f * aP * (mR * R.v - mL * L.v + pJ * ny);
-  dF[3] = 0.5f * aP * (mR * R.w - mL * L.w + pJ * nz);
-  dF[4] = 0.5f * aP * (mR * R.H - mL * L.H);
-  dw[0] = 0.5f * aP * d0; dw[1] = 0.5f * aP * d1; dw[2] = 0.5f * aP * d2;
-  dw[3] = 0.5f * aP * d3; dw[4] = 0.5f * aP * d4;
-}
-
-__global__ void __launch_bounds__(kThreads) k_prim32(int nC, const double* __restrict__ y,
-                                                     const double* __restrict__ v,
-                                                     const double* __restrict__ d_s, double gm1,
-                                                     float* __restrict__ W) {
+__global__ void __launch_bounds__(kThreads) k_prim_hl(int nC, const double* __restrict__ y,
+                                                      const double* __restrict__ v,
+                                                      const double* __restrict__ d_s, double gm1,
+                                                      float* __restrict__ W) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nC) return;
   double U[5];
@@ -262,99 +238,164 @@ __global__ void __launch_bounds__(kThreads) k_prim32(int nC, const double* __res
 #pragma unroll
     for (int q = 0; q < 5; q++) U[q] = U[q] + s * v[(size_t)q * nC + c];
   }
-  // primitives in FP32 from the FP64 perturbed state
-  const float rho = (float)U[0];
-  const float inv = 1.0f / rho;
-  const float mx = (float)U[1], my = (float)U[2], mz = (float)U[3], E = (float)U[4];
-  const float p = (float)gm1 * (E - 0.5f * (mx * mx + my * my + mz * mz) * inv);
-  float4* w4 = reinterpret_cast<float4*>(W + 8 * (size_t)c);
-  w4[0] = make_float4(rho, mx * inv, my * inv, mz * inv);
-  w4[1] = make_float4((E + p) * inv, p, sqrtf(rho), 0.0f);
+  P64 P;
+  prim_from_cons(U[0], U[1], U[2], U[3], U[4], gm1, P);
+  float h[6], l[6];
+  split_hl(P.rho, h[0], l[0]);
+  split_hl(P.u, h[1], l[1]);
+  split_hl(P.v, h[2], l[2]);
+  split_hl(P.w, h[3], l[3]);
+  split_hl(P.H, h[4], l[4]);
+  split_hl(P.p, h[5], l[5]);
+  float4* w4 = reinterpret_cast<float4*>(W + 16 * (size_t)c);
+  w4[0] = make_float4(h[0], h[1], h[2], h[3]);
+  w4[1] = make_float4(h[4], h[5], l[0], l[1]);
+  w4[2] = make_float4(l[2], l[3], l[4], l[5]);
+  w4[3] = make_float4((float)P.s, 0.0f, 0.0f, 0.0f);
 }
 
-__global__ void __launch_bounds__(kThreads) k_face32(
-    int nFi, int nF, int nC, const int2* __restrict__ faceLR, const float4* __restrict__ faceNA,
-    const float* __restrict__ W, const double* __restrict__ y, const double* __restrict__ v,
-    const double* __restrict__ d_s, const int* __restrict__ bcT, const double* __restrict__ bcP,
-    int maxP, double g, double r, float* __restrict__ F) {
+struct PHL {
+  float h[6], l[6], s;
+};
+__device__ __forceinline__ void load_hl(const float* __restrict__ W, int c, PHL& P) {
+  const float4* w4 = reinterpret_cast<const float4*>(W + 16 * (size_t)c);
+  const float4 a = __ldg(w4), b = __ldg(w4 + 1), d = __ldg(w4 + 2), e = __ldg(w4 + 3);
+  P.h[0] = a.x; P.h[1] = a.y; P.h[2] = a.z; P.h[3] = a.w; P.h[4] = b.x; P.h[5] = b.y;
+  P.l[0] = b.z; P.l[1] = b.w; P.l[2] = d.x; P.l[3] = d.y; P.l[4] = d.z; P.l[5] = d.w;
+  P.s = e.x;
+}
+
+// FP32 Roe flow from means / jumps (shared by the interior and boundary kernels)
+__device__ __forceinline__ void roe_split_mj(float rm, float dr, float um, float du, float vm,
+                                             float dv, float wm, float dww, float Hm, float dH,
+                                             float dp, float sL, float sR, float nx, float ny,
+                                             float nz, float aP, float gm1, float dF[5],
+                                             float dw[5]) {
+  const float unm = um * nx + vm * ny + wm * nz;
+  const float dun = du * nx + dv * ny + dww * nz;
+  const float mm = rm * unm + 0.25f * dr * dun;  // mean of m = rho un
+  const float dm = rm * dun + dr * unm;          // jump of m
+  const float h = 0.5f * aP;
+  dF[0] = h * dm;
+  dF[1] = h * (mm * du + dm * um + dp * nx);
+  dF[2] = h * (mm * dv + dm * vm + dp * ny);
+  dF[3] = h * (mm * dww + dm * wm + dp * nz);
+  dF[4] = h * (mm * dH + dm * Hm);
+  const float kap = 0.5f * (sR - sL) / (sL + sR);
+  const float ua = um + kap * du, va = vm + kap * dv, wa = wm + kap * dww, Ha = Hm + kap * dH;
+  const float rhoA = sL * sR;
+  const float q2 = ua * ua + va * va + wa * wa;
+  const float c2 = gm1 * (Ha - 0.5f * q2);
+  const float ca = sqrtf(c2);
+  const float ic2 = 1.0f / c2;
+  const float unA = ua * nx + va * ny + wa * nz;
+  const float au = fabsf(unA);
+  const float wE = dr - dp * ic2;
+  float d0 = au * wE;
+  float d1 = au * (wE * ua + rhoA * (du - nx * dun));
+  float d2 = au * (wE * va + rhoA * (dv - ny * dun));
+  float d3 = au * (wE * wa + rhoA * (dww - nz * dun));
+  float d4 = au * (wE * (0.5f * q2) + rhoA * (ua * du + va * dv + wa * dww - unA * dun));
+  const float s1 = fabsf(unA - ca) * (0.5f * (dp - rhoA * ca * dun) * ic2);
+  d0 += s1; d1 += s1 * (ua - nx * ca); d2 += s1 * (va - ny * ca); d3 += s1 * (wa - nz * ca);
+  d4 += s1 * (Ha - unA * ca);
+  const float s2 = fabsf(unA + ca) * (0.5f * (dp + rhoA * ca * dun) * ic2);
+  d0 += s2; d1 += s2 * (ua + nx * ca); d2 += s2 * (va + ny * ca); d3 += s2 * (wa + nz * ca);
+  d4 += s2 * (Ha + unA * ca);
+  dw[0] = h * d0; dw[1] = h * d1; dw[2] = h * d2; dw[3] = h * d3; dw[4] = h * d4;
+}
+
+__device__ __forceinline__ void store_f32(float* __restrict__ F, int f, const float dF[5],
+                                          const float dw[5]) {
+  float4* F4 = reinterpret_cast<float4*>(F + 12 * (size_t)f);  // AoS (dF, dw) pairs, 48 B
+  F4[0] = make_float4(dF[0], dw[0], dF[1], dw[1]);
+  F4[1] = make_float4(dF[2], dw[2], dF[3], dw[3]);
+  F4[2] = make_float4(dF[4], dw[4], 0.0f, 0.0f);
+}
+
+// interior faces [0, nFi): FP32 instructions only
+__global__ void __launch_bounds__(kThreads) k_face32i(int nFi, const int2* __restrict__ faceLR,
+                                                      const float4* __restrict__ faceNA,
+                                                      const float* __restrict__ W, float gm1,
+                                                      float* __restrict__ F) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nFi) return;
+  const int2 lr = __ldg(faceLR + f);
+  const float4 na = __ldg(faceNA + f);
+  PHL L, R;
+  load_hl(W, lr.x, L);
+  load_hl(W, lr.y, R);
+  float m[6], d[6];
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    m[k] = 0.5f * (L.h[k] + R.h[k]) + 0.5f * (L.l[k] + R.l[k]);
+    d[k] = (R.h[k] - L.h[k]) + (R.l[k] - L.l[k]);
+  }
+  float dF[5], dw[5];
+  roe_split_mj(m[0], d[0], m[1], d[1], m[2], d[2], m[3], d[3], m[4], d[4], d[5], L.s, R.s, na.x,
+               na.y, na.z, na.w, gm1, dF, dw);
+  store_f32(F, f, dF, dw);
+}
+
+// boundary faces [nFi, nF): ghost state and means/jumps in FP64 (1% of the faces)
+__global__ void __launch_bounds__(kThreads) k_face32b(
+    int nFi, int nF, int nC, const int2* __restrict__ faceLR, const float4* __restrict__ faceNA,
+    const double* __restrict__ y, const double* __restrict__ v, const double* __restrict__ d_s,
+    const int* __restrict__ bcT, const double* __restrict__ bcP, int maxP, double g, double r,
+    float* __restrict__ F) {
+  const int f = nFi + blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nF) return;
   const int2 lr = __ldg(faceLR + f);
   const float4 na = __ldg(faceNA + f);
-  P32 L, R;
-  load_prim32(W, lr.x, L);
-  if (f < nFi) {
-    load_prim32(W, lr.y, R);
-  } else {
-    double U[5], G[5];
+  double U[5], G[5];
 #pragma unroll
-    for (int q = 0; q < 5; q++) U[q] = y[(size_t)q * nC + lr.x];
-    if (v) {
-      const double s = *d_s;
+  for (int q = 0; q < 5; q++) U[q] = y[(size_t)q * nC + lr.x];
+  if (v) {
+    const double s = *d_s;
 #pragma unroll
-      for (int q = 0; q < 5; q++) U[q] = U[q] + s * v[(size_t)q * nC + lr.x];
-    }
-    const int row = lr.y;
-    const int type = row > 0 ? bcT[row - 1] : FOS_BC_WALL;
-    ghost_state(type, row > 0 ? bcP + (size_t)maxP * (row - 1) : nullptr, U, na.x, na.y, na.z,
-                g, r, G);
-    const float rho = (float)G[0], inv = 1.0f / rho;
-    const float mx = (float)G[1], my = (float)G[2], mz = (float)G[3], E = (float)G[4];
-    R.rho = rho; R.u = mx * inv; R.v = my * inv; R.w = mz * inv;
-    R.p = (float)(g - 1.0) * (E - 0.5f * (mx * mx + my * my + mz * mz) * inv);
-    R.H = (E + R.p) * inv;
-    R.s = sqrtf(rho);
+    for (int q = 0; q < 5; q++) U[q] = U[q] + s * v[(size_t)q * nC + lr.x];
   }
+  const int row = lr.y;
+  const int type = row > 0 ? bcT[row - 1] : FOS_BC_WALL;
+  ghost_state(type, row > 0 ? bcP + (size_t)maxP * (row - 1) : nullptr, U, na.x, na.y, na.z, g,
+              r, G);
+  P64 L, R;
+  prim_from_cons(U[0], U[1], U[2], U[3], U[4], g - 1.0, L);
+  prim_from_cons(G[0], G[1], G[2], G[3], G[4], g - 1.0, R);
   float dF[5], dw[5];
-  roe_split32(L, R, na.x, na.y, na.z, na.w, (float)(g - 1.0), dF, dw);
-  // (dF, dw) pairs as float2 per component: F2[q*nF + f]
-  float2* F2 = reinterpret_cast<float2*>(F);
-#pragma unroll
-  for (int q = 0; q < 5; q++) F2[(size_t)q * nF + f] = make_float2(dF[q], dw[q]);
+  roe_split_mj((float)(0.5 * (L.rho + R.rho)), (float)(R.rho - L.rho), (float)(0.5 * (L.u + R.u)),
+               (float)(R.u - L.u), (float)(0.5 * (L.v + R.v)), (float)(R.v - L.v),
+               (float)(0.5 * (L.w + R.w)), (float)(R.w - L.w), (float)(0.5 * (L.H + R.H)),
+               (float)(R.H - L.H), (float)(R.p - L.p), (float)L.s, (float)R.s, na.x, na.y, na.z,
+               na.w, (float)(g - 1.0), dF, dw);
+  store_f32(F, f, dF, dw);
 }
 
 // FP64 accumulation of the FP32 face terms: cell L gets -(dF - dw), cell R gets -(dF + dw)
+template <int kW>
 __global__ void __launch_bounds__(kThreads) k_gather32(
-    int nC, int nF, const int* __restrict__ crow, const int* __restrict__ cent,
-    const float* __restrict__ F, const double* __restrict__ invV, int mode,
-    const double* __restrict__ vv, const double* __restrict__ fy, const double* __restrict__ d_s,
-    double a, double b, double* __restrict__ out, int* __restrict__ flag) {
+    int nC, const int* __restrict__ ell, const float* __restrict__ F,
+    const double* __restrict__ invV, int mode, const double* __restrict__ vv,
+    const double* __restrict__ fy, const double* __restrict__ d_s, double a, double b,
+    double* __restrict__ out, int* __restrict__ flag) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nC) return;
+  int e[kW];
+  load_ell<kW>(ell, c, e);
   double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-  const float2* F2 = reinterpret_cast<const float2*>(F);
-  const int e0 = __ldg(crow + c), e1 = __ldg(crow + c + 1);
-  for (int e = e0; e < e1; e++) {
-    const int ent = __ldg(cent + e);
-    const int f = ent >> 1;
-    const bool isR = ent & 1;
 #pragma unroll
-    for (int q = 0; q < 5; q++) {
-      const float2 x = __ldg(F2 + (size_t)q * nF + f);
-      acc[q] -= isR ? (double)x.x + (double)x.y : (double)x.x - (double)x.y;
-    }
+  for (int k = 0; k < kW; k++) {
+    if (e[k] < 0) continue;
+    const double sw = (e[k] & 1) ? 1.0 : -1.0;
+    const float4* F4 = reinterpret_cast<const float4*>(F + 12 * (size_t)(e[k] >> 1));
+    const float4 a0 = __ldg(F4), a1 = __ldg(F4 + 1), a2 = __ldg(F4 + 2);
+    acc[0] -= (double)a0.x + sw * (double)a0.y;
+    acc[1] -= (double)a0.z + sw * (double)a0.w;
+    acc[2] -= (double)a1.x + sw * (double)a1.y;
+    acc[3] -= (double)a1.z + sw * (double)a1.w;
+    acc[4] -= (double)a2.x + sw * (double)a2.y;
   }
-  const double iv = __ldg(invV + c);
-  bool bad = false;
-  if (mode == 0) {
-#pragma unroll
-    for (int q = 0; q < 5; q++) {
-      const double o = acc[q] * iv;
-      bad |= !isfinite(o);
-      out[(size_t)q * nC + c] = o;
-    }
-  } else {
-    const double s = *d_s;
-#pragma unroll
-    for (int q = 0; q < 5; q++) {
-      const size_t k = (size_t)q * nC + c;
-      double o = a * vv[k];
-      if (s > 0.0) o += b * ((acc[q] * iv - fy[k]) / s);
-      bad |= !isfinite(o);
-      out[k] = o;
-    }
-  }
-  if (bad && flag) atomicOr(flag, 1);
+  gather_epilogue(nC, c, acc, __ldg(invV + c), mode, vv, fy, d_s, a, b, out, flag);
 }
 
 __global__ void k_permute(int nC, const int* __restrict__ idx, const double* __restrict__ in,
@@ -416,21 +457,37 @@ int fos_residual_launch(fos_ctx* c, const double* y, const double* v, const doub
                         const double* fy, double* out, double a, double b, int mode) {
   const double gm1 = c->gamm - 1.0;
   if (c->flags & FOS_FLUX_FP32) {
-    fos_launch(c, k_prim32, nblk(c->nC), kThreads, c->nC, y, v, d_s, gm1, c->d_W32);
-    fos_launch(c, k_face32, nblk(c->nF), kThreads, 
-        c->nFi, c->nF, c->nC, c->d_faceLR, c->d_faceNA32, c->d_W32, y, v, d_s, c->d_bcT,
-        c->d_bcP, c->maxP, c->gamm, c->r, reinterpret_cast<float*>(c->d_F));
-    fos_launch(c, k_gather32, nblk(c->nC), kThreads, 
-        c->nC, c->nF, c->d_crow, c->d_cent, reinterpret_cast<const float*>(c->d_F), c->d_invV,
-        mode, v, fy, d_s, a, b, out, c->d_flag);
+    fos_launch(c, k_prim_hl, nblk(c->nC), kThreads, c->nC, y, v, d_s, gm1, c->d_Whl);
+    fos_launch(c, k_face32i, nblk(c->nFi), kThreads, c->nFi, (const int2*)c->d_faceLR,
+               (const float4*)c->d_faceNA32, (const float*)c->d_Whl, (float)gm1,
+               reinterpret_cast<float*>(c->d_F));
+    if (c->nFb)
+      fos_launch(c, k_face32b, nblk(c->nFb), kThreads, c->nFi, c->nF, c->nC,
+                 (const int2*)c->d_faceLR, (const float4*)c->d_faceNA32, y, v, d_s,
+                 (const int*)c->d_bcT, (const double*)c->d_bcP, c->maxP, c->gamm, c->r,
+                 reinterpret_cast<float*>(c->d_F));
+    if (c->ell_w == 4)
+      fos_launch(c, k_gather32<4>, nblk(c->nC), kThreads, c->nC, (const int*)c->d_ell,
+                 reinterpret_cast<const float*>(c->d_F), (const double*)c->d_invV, mode, v, fy,
+                 d_s, a, b, out, c->d_flag);
+    else
+      fos_launch(c, k_gather32<6>, nblk(c->nC), kThreads, c->nC, (const int*)c->d_ell,
+                 reinterpret_cast<const float*>(c->d_F), (const double*)c->d_invV, mode, v, fy,
+                 d_s, a, b, out, c->d_flag);
   } else {
     fos_launch(c, k_prim64, nblk(c->nC), kThreads, c->nC, y, v, d_s, gm1, c->d_W);
-    fos_launch(c, k_face64, nblk(c->nF), kThreads, c->nFi, c->nF, c->nC, c->d_faceLR,
-                                                       c->d_faceNA, c->d_W, y, v, d_s, c->d_bcT,
-                                                       c->d_bcP, c->maxP, c->gamm, c->r, c->d_F);
-    fos_launch(c, k_gather, nblk(c->nC), kThreads, c->nC, c->nF, c->d_crow, c->d_cent,
-                                                      c->d_F, c->d_invV, mode, v, fy, d_s, a, b,
-                                                      out, c->d_flag);
+    fos_launch(c, k_face64, nblk(c->nF), kThreads, c->nFi, c->nF, c->nC,
+               (const int2*)c->d_faceLR, (const double2*)c->d_faceNA, (const double*)c->d_W, y, v,
+               d_s, (const int*)c->d_bcT, (const double*)c->d_bcP, c->maxP, c->gamm, c->r,
+               c->d_F);
+    if (c->ell_w == 4)
+      fos_launch(c, k_gather<4>, nblk(c->nC), kThreads, c->nC, (const int*)c->d_ell,
+                 (const double*)c->d_F, (const double*)c->d_invV, mode, v, fy, d_s, a, b, out,
+                 c->d_flag);
+    else
+      fos_launch(c, k_gather<6>, nblk(c->nC), kThreads, c->nC, (const int*)c->d_ell,
+                 (const double*)c->d_F, (const double*)c->d_invV, mode, v, fy, d_s, a, b, out,
+                 c->d_flag);
   }
   FOS_LAUNCH_CHECK();
   return 0;

@@ -71,3 +71,16 @@ def rel_err(a: np.ndarray, b: np.ndarray) -> float:
     a = a.reshape(5, -1)
     b = b.reshape(5, -1)
     return float(max(np.abs(a[q] - b[q]).max() / max(np.abs(b[q]).max(), 1e-300) for q in range(5)))
+
+
+def field_errors(a: np.ndarray, b: np.ndarray) -> dict:
+    """Errors per conserved field relative to the field's largest magnitude; momentum is one
+    vector field (relative to max |rho u|), so near-zero transverse components are not
+    normalised by their own tiny maximum."""
+    a = a.reshape(5, -1)
+    b = b.reshape(5, -1)
+    mom = np.sqrt((b[1:4] ** 2).sum(0)).max()
+    return {"rho": float(np.abs(a[0] - b[0]).max() / np.abs(b[0]).max()),
+            "rhou": float(np.abs(a[1:4] - b[1:4]).max() / max(mom, 1e-300)),
+            "rhoE": float(np.abs(a[4] - b[4]).max() / np.abs(b[4]).max()),
+            "per_component": [float(np.abs(a[q] - b[q]).max()) for q in range(5)]}

@@ -9,15 +9,16 @@ import pytest
 
 from fosolvers_gb300 import mesh as M
 from fosolvers_gb300.euler import FLUX_FP32, ILU_COLOR, ILU_FP32
-from helpers import Case, rel_err
+from helpers import Case, field_errors, rel_err
 from oracle import pyoracle as O
 
 pytestmark = pytest.mark.gpu
 
 
-def oracle_run(c: Case, nsteps=None, use_prec=1):
+def oracle_run(c: Case, nsteps=None, use_prec=1, **kw):
     wl = c.wl
-    opts = O.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=nsteps or wl.nsteps, use_prec=use_prec)
+    opts = O.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=nsteps or wl.nsteps, use_prec=use_prec,
+                          **kw)
     y = c.y0.copy()
     c.match_ilu_order()
     rhs, pset, psol = c.oracle.callbacks()
@@ -26,13 +27,14 @@ def oracle_run(c: Case, nsteps=None, use_prec=1):
     return y, st
 
 
-def gpu_run(c: Case, nsteps=None, precond=1):
+def gpu_run(c: Case, nsteps=None, precond=1, **kw):
     import torch
     wl = c.wl
     yr = torch.from_numpy(c.y0).cuda()
     y = torch.empty_like(yr)
     c.gpu.to_internal(yr, y)
-    opts = c.gpu.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=nsteps or wl.nsteps, precond=precond)
+    opts = c.gpu.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=nsteps or wl.nsteps, precond=precond,
+                              **kw)
     rc, st = c.gpu.bdf_run(y, opts)
     assert rc == 0, st
     c.gpu.to_reference(y, yr)
@@ -46,7 +48,7 @@ def test_sod16_twenty_steps_matches_oracle(cuda):
     y_ref, st_ref = oracle_run(c)
     y, st = gpu_run(c)
     err = rel_err(y, y_ref)
-    print("sod16", err, st, st_ref)
+    print("sod16 parity", err, st, st_ref)
     assert st["n_steps"] == 20
     assert st["n_newton"] == st_ref["n_newton"]
     assert err <= 1e-10
@@ -61,9 +63,13 @@ def test_sine_bdf2_matches_oracle(cuda, flags):
 
 
 def test_bump_cfl5_matches_oracle(cuda):
+    """Supersonic bump at CFL ~5 (static inflow, extrapolated outflow, walls).  With ~40
+    Krylov iterations per Newton solve the finite-difference Jv rounding (~1e-8 relative)
+    separates the two iterations within the Newton tolerance ball, so parity is checked at a
+    Newton tolerance tightened to 1e-11 (both runs converge onto the same discrete solution)."""
     c = Case(M.make_workload("bump192", scale=24))
-    y_ref, _ = oracle_run(c, nsteps=4)
-    y, st = gpu_run(c, nsteps=4)
+    y_ref, _ = oracle_run(c, nsteps=4, newton_rtol=1e-11)
+    y, st = gpu_run(c, nsteps=4, newton_rtol=1e-11)
     assert rel_err(y, y_ref) <= 1e-10
 
 
@@ -93,10 +99,11 @@ def test_dropin_callbacks_under_reference_driver(cuda):
 @pytest.mark.parametrize("extra", [0, ILU_COLOR])
 def test_fp32_form_within_1e6(cuda, extra):
     """FP32 Roe flux + FP32 ILU(0) factors/apply, FP64 Newton/orthogonalisation: state within
-    1e-6 of the FP64 oracle after the Sod workload's 20 steps."""
+    1e-6 of the FP64 oracle after the Sod workload's 20 steps, per conserved field (density,
+    momentum vector, energy), relative to the field's largest magnitude."""
     c = Case(M.make_workload("sod16"), flags=FLUX_FP32 | ILU_FP32 | extra)
     y_ref, _ = oracle_run(c)
     y, st = gpu_run(c)
-    err = rel_err(y, y_ref)
+    err = field_errors(y, y_ref)
     print("fp32 form sod16", err, st)
-    assert err <= 1e-6
+    assert max(err["rho"], err["rhou"], err["rhoE"]) <= 1e-6
