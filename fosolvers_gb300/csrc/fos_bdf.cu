@@ -7,8 +7,8 @@
 //   BDF2: G(y) = y - 2/3 dt f(y) - (4/3 y_n - 1/3 y_{n-1})  gamma = 2/3 dt (first step BDF1)
 //   Newton: y_0 = y_n; stop when ||G(y_k)||_2 <= rtol ||y_n||_2 + atol sqrt(N), in FP64
 //   linear: right-preconditioned restarted GMRES(maxl) on J_G d = -G, Arnoldi by classical
-//           Gram--Schmidt with one re-orthogonalisation (CGS2) in FP64, Givens least
-//           squares on the host, stop at ||r|| <= lin_rtol ||G||
+//           Gram--Schmidt in FP64 with a second pass when ||w_1|| < ||w_0||/sqrt(2) (DGKS),
+//           Givens least squares on the host, stop at ||r|| <= lin_rtol ||G||
 //   J_G v = v - gamma (f(y + s v) - f(y))/s, s = jv_eps (1 + ||y||)/||v|| (fused kernel)
 //   preconditioner: pset once per BDF step (jok = 0 unless jac_reuse), psol = block ILU(0)
 // All reductions are deterministic two-stage warp-shuffle reductions.
@@ -52,20 +52,23 @@ __device__ __forceinline__ void block_reduce_store(double (&acc)[NV], int nv, do
   }
 }
 
-// h[l] = V_l . w for l < NV (NV fixed at compile time: accumulators stay in registers)
-template <int NV>
+// h[l] = V_l . w for l < NV (NV fixed at compile time: accumulators stay in registers),
+// plus h[NV] = ||w||^2 when NRM
+template <int NV, bool NRM>
 __global__ void __launch_bounds__(kT) k_mdot(long n, const double* __restrict__ V, long ldv,
                                              const double* __restrict__ w,
                                              double* __restrict__ part) {
-  double acc[NV];
+  constexpr int NA = NV + (NRM ? 1 : 0);
+  double acc[NA];
 #pragma unroll
-  for (int l = 0; l < NV; l++) acc[l] = 0.0;
+  for (int l = 0; l < NA; l++) acc[l] = 0.0;
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     const double wi = w[i];
 #pragma unroll
     for (int l = 0; l < NV; l++) acc[l] += V[(size_t)l * ldv + i] * wi;
+    if (NRM) acc[NA - 1] += wi * wi;
   }
-  block_reduce_store<NV>(acc, NV, part);
+  block_reduce_store<NA>(acc, NA, part);
 }
 
 // w -= sum_l h[l] V_l ; then part <- V_l . w (MODE 0, CGS2 second pass) or ||w||^2 (MODE 1)
@@ -201,7 +204,7 @@ int work_get(fos_ctx* c, int maxl, Work** out) {
   for (double** p : {&wk->w, &wk->yn, &wk->ym, &wk->hist, &wk->f, &wk->b, &wk->d, &wk->yh})
     FOS_CUDA(cudaMalloc(p, sizeof(double) * N));
   FOS_CUDA(cudaMalloc(&wk->part, sizeof(double) * kRedBlocks * kMaxVec));
-  FOS_CUDA(cudaMalloc(&wk->sc, sizeof(double) * 4 * kMaxVec));
+  FOS_CUDA(cudaMalloc(&wk->sc, sizeof(double) * 6 * kMaxVec));
   *out = wk;
   return 0;
 }
@@ -238,10 +241,11 @@ struct Driver {
     FOS_LAUNCH_CHECK();
     return 0;
   }
+  template <bool NRM>
   int mdot(int nv, const double* V, long ldv, const double* w) {
     switch (nv) {
 #define FOS_MDOT(K) \
-  case K: fos_launch(c, k_mdot<K>, kRedBlocks, kT, wk.N, V, ldv, w, wk.part); break;
+  case K: fos_launch(c, k_mdot<K, NRM>, kRedBlocks, kT, wk.N, V, ldv, w, wk.part); break;
       FOS_MDOT(1) FOS_MDOT(2) FOS_MDOT(3) FOS_MDOT(4) FOS_MDOT(5) FOS_MDOT(6) FOS_MDOT(7)
       FOS_MDOT(8) FOS_MDOT(9) FOS_MDOT(10) FOS_MDOT(11) FOS_MDOT(12) FOS_MDOT(13) FOS_MDOT(14)
       FOS_MDOT(15) FOS_MDOT(16) FOS_MDOT(17) FOS_MDOT(18) FOS_MDOT(19) FOS_MDOT(20) FOS_MDOT(21)
@@ -295,11 +299,12 @@ struct Driver {
     return fos_residual_launch(c, y, v, c->d_scal + 1, fy, w, 1.0, -gamma, 1);
   }
 
+  long reorth = 0;
   // GMRES on J_G d = b; d starts at zero
   int gmres(const double* y, const double* fy, double gamma, double ynorm, double bnorm, int* its) {
     const long N = wk.N;
     const int m = o.maxl;
-    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), yv(m), hbuf(3 * kMaxVec);
+    std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), yv(m), hbuf(4 * kMaxVec);
     FOS_CUDA(cudaMemsetAsync(wk.d, 0, sizeof(double) * N, c->stream));
     *its = 0;
     if (bnorm == 0.0) return 0;
@@ -320,16 +325,27 @@ struct Driver {
         if (rc) return rc;
         (*its)++;
         const int nv = j + 1;
-        if ((rc = mdot(nv, wk.V, N, wk.w))) return rc;
-        if ((rc = reduce(nv, wk.sc))) return rc;
-        if ((rc = update<0>(nv, wk.V, N, wk.sc, wk.w))) return rc;
-        if ((rc = reduce(nv, wk.sc + kMaxVec))) return rc;
-        if ((rc = update<1>(nv, wk.V, N, wk.sc + kMaxVec, wk.w))) return rc;
-        if ((rc = reduce(1, wk.sc + 2 * kMaxVec))) return rc;
-        if ((rc = fetch(wk.sc, hbuf.data(), 3 * kMaxVec))) return rc;
+        // classical Gram--Schmidt, re-orthogonalised only when the first pass removed more
+        // than 1 - 1/sqrt(2) of ||w|| (Daniel--Gragg--Kaufman--Stewart criterion)
+        if ((rc = mdot<true>(nv, wk.V, N, wk.w))) return rc;           // h, ||w||^2
+        if ((rc = reduce(nv + 1, wk.sc))) return rc;
+        if ((rc = update<1>(nv, wk.V, N, wk.sc, wk.w))) return rc;     // w -= V h, ||w||^2
+        if ((rc = reduce(1, wk.sc + kMaxVec))) return rc;
+        if ((rc = fetch(wk.sc, hbuf.data(), kMaxVec + 1))) return rc;
         double* col = &H[(size_t)(m + 1) * j];
-        for (int l = 0; l < nv; l++) col[l] = hbuf[l] + hbuf[kMaxVec + l];
-        const double hn = std::sqrt(hbuf[2 * kMaxVec]);
+        for (int l = 0; l < nv; l++) col[l] = hbuf[l];
+        double hn2 = hbuf[kMaxVec];
+        if (hn2 < 0.5 * hbuf[nv]) {
+          if ((rc = mdot<false>(nv, wk.V, N, wk.w))) return rc;
+          if ((rc = reduce(nv, wk.sc + 2 * kMaxVec))) return rc;
+          if ((rc = update<1>(nv, wk.V, N, wk.sc + 2 * kMaxVec, wk.w))) return rc;
+          if ((rc = reduce(1, wk.sc + 3 * kMaxVec))) return rc;
+          if ((rc = fetch(wk.sc + 2 * kMaxVec, hbuf.data() + 2 * kMaxVec, kMaxVec + 1))) return rc;
+          for (int l = 0; l < nv; l++) col[l] += hbuf[2 * kMaxVec + l];
+          hn2 = hbuf[3 * kMaxVec];
+          reorth++;
+        }
+        const double hn = std::sqrt(hn2);
         col[j + 1] = hn;
         if (hn > 0.0) fos_launch(c, k_scale, nb(N), kT, N, wk.w, 1.0 / hn, wk.V + (size_t)(j + 1) * N);
         for (int l = 0; l < j; l++) {
@@ -352,9 +368,10 @@ struct Driver {
         for (int q = l + 1; q < kend; q++) s -= H[l + (size_t)(m + 1) * q] * yv[q];
         yv[l] = s / H[l + (size_t)(m + 1) * l];
       }
-      FOS_CUDA(cudaMemcpyAsync(wk.sc + 3 * kMaxVec, yv.data(), sizeof(double) * kend,
+      FOS_CUDA(cudaMemcpyAsync(wk.sc + 4 * kMaxVec, yv.data(), sizeof(double) * kend,
                                cudaMemcpyHostToDevice, c->stream));
-      fos_launch(c, k_comb, nb(N), kT, N, kend, wk.Z, N, wk.sc + 3 * kMaxVec, wk.d);
+      fos_launch(c, k_comb, nb(N), kT, N, kend, (const double*)wk.Z, N,
+                 (const double*)(wk.sc + 4 * kMaxVec), wk.d);
       FOS_LAUNCH_CHECK();
       if (conv || cyc == o.max_restarts) return conv ? 0 : 1;
       // restart from the true residual r = b - J_G d

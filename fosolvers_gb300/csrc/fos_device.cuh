@@ -90,3 +90,53 @@ static __device__ __noinline__ void ghost_state(int type, const double* __restri
   }
 }
 
+
+// ------------------------------------------------------------------ FP64-pipe-free helpers
+// GB300 executes FP64 arithmetic and FP64<->FP32 conversions at a small fraction of the FP32
+// rate, so the FP32 kernels convert with integer instructions on the IEEE-754 fields.
+
+// binary32 -> binary64 by re-biasing the exponent field (exact for normal numbers and zero;
+// binary32 subnormals flush to zero; inf / nan stay inf / nan)
+__device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xffu;
+  const unsigned long long sgn = (unsigned long long)(b >> 31) << 63;
+  const unsigned long long man = (unsigned long long)(b & 0x7fffffu) << 29;
+  const unsigned long long e64 = (e == 0xffu) ? 0x7ffull : (unsigned long long)(e + 896u);
+  const unsigned long long bits = (e == 0u) ? sgn : (sgn | (e64 << 52) | man);
+  return __longlong_as_double((long long)bits);
+}
+
+// binary64 -> binary32 keeping the top 23 fraction bits (rounding toward zero); magnitudes
+// below the binary32 normal range flush to zero, above it become infinity
+__device__ __forceinline__ float d2f_trunc(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned sgn = (unsigned)(b >> 63) << 31;
+  const int e = (int)((b >> 52) & 0x7ffull);
+  const unsigned man = (unsigned)((b >> 29) & 0x7fffffull);
+  const int e32 = e - 896;
+  unsigned bits;
+  if (e == 0x7ff) bits = sgn | 0x7f800000u | (man ? 0x400000u : 0u);
+  else if (e32 <= 0) bits = sgn;
+  else if (e32 >= 255) bits = sgn | 0x7f800000u;
+  else bits = sgn | ((unsigned)e32 << 23) | man;
+  return __uint_as_float(bits);
+}
+
+// x = hi + lo with hi = x's top 24 significand bits (exact) and lo = the rest rounded toward
+// zero to 24 bits: one FP64 subtraction, the rest integer instructions
+__device__ __forceinline__ void split_hl_bits(double x, float& hi, float& lo) {
+  const double xh = __longlong_as_double(__double_as_longlong(x) & ~0x1fffffffll);
+  hi = d2f_trunc(xh);
+  lo = d2f_trunc(x - xh);
+}
+
+// 1/a in FP64 by Newton--Raphson iteration x <- x (2 - a x) from an FP32 seed (two steps
+// take the ~2^-23 seed error to the FP64 rounding level); four FP64 FMAs
+__device__ __forceinline__ double rcp64(double a) {
+  double x = f2d_bits(__frcp_rn(d2f_trunc(a)));
+  double e = fma(-a, x, 1.0);
+  x = fma(x, e, x);
+  e = fma(-a, x, 1.0);
+  return fma(x, e, x);
+}

@@ -98,7 +98,7 @@ struct fos_ctx {
   int ilu_colors = 0;            // > 0: ILU order is colour-major (FOS_ILU_COLOR)
   bool has_factor = false;
   std::vector<int> h_ilu_pos;     // ILU position of every internal row
-  double* d_ilu_tmp = nullptr;  // [5*nC]
+  double* d_ilu_tmp = nullptr;  // two AoS sweep vectors, 8 values per row each
   fos_bdf_work* bdf = nullptr;  // driver workspace, kept between calls
   long n_launch = 0;            // kernels launched through fos_launch
 

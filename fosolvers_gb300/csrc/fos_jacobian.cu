@@ -216,101 +216,149 @@ __device__ __forceinline__ bool inv5(T a[25]) {
   return ok;
 }
 
-// One level of the block ILU(0) factorisation, one thread per block row i:
+// One level of the block ILU(0) factorisation, five lanes per block row i (lane a owns
+// row a of every block of row i; six rows per warp):
 //   LU_i* = P_i* = delta - gamma/v_i J_i*          (copy of the row, fused)
 //   for k in lower(i) (ILU order): LU_ik = LU_ik inv(D_k); LU_ij -= LU_ik LU_kj (j in row i)
-//   D_i = LU_ii -> stored inverted
-// Rows of one level only read finished rows of earlier levels and write their own row.
+//   D_i = LU_ii -> inverted by Gauss--Jordan across the five lanes (shuffles)
+// A lane only reads its own row of row i's blocks and whole blocks of finished rows, so
+// the lanes of a row need no synchronisation until the diagonal inversion.
 template <typename TF>
-__global__ void __launch_bounds__(kT) k_ilu_factor_level(
+__global__ void __launch_bounds__(kT) k_ilu_factor5(
     int n, const int* __restrict__ rows, const int* __restrict__ rowptr,
     const int* __restrict__ diag, const double* __restrict__ invV, double gamma,
     const double* __restrict__ J, const int* __restrict__ upd_ptr, const int3* __restrict__ upd,
     TF* __restrict__ LU, int* __restrict__ ierr) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  const int i = rows[t];
-  const double s = gamma * invV[i];
-  for (int sl = rowptr[i]; sl < rowptr[i + 1]; sl++) {
-    const double* src = J + 25 * (size_t)sl;
-    TF* dst = LU + 25 * (size_t)sl;
-    const bool dg = sl == diag[i];
-#pragma unroll
-    for (int k = 0; k < 25; k++) dst[k] = (TF)(((dg && k / 5 == k % 5) ? 1.0 : 0.0) - s * src[k]);
-  }
-  for (int o = upd_ptr[i]; o < upd_ptr[i + 1]; o++) {
-    const int3 op = upd[o];
-    TF A[25], B[25];
-#pragma unroll
-    for (int k = 0; k < 25; k++) { A[k] = LU[25 * (size_t)op.x + k]; B[k] = LU[25 * (size_t)op.y + k]; }
-    TF* dst = LU + 25 * (size_t)(op.z < 0 ? op.x : op.z);
-#pragma unroll
-    for (int a = 0; a < 5; a++)
-#pragma unroll
-      for (int b = 0; b < 5; b++) {
-        TF acc = op.z < 0 ? TF(0) : dst[5 * a + b];
-        TF p = 0;
-#pragma unroll
-        for (int k = 0; k < 5; k++) p += A[5 * a + k] * B[5 * k + b];
-        dst[5 * a + b] = op.z < 0 ? p : acc - p;
-      }
-  }
-  TF D[25];
-  TF* dd = LU + 25 * (size_t)diag[i];
-#pragma unroll
-  for (int k = 0; k < 25; k++) D[k] = dd[k];
-  if (!inv5(D)) {
-    atomicMin(ierr, i + 1);
-    return;
-  }
-#pragma unroll
-  for (int k = 0; k < 25; k++) dd[k] = D[k];
-}
-
-// Triangular sweeps, five lanes per block row (lane a owns component a and reads row a
-// of every 5x5 block: 40 contiguous bytes per lane, 200 per row).
-//   forward:  y_i = r_i - sum_{k in lower(i)} L_ik y_k           (unit block diagonal)
-//   backward: z_i = inv(D_i) (y_i - sum_{j in upper(i)} U_ij z_j)
-template <typename TF, bool FWD>
-__global__ void __launch_bounds__(kT) k_ilu_sweep(int n, int nC, const int* __restrict__ rows,
-                                                  const int* __restrict__ rowptr,
-                                                  const int* __restrict__ col,
-                                                  const int* __restrict__ diag,
-                                                  const TF* __restrict__ LU,
-                                                  const double* __restrict__ in,
-                                                  double* __restrict__ out) {
   const int lane = threadIdx.x & 31;
-  const int sub = lane / 5, a = lane - 5 * sub;  // 6 rows per warp, lanes 30, 31 idle
+  const int sub = lane / 5, a = lane - 5 * sub;
   const int t = (blockIdx.x * blockDim.x + threadIdx.x) / 32 * 6 + sub;
   const bool active = sub < 6 && t < n;
   const int i = active ? rows[t] : 0;
-  TF acc = active ? (TF)in[(size_t)a * nC + i] : TF(0);
+  TF D[5] = {TF(0), TF(0), TF(0), TF(0), TF(0)};
   if (active) {
-    const int s0 = FWD ? rowptr[i] : diag[i] + 1;
-    const int s1 = FWD ? diag[i] : rowptr[i + 1];
-    for (int s = s0; s < s1; s++) {
-      const int k = col[s];
-      const TF* B = LU + 25 * (size_t)s + 5 * a;
+    const double s = gamma * invV[i];
+    for (int sl = rowptr[i]; sl < rowptr[i + 1]; sl++) {
+      const double* src = J + 25 * (size_t)sl + 5 * a;
+      TF* dst = LU + 25 * (size_t)sl + 5 * a;
+      const bool dg = sl == diag[i];
 #pragma unroll
-      for (int b = 0; b < 5; b++) acc -= __ldg(B + b) * (TF)out[(size_t)b * nC + k];
+      for (int b = 0; b < 5; b++) dst[b] = (TF)(((dg && b == a) ? 1.0 : 0.0) - s * src[b]);
+    }
+    for (int o = upd_ptr[i]; o < upd_ptr[i + 1]; o++) {
+      const int3 op = upd[o];
+      TF A[5];
+#pragma unroll
+      for (int k = 0; k < 5; k++) A[k] = LU[25 * (size_t)op.x + 5 * a + k];
+      const TF* B = LU + 25 * (size_t)op.y;
+      TF* dst = LU + 25 * (size_t)(op.z < 0 ? op.x : op.z) + 5 * a;
+#pragma unroll
+      for (int b = 0; b < 5; b++) {
+        TF p = 0;
+#pragma unroll
+        for (int k = 0; k < 5; k++) p += A[k] * B[5 * k + b];
+        dst[b] = op.z < 0 ? p : dst[b] - p;
+      }
+    }
+#pragma unroll
+    for (int b = 0; b < 5; b++) D[b] = LU[25 * (size_t)diag[i] + 5 * a + b];
+  }
+  // Gauss--Jordan without pivoting: step k broadcasts row k (lane base + k)
+  const int base = lane - a;
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < 5; k++) {
+    TF rk[5];
+#pragma unroll
+    for (int b = 0; b < 5; b++) rk[b] = __shfl_sync(0xffffffffu, D[b], base + k < 32 ? base + k : 0);
+    const TF piv = rk[k];
+    ok &= !(active && piv == TF(0));
+    const TF ip = TF(1) / piv;
+    if (a == k) {
+#pragma unroll
+      for (int b = 0; b < 5; b++) D[b] = (b == k) ? ip : D[b] * ip;
+    } else {
+      const TF f = D[k];
+#pragma unroll
+      for (int b = 0; b < 5; b++) D[b] = (b == k) ? -f * ip : D[b] - f * (rk[b] * ip);
     }
   }
-  if (FWD) {
-    if (active) out[(size_t)a * nC + i] = (double)acc;
-    return;
+  if (!active) return;
+  if (!ok) atomicMin(ierr, i + 1);
+#pragma unroll
+  for (int b = 0; b < 5; b++) LU[25 * (size_t)diag[i] + 5 * a + b] = D[b];
+}
+
+// Triangular sweeps, five lanes per block row (lane a owns component a and reads row a
+// of every 5x5 block).  Intermediate vectors are AoS in TF (8 per row, 32 / 64 B), so the
+// neighbour values of a row are one sector; r (in) and z (out) are the FP64 SoA vectors.
+//   forward:  y_i = r_i - sum_{k in lower(i)} L_ik y_k           (unit block diagonal)
+//   backward: z_i = inv(D_i) (y_i - sum_{j in upper(i)} U_ij z_j)
+template <typename TF>
+__device__ __forceinline__ TF from64(double x) {
+  if constexpr (sizeof(TF) == 4) return d2f_trunc(x); else return (TF)x;
+}
+template <typename TF>
+__device__ __forceinline__ double to64(TF x) {
+  if constexpr (sizeof(TF) == 4) return f2d_bits(x); else return (double)x;
+}
+
+template <typename TF>
+__global__ void __launch_bounds__(kT) k_ilu_fwd5(int n, int nC, const int* __restrict__ rows,
+                                                 const int* __restrict__ rowptr,
+                                                 const int* __restrict__ col,
+                                                 const int* __restrict__ diag,
+                                                 const TF* __restrict__ LU,
+                                                 const double* __restrict__ r,
+                                                 TF* __restrict__ yv) {
+  const int lane = threadIdx.x & 31;
+  const int sub = lane / 5, a = lane - 5 * sub;
+  const int t = (blockIdx.x * blockDim.x + threadIdx.x) / 32 * 6 + sub;
+  if (sub >= 6 || t >= n) return;
+  const int i = rows[t];
+  TF acc = from64<TF>(r[(size_t)a * nC + i]);
+  for (int s = rowptr[i]; s < diag[i]; s++) {
+    const TF* yk = yv + 8 * (size_t)col[s];
+    const TF* B = LU + 25 * (size_t)s + 5 * a;
+#pragma unroll
+    for (int b = 0; b < 5; b++) acc -= __ldg(B + b) * yk[b];
   }
-  // z_i = inv(D_i) acc: exchange the five components of the row through shuffles
+  yv[8 * (size_t)i + a] = acc;
+}
+
+template <typename TF>
+__global__ void __launch_bounds__(kT) k_ilu_bwd5(int n, int nC, const int* __restrict__ rows,
+                                                 const int* __restrict__ rowptr,
+                                                 const int* __restrict__ col,
+                                                 const int* __restrict__ diag,
+                                                 const TF* __restrict__ LU,
+                                                 const TF* __restrict__ yv,
+                                                 TF* __restrict__ zv, double* __restrict__ z) {
+  const int lane = threadIdx.x & 31;
+  const int sub = lane / 5, a = lane - 5 * sub;
+  const int t = (blockIdx.x * blockDim.x + threadIdx.x) / 32 * 6 + sub;
+  const bool active = sub < 6 && t < n;
+  const int i = active ? rows[t] : 0;
+  TF acc = TF(0);
+  if (active) {
+    acc = yv[8 * (size_t)i + a];
+    for (int s = diag[i] + 1; s < rowptr[i + 1]; s++) {
+      const TF* zj = zv + 8 * (size_t)col[s];
+      const TF* B = LU + 25 * (size_t)s + 5 * a;
+#pragma unroll
+      for (int b = 0; b < 5; b++) acc -= __ldg(B + b) * zj[b];
+    }
+  }
   TF comp[5];
   const int base = lane - a;
 #pragma unroll
   for (int b = 0; b < 5; b++) comp[b] = __shfl_sync(0xffffffffu, acc, base + b < 32 ? base + b : 0);
-  if (active) {
-    const TF* D = LU + 25 * (size_t)diag[i] + 5 * a;
-    TF z = 0;
+  if (!active) return;
+  const TF* Dr = LU + 25 * (size_t)diag[i] + 5 * a;
+  TF zz = 0;
 #pragma unroll
-    for (int b = 0; b < 5; b++) z += __ldg(D + b) * comp[b];
-    out[(size_t)a * nC + i] = (double)z;
-  }
+  for (int b = 0; b < 5; b++) zz += __ldg(Dr + b) * comp[b];
+  zv[8 * (size_t)i + a] = zz;
+  z[(size_t)a * nC + i] = to64<TF>(zz);
 }
 
 }  // namespace
@@ -453,7 +501,7 @@ int fos_jac_setup(fos_ctx* c) {
     return -100;
   FOS_CUDA(cudaMalloc((void**)&c->d_J, 25 * sizeof(double) * (size_t)c->nnzb));
   FOS_CUDA(cudaMalloc((void**)&c->d_Jb, 25 * sizeof(double) * (size_t)std::max(c->nFb, 1)));
-  FOS_CUDA(cudaMalloc((void**)&c->d_ilu_tmp, 5 * sizeof(double) * (size_t)nC));
+  FOS_CUDA(cudaMalloc((void**)&c->d_ilu_tmp, 16 * sizeof(double) * (size_t)nC));  // 2 AoS vectors
   FOS_CUDA(cudaMalloc((void**)&c->d_ierr, sizeof(int)));
   if (c->flags & FOS_ILU_FP32)
     FOS_CUDA(cudaMalloc((void**)&c->d_LU32, 25 * sizeof(float) * (size_t)c->nnzb));
@@ -490,11 +538,11 @@ int fos_ilu_factor(fos_ctx* c, double gamma) {
     const int n = c->lev_f[l + 1] - c->lev_f[l];
     const int* rows = c->d_lrows_f + c->lev_f[l];
     if (c->flags & FOS_ILU_FP32)
-      fos_launch(c, k_ilu_factor_level<float>, nb(n), kT, n, rows, (const int*)c->d_rowptr,
+      fos_launch(c, k_ilu_factor5<float>, nb_rows5(n), kT, n, rows, (const int*)c->d_rowptr,
                  (const int*)c->d_diag, (const double*)c->d_invV, gamma, (const double*)c->d_J,
                  (const int*)c->d_upd_ptr, (const int3*)c->d_upd, c->d_LU32, c->d_ierr);
     else
-      fos_launch(c, k_ilu_factor_level<double>, nb(n), kT, n, rows, (const int*)c->d_rowptr,
+      fos_launch(c, k_ilu_factor5<double>, nb_rows5(n), kT, n, rows, (const int*)c->d_rowptr,
                  (const int*)c->d_diag, (const double*)c->d_invV, gamma, (const double*)c->d_J,
                  (const int*)c->d_upd_ptr, (const int3*)c->d_upd, c->d_LU, c->d_ierr);
   }
@@ -508,35 +556,29 @@ int fos_ilu_factor(fos_ctx* c, double gamma) {
   return 0;
 }
 
-int fos_ilu_apply(fos_ctx* c, const double* r, double* z) {
-  double* tmp = c->d_ilu_tmp;
-  const bool f32 = (c->flags & FOS_ILU_FP32) != 0;
+template <typename TF>
+static int ilu_apply_t(fos_ctx* c, const TF* LU, const double* r, double* z) {
+  TF* yv = reinterpret_cast<TF*>(c->d_ilu_tmp);
+  TF* zv = yv + 8 * (size_t)c->nC;
   for (int l = 0; l < c->ilu_nlev_f; l++) {
     const int n = c->lev_f[l + 1] - c->lev_f[l];
-    const int* rows = c->d_lrows_f + c->lev_f[l];
-    if (f32)
-      fos_launch(c, k_ilu_sweep<float, true>, nb_rows5(n), kT, n, c->nC, rows,
-                 (const int*)c->d_rowptr, (const int*)c->d_col, (const int*)c->d_diag,
-                 (const float*)c->d_LU32, r, tmp);
-    else
-      fos_launch(c, k_ilu_sweep<double, true>, nb_rows5(n), kT, n, c->nC, rows,
-                 (const int*)c->d_rowptr, (const int*)c->d_col, (const int*)c->d_diag,
-                 (const double*)c->d_LU, r, tmp);
+    fos_launch(c, k_ilu_fwd5<TF>, nb_rows5(n), kT, n, c->nC,
+               (const int*)(c->d_lrows_f + c->lev_f[l]), (const int*)c->d_rowptr,
+               (const int*)c->d_col, (const int*)c->d_diag, LU, r, yv);
   }
   for (int l = 0; l < c->ilu_nlev_b; l++) {
     const int n = c->lev_b[l + 1] - c->lev_b[l];
-    const int* rows = c->d_lrows_b + c->lev_b[l];
-    if (f32)
-      fos_launch(c, k_ilu_sweep<float, false>, nb_rows5(n), kT, n, c->nC, rows,
-                 (const int*)c->d_rowptr, (const int*)c->d_col, (const int*)c->d_diag,
-                 (const float*)c->d_LU32, (const double*)tmp, z);
-    else
-      fos_launch(c, k_ilu_sweep<double, false>, nb_rows5(n), kT, n, c->nC, rows,
-                 (const int*)c->d_rowptr, (const int*)c->d_col, (const int*)c->d_diag,
-                 (const double*)c->d_LU, (const double*)tmp, z);
+    fos_launch(c, k_ilu_bwd5<TF>, nb_rows5(n), kT, n, c->nC,
+               (const int*)(c->d_lrows_b + c->lev_b[l]), (const int*)c->d_rowptr,
+               (const int*)c->d_col, (const int*)c->d_diag, LU, (const TF*)yv, zv, z);
   }
   FOS_LAUNCH_CHECK();
   return 0;
+}
+
+int fos_ilu_apply(fos_ctx* c, const double* r, double* z) {
+  if (c->flags & FOS_ILU_FP32) return ilu_apply_t<float>(c, c->d_LU32, r, z);
+  return ilu_apply_t<double>(c, c->d_LU, r, z);
 }
 
 extern "C" long fos_euler_jac_copy(fos_ctx* c, int* rowptr, int* col, double* val) {

@@ -179,12 +179,11 @@ __device__ __forceinline__ void gather_epilogue(int nC, int c, const double acc[
       out[(size_t)q * nC + c] = o;
     }
   } else {
-    const double s = *d_s;
+    const double bs = d_s[0] > 0.0 ? b * d_s[1] : 0.0;  // b / s
 #pragma unroll
     for (int q = 0; q < 5; q++) {
       const size_t k = (size_t)q * nC + c;
-      double o = a * vv[k];
-      if (s > 0.0) o += b * ((acc[q] * iv - fy[k]) / s);
+      const double o = fma(bs, fma(acc[q], iv, -fy[k]), a * vv[k]);
       bad |= !isfinite(o);
       out[k] = o;
     }
@@ -220,10 +219,6 @@ __global__ void __launch_bounds__(kThreads) k_gather(
 // so a face jump (hR - hL) + (lR - lL) keeps FP32 relative accuracy of the jump itself
 // while the face kernel issues FP32 instructions only.  Layout: 16 floats (64 B) per cell
 // = (rho, u, v, w, H, p) hi, (rho, u, v, w, H, p) lo, sqrt(rho), 0, 0, 0.
-__device__ __forceinline__ void split_hl(double x, float& h, float& l) {
-  h = (float)x;
-  l = (float)(x - (double)h);
-}
 __global__ void __launch_bounds__(kThreads) k_prim_hl(int nC, const double* __restrict__ y,
                                                       const double* __restrict__ v,
                                                       const double* __restrict__ d_s, double gm1,
@@ -236,22 +231,24 @@ __global__ void __launch_bounds__(kThreads) k_prim_hl(int nC, const double* __re
   if (v) {
     const double s = *d_s;
 #pragma unroll
-    for (int q = 0; q < 5; q++) U[q] = U[q] + s * v[(size_t)q * nC + c];
+    for (int q = 0; q < 5; q++) U[q] = fma(s, v[(size_t)q * nC + c], U[q]);
   }
-  P64 P;
-  prim_from_cons(U[0], U[1], U[2], U[3], U[4], gm1, P);
+  const double inv = rcp64(U[0]);
+  const double u = U[1] * inv, vv = U[2] * inv, w = U[3] * inv;
+  const double p = gm1 * (U[4] - 0.5 * (U[1] * u + U[2] * vv + U[3] * w));
+  const double H = (U[4] + p) * inv;
   float h[6], l[6];
-  split_hl(P.rho, h[0], l[0]);
-  split_hl(P.u, h[1], l[1]);
-  split_hl(P.v, h[2], l[2]);
-  split_hl(P.w, h[3], l[3]);
-  split_hl(P.H, h[4], l[4]);
-  split_hl(P.p, h[5], l[5]);
+  split_hl_bits(U[0], h[0], l[0]);
+  split_hl_bits(u, h[1], l[1]);
+  split_hl_bits(vv, h[2], l[2]);
+  split_hl_bits(w, h[3], l[3]);
+  split_hl_bits(H, h[4], l[4]);
+  split_hl_bits(p, h[5], l[5]);
   float4* w4 = reinterpret_cast<float4*>(W + 16 * (size_t)c);
   w4[0] = make_float4(h[0], h[1], h[2], h[3]);
   w4[1] = make_float4(h[4], h[5], l[0], l[1]);
   w4[2] = make_float4(l[2], l[3], l[4], l[5]);
-  w4[3] = make_float4((float)P.s, 0.0f, 0.0f, 0.0f);
+  w4[3] = make_float4(sqrtf(h[0] + l[0]), 0.0f, 0.0f, 0.0f);
 }
 
 struct PHL {
@@ -386,14 +383,14 @@ __global__ void __launch_bounds__(kThreads) k_gather32(
 #pragma unroll
   for (int k = 0; k < kW; k++) {
     if (e[k] < 0) continue;
-    const double sw = (e[k] & 1) ? 1.0 : -1.0;
+    const float sw = (e[k] & 1) ? 1.0f : -1.0f;  // R: -(dF + dw), L: -(dF - dw)
     const float4* F4 = reinterpret_cast<const float4*>(F + 12 * (size_t)(e[k] >> 1));
     const float4 a0 = __ldg(F4), a1 = __ldg(F4 + 1), a2 = __ldg(F4 + 2);
-    acc[0] -= (double)a0.x + sw * (double)a0.y;
-    acc[1] -= (double)a0.z + sw * (double)a0.w;
-    acc[2] -= (double)a1.x + sw * (double)a1.y;
-    acc[3] -= (double)a1.z + sw * (double)a1.w;
-    acc[4] -= (double)a2.x + sw * (double)a2.y;
+    acc[0] -= f2d_bits(fmaf(sw, a0.y, a0.x));
+    acc[1] -= f2d_bits(fmaf(sw, a0.w, a0.z));
+    acc[2] -= f2d_bits(fmaf(sw, a1.y, a1.x));
+    acc[3] -= f2d_bits(fmaf(sw, a1.w, a1.z));
+    acc[4] -= f2d_bits(fmaf(sw, a2.y, a2.x));
   }
   gather_epilogue(nC, c, acc, __ldg(invV + c), mode, vv, fy, d_s, a, b, out, flag);
 }
@@ -446,7 +443,9 @@ __global__ void k_sum_final(const double* __restrict__ part, int np, double* __r
 
 __global__ void k_sigma(double* scal, double ynorm, double eps) {
   const double vn2 = scal[0];
-  scal[1] = vn2 > 0.0 ? eps * (1.0 + ynorm) / sqrt(vn2) : 0.0;
+  const double s = vn2 > 0.0 ? eps * (1.0 + ynorm) / sqrt(vn2) : 0.0;
+  scal[1] = s;
+  scal[2] = s > 0.0 ? 1.0 / s : 0.0;
 }
 
 inline int nblk(long n, int t = kThreads) { return (int)((n + t - 1) / t); }

@@ -1054,8 +1054,8 @@ int oe_ilu_ierr(const oe_ctx* c) { return c->ierr; }
  * callbacks by (SUNDIALS.f90:745-845; foeuler.f90:171-174,450):
  *   G(y) = y - gamma f(t,y) - h,  gamma = beta*dt, h = history combination
  *   J_G v ~ v - gamma (f(y + s v) - f(y))/s,  s = jv_eps (1 + ||y||_2)/||v||_2
- *   right-preconditioned restarted GMRES(maxl), classical Gram-Schmidt with one
- *   re-orthogonalisation (CGS2), Givens least squares, stop at ||r|| <= lin_rtol ||b||
+ *   right-preconditioned restarted GMRES(maxl), classical Gram-Schmidt with a second
+ *   pass when ||w1||^2 < ||w0||^2/2 (DGKS), Givens least squares, stop at ||r|| <= lin_rtol ||b||
  *   Newton stops when ||G(y_k)||_2 <= rtol ||y_n||_2 + atol sqrt(n) (FP64 residual norm). */
 typedef struct {
   int n;
@@ -1129,13 +1129,18 @@ static int nk_gmres(nk_op* op, const double* b, double* x, int m, int max_restar
       rc = nk_matvec(op, zj, w);
       if (rc) { status = rc < 0 ? rc : -2; goto done; }
       it++;
-      /* CGS2 */
+      /* classical Gram--Schmidt; second pass only when ||w1||^2 < ||w0||^2 / 2 (DGKS) */
+      double w0 = vdot(n, w, w);
       for (int l = 0; l <= j; l++) h[l] = vdot(n, V + (size_t)n * l, w);
       for (int l = 0; l <= j; l++) { const double* vl = V + (size_t)n * l; for (int i = 0; i < n; i++) w[i] -= h[l] * vl[i]; }
-      for (int l = 0; l <= j; l++) h2[l] = vdot(n, V + (size_t)n * l, w);
-      for (int l = 0; l <= j; l++) { const double* vl = V + (size_t)n * l; for (int i = 0; i < n; i++) w[i] -= h2[l] * vl[i]; }
-      for (int l = 0; l <= j; l++) h[l] += h2[l];
-      double hn = sqrt(vdot(n, w, w));
+      double w1 = vdot(n, w, w);
+      if (w1 < 0.5 * w0) {
+        for (int l = 0; l <= j; l++) h2[l] = vdot(n, V + (size_t)n * l, w);
+        for (int l = 0; l <= j; l++) { const double* vl = V + (size_t)n * l; for (int i = 0; i < n; i++) w[i] -= h2[l] * vl[i]; }
+        for (int l = 0; l <= j; l++) h[l] += h2[l];
+        w1 = vdot(n, w, w);
+      }
+      double hn = sqrt(w1);
       for (int l = 0; l <= j; l++) H[l + (size_t)(m + 1) * j] = h[l];
       H[j + 1 + (size_t)(m + 1) * j] = hn;
       if (hn > 0.0) { double* vn = V + (size_t)n * (j + 1); for (int i = 0; i < n; i++) vn[i] = w[i] / hn; }

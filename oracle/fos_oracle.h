@@ -125,7 +125,7 @@ typedef struct {
   double last_gnorm;
 } o_bdf_stats;
 void o_bdf_defaults(o_bdf_opts* o);
-/* fixed-step BDF1/BDF2 Newton--GMRES(maxl) with right preconditioning, CGS2 Arnoldi.
+/* fixed-step BDF1/BDF2 Newton--GMRES(maxl) with right preconditioning, CGS + DGKS Arnoldi.
  * y in/out (length n). returns 0 on success, >0 if a step failed to converge. */
 int o_bdf_run(int n, o_rhs_fn rhs, o_pset_fn pset, o_psol_fn psol, void* ud, double t0,
               double* y, const o_bdf_opts* opts, o_bdf_stats* st);
