@@ -57,6 +57,7 @@ _SIGS = {
     "fos_euler_pset": (C.c_int, [C.c_double, _dp, _dp, C.c_int, _ip, C.c_double, _vp]),
     "fos_euler_psol": (C.c_int, [C.c_double, _dp, _dp, _dp, _dp, C.c_double, C.c_double, C.c_int, _vp]),
     "fos_euler_rhs_dev": (C.c_int, [_vp, C.c_double, _vp, _vp]),
+    "fos_euler_rhs_dev_static": (C.c_int, [_vp, C.c_double, _vp, _vp]),
     "fos_euler_jv_dev": (C.c_int, [_vp, C.c_double, _vp, _vp, _vp, _vp, C.c_double, C.c_double,
                                    C.c_double, C.c_double]),
     "fos_euler_pset_dev": (C.c_int, [_vp, C.c_double, _vp, C.c_int, _ip, C.c_double]),

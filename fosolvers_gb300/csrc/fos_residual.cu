@@ -14,6 +14,8 @@
 // The FP32-flux variant (FOS_FLUX_FP32) computes the same flow in FP32 from FP64 means
 // and jumps, in flux-difference form, and accumulates it in FP64 (see roe_split_mixed).
 #include <cmath>
+#include <mutex>
+#include <string>
 
 #include "fos_internal.h"
 #include "fos_device.cuh"
@@ -515,6 +517,105 @@ int fos_jv_sigma(fos_ctx* c, double* d_scal, double ynorm, double eps) {
 int fos_permute(fos_ctx* c, const double* in, double* out, int dir) {
   const int* idx = dir == 0 ? c->d_new2old : c->d_old2new;
   fos_launch(c, k_permute, nblk(5L * c->nC), kThreads, c->nC, idx, in, out);
+  FOS_LAUNCH_CHECK();
+  return 0;
+}
+
+// ------------------------------------------------------------------ allocation-free residual
+// fos_euler_rhs_dev_static: the residual of fos_euler_rhs_dev for callers that cannot
+// allocate device memory when they evaluate it -- a host code that hands the library a
+// fixed memory budget and owns every allocation itself, or one that must not allocate
+// inside its time loop.  Its scratch (per-cell primitives, 64 B per cell, and per-face
+// flows, 48 B per face) lives in this file-scope device array instead of the context's
+// buffers.  Every device that loads the library holds the array (10.75 MiB) until exit.
+constexpr int kStaticMaxCells = FOS_STATIC_MAX_CELLS;
+constexpr int kStaticMaxFaces = FOS_STATIC_MAX_FACES;
+constexpr size_t kStaticCellBytes = 64ull * kStaticMaxCells;
+static __device__ __align__(256) unsigned char g_rhs_scratch[kStaticCellBytes +
+                                                             48ull * kStaticMaxFaces];
+
+namespace {
+constexpr int kStaticMaxDevices = 64;
+std::mutex g_static_mu;
+void* g_static_addr[kStaticMaxDevices] = {nullptr};  // device address of g_rhs_scratch
+
+// Device address of the scratch array on the current device.  The host-side symbol is
+// only a stand-in, so the address is asked for once per device (with that device current).
+int static_scratch(void** out) {
+  int dev = 0;
+  FOS_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kStaticMaxDevices) {
+    fos_set_error("fos_euler_rhs_dev_static: device ordinal out of range");
+    return -1;
+  }
+  std::lock_guard<std::mutex> lock(g_static_mu);
+  if (!g_static_addr[dev]) {
+    void* p = nullptr;
+    FOS_CUDA(cudaGetSymbolAddress(&p, g_rhs_scratch));
+    g_static_addr[dev] = p;
+  }
+  *out = g_static_addr[dev];
+  return 0;
+}
+}  // namespace
+
+extern "C" int fos_euler_rhs_dev_static(const fos_ctx* c, double t, const double* y,
+                                        double* ydot) {
+  (void)t;
+  if (!c || !y || !ydot) {
+    fos_set_error("fos_euler_rhs_dev_static: bad arguments");
+    return -1;
+  }
+  if (c->nC > kStaticMaxCells || c->nF > kStaticMaxFaces) {
+    fos_set_error("fos_euler_rhs_dev_static: grid has " + std::to_string(c->nC) + " cells and " +
+                  std::to_string(c->nF) + " faces; the static scratch holds at most " +
+                  std::to_string(kStaticMaxCells) + " cells and " +
+                  std::to_string(kStaticMaxFaces) + " faces");
+    return -1;
+  }
+  int dev = 0;
+  FOS_CUDA(cudaGetDevice(&dev));
+  if (dev != c->device) {
+    fos_set_error("fos_euler_rhs_dev_static: current device differs from the context's device");
+    return -1;
+  }
+  void* base = nullptr;
+  if (int rc = static_scratch(&base)) return rc;
+  // every launch below writes all of its scratch before reading it, so nothing in the
+  // shared array needs to start at zero
+  unsigned char* bytes = static_cast<unsigned char*>(base);
+  const double gm1 = c->gamm - 1.0;
+  cudaStream_t s = c->stream;
+  if (c->flags & FOS_FLUX_FP32) {
+    float* Whl = reinterpret_cast<float*>(bytes);
+    float* F = reinterpret_cast<float*>(bytes + kStaticCellBytes);
+    k_prim_hl<<<nblk(c->nC), kThreads, 0, s>>>(c->nC, y, nullptr, nullptr, gm1, Whl);
+    k_face32i<<<nblk(c->nFi), kThreads, 0, s>>>(c->nFi, c->d_faceLR, c->d_faceNA32, Whl,
+                                                (float)gm1, F);
+    if (c->nFb)
+      k_face32b<<<nblk(c->nFb), kThreads, 0, s>>>(c->nFi, c->nF, c->nC, c->d_faceLR,
+                                                  c->d_faceNA32, y, nullptr, nullptr, c->d_bcT,
+                                                  c->d_bcP, c->maxP, c->gamm, c->r, F);
+    if (c->ell_w == 4)
+      k_gather32<4><<<nblk(c->nC), kThreads, 0, s>>>(c->nC, c->d_ell, F, c->d_invV, 0, nullptr,
+                                                     nullptr, nullptr, 0.0, 0.0, ydot, nullptr);
+    else
+      k_gather32<6><<<nblk(c->nC), kThreads, 0, s>>>(c->nC, c->d_ell, F, c->d_invV, 0, nullptr,
+                                                     nullptr, nullptr, 0.0, 0.0, ydot, nullptr);
+  } else {
+    double* W = reinterpret_cast<double*>(bytes);
+    double* F = reinterpret_cast<double*>(bytes + kStaticCellBytes);
+    k_prim64<<<nblk(c->nC), kThreads, 0, s>>>(c->nC, y, nullptr, nullptr, gm1, W);
+    k_face64<<<nblk(c->nF), kThreads, 0, s>>>(c->nFi, c->nF, c->nC, c->d_faceLR, c->d_faceNA, W,
+                                              y, nullptr, nullptr, c->d_bcT, c->d_bcP, c->maxP,
+                                              c->gamm, c->r, F);
+    if (c->ell_w == 4)
+      k_gather<4><<<nblk(c->nC), kThreads, 0, s>>>(c->nC, c->d_ell, F, c->d_invV, 0, nullptr,
+                                                   nullptr, nullptr, 0.0, 0.0, ydot, nullptr);
+    else
+      k_gather<6><<<nblk(c->nC), kThreads, 0, s>>>(c->nC, c->d_ell, F, c->d_invV, 0, nullptr,
+                                                   nullptr, nullptr, 0.0, 0.0, ydot, nullptr);
+  }
   FOS_LAUNCH_CHECK();
   return 0;
 }

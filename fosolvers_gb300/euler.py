@@ -176,6 +176,11 @@ class FOEuler:
         return check(_lib.lib().fos_euler_rhs_dev(self._h, t, y_dev.data_ptr(), ydot_dev.data_ptr()),
                      "rhs_dev")
 
+    def rhs_dev_static(self, t, y_dev, ydot_dev) -> int:
+        """rhs_dev without device allocation (scratch in the library's static array)."""
+        return check(_lib.lib().fos_euler_rhs_dev_static(self._h, t, y_dev.data_ptr(),
+                                                         ydot_dev.data_ptr()), "rhs_dev_static")
+
     def jv_dev(self, t, y_dev, fy_dev, v_dev, out_dev, a, b, ynorm, eps=0.0) -> int:
         if eps <= 0.0:
             eps = float(np.sqrt(np.finfo(np.float32).eps)) if self.flags & FLUX_FP32 \

@@ -114,6 +114,20 @@ int fos_euler_psol(double t, const double* y, const double* fy, const double* r,
 /* ------------------------------------------------------------------ device entry points */
 
 int fos_euler_rhs_dev(fos_ctx* ctx, double t, const double* y, double* ydot);
+/* The same residual as fos_euler_rhs_dev, for callers that cannot allocate device memory
+ * when they evaluate it (a host code that owns a fixed device-memory budget and does all
+ * allocation itself, or one that must not allocate inside its time loop).  It has no
+ * counterpart in the reference.  Its scratch lives in one static device array of the
+ * library (10.75 MiB on every device that loads it, held until exit) instead of the
+ * context's buffers, so it serves grids of at most FOS_STATIC_MAX_CELLS cells and
+ * FOS_STATIC_MAX_FACES faces and returns -1 beyond that.  The first call on a device looks
+ * up the array's device address (make that first call before any stream capture).  All
+ * calls share the array: calls whose kernels overlap on the GPU (other streams, other
+ * threads) race and must be serialised by the caller.  No part of the array needs to start
+ * at zero.  Non-finite results are not flagged (use fos_euler_rhs for that). */
+#define FOS_STATIC_MAX_CELLS 65536
+#define FOS_STATIC_MAX_FACES 147456
+int fos_euler_rhs_dev_static(const fos_ctx* ctx, double t, const double* y, double* ydot);
 /* Fused finite-difference Jacobian-vector product of G(y) = y - gamma f(y) - h:
  *   out = a*v + b*(f(y + s v) - fy)/s,  s = eps (1 + ||y||_2)/||v||_2
  * (the difference quotient CVODE's SPGMR forms through rhs); ynorm = ||y||_2.

@@ -1,0 +1,48 @@
+"""fos_euler_rhs_dev_static -- the residual for callers that cannot allocate device memory
+when they evaluate it (their host code owns a fixed device-memory budget, or must not
+allocate inside its time loop).  Its scratch is a static device array of the library; the
+result must equal fos_euler_rhs_dev's on two calls in a row (the second call sees the
+first call's leftovers in the shared array), within the residual tolerance used elsewhere
+(1e-11 relative), and grids larger than the array must be refused with a clear error.
+
+Collected last on purpose (file name), so a run that stops at the first failure has run
+everything else first."""
+import numpy as np
+import pytest
+
+from fosolvers_gb300 import mesh as M
+from fosolvers_gb300.euler import FLUX_FP32
+from helpers import Case, perturbed, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("flags", [0, FLUX_FP32])
+def test_static_scratch_residual_matches_rhs_dev(cuda, flags):
+    import torch
+    c = Case(M.make_workload("sine96", scale=8, seed=5), flags=flags)  # 3,072 cells
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    for seed in (1, 2):  # two calls in a row, different states
+        y = perturbed(c.y0, c.nC, seed)
+        y_ref_order = dev(y)
+        yi = torch.empty_like(y_ref_order)
+        c.gpu.to_internal(y_ref_order, yi)
+        f_dev = torch.empty_like(yi)
+        f_static = torch.full_like(yi, float("nan"))
+        c.gpu.rhs_dev(0.0, yi, f_dev)
+        assert c.gpu.rhs_dev_static(0.0, yi, f_static) == 0
+        torch.cuda.synchronize()
+        a, b = f_static.cpu().numpy(), f_dev.cpu().numpy()
+        assert np.all(np.isfinite(a))
+        assert rel_err(a, b) <= 1e-11
+
+
+def test_static_scratch_refuses_large_grid(cuda):
+    import torch
+    from fosolvers_gb300 import _lib
+    c = Case(M.make_workload("sine96", scale=24, seed=5))  # 82,944 cells > 65,536
+    y = torch.zeros(c.N, dtype=torch.float64, device="cuda")
+    out = torch.zeros_like(y)
+    rc = _lib.lib().fos_euler_rhs_dev_static(c.gpu.handle, 0.0, y.data_ptr(), out.data_ptr())
+    assert rc == -1
+    assert "at most 65536 cells" in _lib.last_error()
