@@ -31,8 +31,8 @@ extern "C" const char* fos_last_error(void) { return g_err.c_str(); }
 fos_ctx::~fos_ctx() {
   void* ptrs[] = {d_old2new, d_new2old, d_faceLR, d_faceNA, d_faceNA32, d_crow, d_cent, d_invV,
                   d_bcT, d_bcP, d_W, d_Whl, d_ell, d_F, d_stage, d_y, d_f, d_z, d_red, d_scal,
-                  d_flag, d_rowptr, d_col, d_diag, d_fslot, d_J, d_LU, d_LU32, d_lrows_f,
-                  d_lrows_b, d_upd_ptr, d_upd, d_ilu_tmp, d_Jb, d_ierr};
+                  d_flag, d_prow, d_pcol, d_pdiag, d_cdiag, d_ipos, d_ord, d_fslot, d_Jraw,
+                  d_LU, d_LU32, d_lrows_f, d_lrows_b, d_upd_ptr, d_upd, d_ilu_tmp, d_Jb, d_ierr};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h_scal) cudaFreeHost(h_scal);

@@ -73,27 +73,28 @@ struct fos_ctx {
   int* d_flag = nullptr;      // non-finite flag
   double* h_scal = nullptr;   // pinned [256]
 
-  // ---- Jacobian (block CSR, internal order) and ILU(0)
+  // ---- Jacobian (block CSR in ILU position order) and ILU(0)
   long nnzb = 0;
-  std::vector<int> h_rowptr, h_col;
-  int* d_rowptr = nullptr;    // [nC+1]
-  int* d_col = nullptr;       // [nnzb]
-  int* d_diag = nullptr;      // [nC] slot of the diagonal block
+  std::vector<int> h_prow, h_pcol;
+  int* d_prow = nullptr;      // [nC+1] block rows by position
+  int* d_pcol = nullptr;      // [nnzb] column positions, ascending per row
+  int* d_pdiag = nullptr;     // [nC] slot of the diagonal block, by position
+  int* d_cdiag = nullptr;     // [nC] slot of the diagonal block, by internal cell
+  int* d_ipos = nullptr;      // [nC] internal cell -> position
+  int* d_ord = nullptr;       // [nC] position -> internal cell
   int* d_fslot = nullptr;     // [2*nFi] slots of blocks (L,R) and (R,L) per interior face
-  double* d_J = nullptr;      // [25*nnzb] unscaled Jacobian blocks
-  double* d_Jb = nullptr;     // [25*nFb] boundary-face diagonal terms
+  void* d_Jraw = nullptr;     // [25*nnzb] unscaled Jacobian blocks (FP64, FP32 for FOS_ILU_FP32)
+  void* d_Jb = nullptr;       // [25*nFb] boundary-face diagonal terms (same type)
   int* d_ierr = nullptr;
   bool has_jac = false;
   double* d_LU = nullptr;     // [25*nnzb] factors (FP64), diag blocks hold the inverse
-  float* d_LU32 = nullptr;    // [25*nnzb] FP32 copy for the FP32 apply
-  // ILU ordering (may differ from the residual ordering)
+  float* d_LU32 = nullptr;    // [25*nnzb] factors (FP32)
   int ilu_nlev_f = 0, ilu_nlev_b = 0;
-  std::vector<int> lev_f, lev_b;    // host level pointers into the level-ordered rows
-  int* d_lrows_f = nullptr;         // rows in forward level order
-  int* d_lrows_b = nullptr;         // rows in backward level order
-  // factor update lists: for row i, k in lower(i): triples (slot_ik, slot_kj, slot_ij)
-  int* d_upd_ptr = nullptr;   // [nC+1] per row
-  int3* d_upd = nullptr;      // updates
+  std::vector<int> lev_f, lev_b;    // level pointers (colour starts when colouring)
+  int* d_lrows_f = nullptr;         // level-ordered positions (null when levels are ranges)
+  int* d_lrows_b = nullptr;
+  int* d_upd_ptr = nullptr;   // [nC+1] per position
+  int3* d_upd = nullptr;      // (slot_pq, slot_qj or diag(q), slot_pj or -1)
   int ilu_ierr = 0;
   int ilu_colors = 0;            // > 0: ILU order is colour-major (FOS_ILU_COLOR)
   bool has_factor = false;

@@ -16,10 +16,14 @@
 // Preconditioner: P = I - gamma diag(1/v) J, factored by block ILU(0) (the block
 // form of SPARSKIT ilu0, ITSOL/ilut.f:1793-1917: equal to scalar ILU(0) of the
 // interleaved matrix), with the inverse of each diagonal block stored in its slot
-// like ilu0 stores the inverted diagonal.  Rows are processed level by level:
-// the level of a row is one more than the highest level among its lower-triangle
-// neighbours (forward) / upper-triangle neighbours (backward), cf. SPARSKIT
-// levels (FORMATS/unary.f:1078).  Apply = lusol (ilut.f:2272-2320) in block form.
+// like ilu0 stores the inverted diagonal.  The ILU works in "position" space: block row
+// p is the p-th row of the elimination order (internal order, or colour-major for
+// FOS_ILU_COLOR); each row's blocks are contiguous and sorted by position, so lower(p) =
+// [prow[p], pdiag[p]) and upper(p) = (pdiag[p], prow[p+1]).  Rows are processed level by
+// level: colours (contiguous ranges of p) for FOS_ILU_COLOR, otherwise the level sets of
+// the lower / upper triangles (one more than the highest level among the row's lower /
+// upper neighbours, cf. SPARSKIT levels, FORMATS/unary.f:1078).  Apply = lusol
+// (ilut.f:2272-2320) in block form, on AoS copies of the vectors in position order.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -97,7 +101,7 @@ __device__ __forceinline__ void anfj(const T n[3], const T u[3], T H, T c, T g, 
   }
 }
 
-template <typename T>
+template <typename T, typename TJ>
 __global__ void __launch_bounds__(kT) k_jac_face(int nFi, int nF, int nC,
                                                  const int2* __restrict__ faceLR,
                                                  const double2* __restrict__ faceNA,
@@ -106,8 +110,8 @@ __global__ void __launch_bounds__(kT) k_jac_face(int nFi, int nF, int nC,
                                                  const int* __restrict__ fslot,
                                                  const int* __restrict__ bcT,
                                                  const double* __restrict__ bcP, int maxP,
-                                                 double g, double r, double* __restrict__ J,
-                                                 double* __restrict__ Jb) {
+                                                 double g, double r, TJ* __restrict__ J,
+                                                 TJ* __restrict__ Jb) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nF) return;
   const int2 lr = faceLR[f];
@@ -148,46 +152,47 @@ __global__ void __launch_bounds__(kT) k_jac_face(int nFi, int nF, int nC,
   const T vnR = uR[0] * n[0] + uR[1] * n[1] + uR[2] * n[2];
   const T h = T(0.5) * aP;
   if (f < nFi) {
-    double* oLR = J + 25 * (size_t)fslot[2 * f];      // block (L, R) = JacP(1:5,6:10)
-    double* oRL = J + 25 * (size_t)fslot[2 * f + 1];  // block (R, L) = JacP(6:10,1:5)
+    TJ* oLR = J + 25 * (size_t)fslot[2 * f];      // block (L, R) = JacP(1:5,6:10)
+    TJ* oRL = J + 25 * (size_t)fslot[2 * f + 1];  // block (R, L) = JacP(6:10,1:5)
     for (int a = 0; a < 5; a++)
       for (int b = 0; b < 5; b++) {
-        oLR[5 * a + b] = (double)(-h * (nfj<T>(a, b, n, uR, HR, gg, v2R, vnR) - Ab[5 * a + b]));
-        oRL[5 * a + b] = (double)(h * (nfj<T>(a, b, n, uL, HL, gg, v2L, vnL) + Ab[5 * a + b]));
+        oLR[5 * a + b] = (TJ)(-h * (nfj<T>(a, b, n, uR, HR, gg, v2R, vnR) - Ab[5 * a + b]));
+        oRL[5 * a + b] = (TJ)(h * (nfj<T>(a, b, n, uL, HL, gg, v2L, vnL) + Ab[5 * a + b]));
       }
   } else {
-    double* d = Jb + 25 * (size_t)(f - nFi);  // boundary pair's diagonal term
+    TJ* d = Jb + 25 * (size_t)(f - nFi);  // boundary pair's diagonal term
     for (int a = 0; a < 5; a++)
       for (int b = 0; b < 5; b++)
-        d[5 * a + b] = (double)(-h * (nfj<T>(a, b, n, uL, HL, gg, v2L, vnL) + Ab[5 * a + b]));
+        d[5 * a + b] = (TJ)(-h * (nfj<T>(a, b, n, uL, HL, gg, v2L, vnL) + Ab[5 * a + b]));
   }
 }
 
+template <typename TJ>
 __global__ void __launch_bounds__(kT) k_jac_diag(int nC, int nFi, const int* __restrict__ crow,
                                                  const int* __restrict__ cent,
                                                  const int* __restrict__ fslot,
-                                                 const int* __restrict__ diag,
-                                                 const double* __restrict__ Jb,
-                                                 double* __restrict__ J) {
+                                                 const int* __restrict__ cdiag,
+                                                 const TJ* __restrict__ Jb,
+                                                 TJ* __restrict__ J) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nC) return;
-  double D[25];
+  TJ D[25];
 #pragma unroll
-  for (int k = 0; k < 25; k++) D[k] = 0.0;
+  for (int k = 0; k < 25; k++) D[k] = TJ(0);
   for (int e = crow[c]; e < crow[c + 1]; e++) {
     const int ent = cent[e], f = ent >> 1;
     if (f < nFi) {
       // cell is L: diag += JacP(1:5,1:5) = -block(R,L); cell is R: diag += -block(L,R)
-      const double* o = J + 25 * (size_t)fslot[2 * f + ((ent & 1) ? 0 : 1)];
+      const TJ* o = J + 25 * (size_t)fslot[2 * f + ((ent & 1) ? 0 : 1)];
 #pragma unroll
       for (int k = 0; k < 25; k++) D[k] -= o[k];
     } else {
-      const double* o = Jb + 25 * (size_t)(f - nFi);
+      const TJ* o = Jb + 25 * (size_t)(f - nFi);
 #pragma unroll
       for (int k = 0; k < 25; k++) D[k] += o[k];
     }
   }
-  double* dst = J + 25 * (size_t)diag[c];
+  TJ* dst = J + 25 * (size_t)cdiag[c];
 #pragma unroll
   for (int k = 0; k < 25; k++) dst[k] = D[k];
 }
@@ -216,53 +221,64 @@ __device__ __forceinline__ bool inv5(T a[25]) {
   return ok;
 }
 
-// One level of the block ILU(0) factorisation, five lanes per block row i (lane a owns
-// row a of every block of row i; six rows per warp):
-//   LU_i* = P_i* = delta - gamma/v_i J_i*          (copy of the row, fused)
-//   for k in lower(i) (ILU order): LU_ik = LU_ik inv(D_k); LU_ij -= LU_ik LU_kj (j in row i)
-//   D_i = LU_ii -> inverted by Gauss--Jordan across the five lanes (shuffles)
-// A lane only reads its own row of row i's blocks and whole blocks of finished rows, so
-// the lanes of a row need no synchronisation until the diagonal inversion.
-template <typename TF>
-__global__ void __launch_bounds__(kT) k_ilu_factor5(
-    int n, const int* __restrict__ rows, const int* __restrict__ rowptr,
-    const int* __restrict__ diag, const double* __restrict__ invV, double gamma,
-    const double* __restrict__ J, const int* __restrict__ upd_ptr, const int3* __restrict__ upd,
-    TF* __restrict__ LU, int* __restrict__ ierr) {
+// One level of the block ILU(0) factorisation.  Five lanes per block row p (lane a owns
+// row a of every block of row p), six rows per warp, 24 rows per CTA; the row's blocks
+// live in shared memory while they are being eliminated:
+//   P_p* = delta - gamma/v J_p*                         (copy of the row, fused)
+//   for k in lower(p): L_pk = P_pk inv(D_k); P_pj -= L_pk U_kj for j in upper(k) in row p
+//   D_p = P_pp -> inverted by Gauss--Jordan without pivoting across the five lanes
+// A lane only touches its own row of row p's blocks and reads finished blocks of earlier
+// rows from global memory, so the lanes of a row need no synchronisation until the
+// diagonal inversion (warp shuffles).
+constexpr int kRowsPerCta = 6 * (kT / 32);
+constexpr int kMaxBlocksPerRow = 7;  // diagonal + up to 6 neighbours (hexahedra)
+
+template <typename TF, typename TJ>
+__global__ void __launch_bounds__(kT) k_ilu_factor(
+    int n, const int* __restrict__ rows, int p0, const int* __restrict__ prow,
+    const int* __restrict__ pdiag, const int* __restrict__ ord, const double* __restrict__ invV,
+    double gamma, const TJ* __restrict__ J, const int* __restrict__ upd_ptr,
+    const int3* __restrict__ upd, TF* __restrict__ LU, int* __restrict__ ierr) {
+  __shared__ TF sm[kRowsPerCta][kMaxBlocksPerRow][25];
   const int lane = threadIdx.x & 31;
   const int sub = lane / 5, a = lane - 5 * sub;
+  const int lrow = (threadIdx.x >> 5) * 6 + (sub < 6 ? sub : 0);
   const int t = (blockIdx.x * blockDim.x + threadIdx.x) / 32 * 6 + sub;
   const bool active = sub < 6 && t < n;
-  const int i = active ? rows[t] : 0;
+  const int p = active ? (rows ? rows[t] : p0 + t) : 0;
   TF D[5] = {TF(0), TF(0), TF(0), TF(0), TF(0)};
+  int s0 = 0, sd = 0;
   if (active) {
-    const double s = gamma * invV[i];
-    for (int sl = rowptr[i]; sl < rowptr[i + 1]; sl++) {
-      const double* src = J + 25 * (size_t)sl + 5 * a;
-      TF* dst = LU + 25 * (size_t)sl + 5 * a;
-      const bool dg = sl == diag[i];
+    s0 = prow[p];
+    sd = pdiag[p];
+    const int nb = prow[p + 1] - s0;
+    const double s = gamma * invV[ord[p]];
+    for (int b = 0; b < nb; b++) {
+      const TJ* src = J + 25 * (size_t)(s0 + b) + 5 * a;
+      const bool dg = (s0 + b) == sd;
 #pragma unroll
-      for (int b = 0; b < 5; b++) dst[b] = (TF)(((dg && b == a) ? 1.0 : 0.0) - s * src[b]);
+      for (int k = 0; k < 5; k++)
+        sm[lrow][b][5 * a + k] = (TF)(((dg && k == a) ? 1.0 : 0.0) - s * (double)src[k]);
     }
-    for (int o = upd_ptr[i]; o < upd_ptr[i + 1]; o++) {
+    for (int o = upd_ptr[p]; o < upd_ptr[p + 1]; o++) {
       const int3 op = upd[o];
       TF A[5];
+      TF* Ar = &sm[lrow][op.x - s0][5 * a];
 #pragma unroll
-      for (int k = 0; k < 5; k++) A[k] = LU[25 * (size_t)op.x + 5 * a + k];
+      for (int k = 0; k < 5; k++) A[k] = Ar[k];
       const TF* B = LU + 25 * (size_t)op.y;
-      TF* dst = LU + 25 * (size_t)(op.z < 0 ? op.x : op.z) + 5 * a;
+      TF* dst = &sm[lrow][(op.z < 0 ? op.x : op.z) - s0][5 * a];
 #pragma unroll
       for (int b = 0; b < 5; b++) {
-        TF p = 0;
+        TF acc = 0;
 #pragma unroll
-        for (int k = 0; k < 5; k++) p += A[k] * B[5 * k + b];
-        dst[b] = op.z < 0 ? p : dst[b] - p;
+        for (int k = 0; k < 5; k++) acc += A[k] * B[5 * k + b];
+        dst[b] = op.z < 0 ? acc : dst[b] - acc;
       }
     }
 #pragma unroll
-    for (int b = 0; b < 5; b++) D[b] = LU[25 * (size_t)diag[i] + 5 * a + b];
+    for (int b = 0; b < 5; b++) D[b] = sm[lrow][sd - s0][5 * a + b];
   }
-  // Gauss--Jordan without pivoting: step k broadcasts row k (lane base + k)
   const int base = lane - a;
   bool ok = true;
 #pragma unroll
@@ -283,16 +299,17 @@ __global__ void __launch_bounds__(kT) k_ilu_factor5(
     }
   }
   if (!active) return;
-  if (!ok) atomicMin(ierr, i + 1);
+  if (!ok) atomicMin(ierr, p + 1);
 #pragma unroll
-  for (int b = 0; b < 5; b++) LU[25 * (size_t)diag[i] + 5 * a + b] = D[b];
+  for (int b = 0; b < 5; b++) sm[lrow][sd - s0][5 * a + b] = D[b];
+  const int nb = prow[p + 1] - s0;
+  for (int b = 0; b < nb; b++) {
+    TF* dst = LU + 25 * (size_t)(s0 + b) + 5 * a;
+#pragma unroll
+    for (int k = 0; k < 5; k++) dst[k] = sm[lrow][b][5 * a + k];
+  }
 }
 
-// Triangular sweeps, five lanes per block row (lane a owns component a and reads row a
-// of every 5x5 block).  Intermediate vectors are AoS in TF (8 per row, 32 / 64 B), so the
-// neighbour values of a row are one sector; r (in) and z (out) are the FP64 SoA vectors.
-//   forward:  y_i = r_i - sum_{k in lower(i)} L_ik y_k           (unit block diagonal)
-//   backward: z_i = inv(D_i) (y_i - sum_{j in upper(i)} U_ij z_j)
 template <typename TF>
 __device__ __forceinline__ TF from64(double x) {
   if constexpr (sizeof(TF) == 4) return d2f_trunc(x); else return (TF)x;
@@ -302,50 +319,73 @@ __device__ __forceinline__ double to64(TF x) {
   if constexpr (sizeof(TF) == 4) return f2d_bits(x); else return (double)x;
 }
 
+// r (FP64 SoA, internal order) -> rv (AoS, 8 per row, position order)
 template <typename TF>
-__global__ void __launch_bounds__(kT) k_ilu_fwd5(int n, int nC, const int* __restrict__ rows,
-                                                 const int* __restrict__ rowptr,
-                                                 const int* __restrict__ col,
-                                                 const int* __restrict__ diag,
-                                                 const TF* __restrict__ LU,
-                                                 const double* __restrict__ r,
-                                                 TF* __restrict__ yv) {
+__global__ void k_ilu_in(int nC, const int* __restrict__ ipos, const double* __restrict__ r,
+                         TF* __restrict__ rv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nC) return;
+  TF* dst = rv + 8 * (size_t)ipos[i];
+#pragma unroll
+  for (int a = 0; a < 5; a++) dst[a] = from64<TF>(r[(size_t)a * nC + i]);
+}
+// zv (AoS, position order) -> z (FP64 SoA, internal order)
+template <typename TF>
+__global__ void k_ilu_out(int nC, const int* __restrict__ ipos, const TF* __restrict__ zv,
+                          double* __restrict__ z) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nC) return;
+  const TF* src = zv + 8 * (size_t)ipos[i];
+#pragma unroll
+  for (int a = 0; a < 5; a++) z[(size_t)a * nC + i] = to64<TF>(src[a]);
+}
+
+// Triangular sweeps in position space, five lanes per block row (lane a owns component
+// a and reads row a of every 5x5 block).  The forward sweep overwrites rv with y in place
+// (a row reads only its own rv and earlier rows' y).
+//   forward:  y_p = r_p - sum_{q in lower(p)} L_pq y_q           (unit block diagonal)
+//   backward: z_p = inv(D_p) (y_p - sum_{q in upper(p)} U_pq z_q)
+template <typename TF>
+__global__ void __launch_bounds__(kT) k_ilu_fwd(int n, const int* __restrict__ rows, int p0,
+                                                const int* __restrict__ prow,
+                                                const int* __restrict__ pcol,
+                                                const int* __restrict__ pdiag,
+                                                const TF* __restrict__ LU, TF* __restrict__ yv) {
   const int lane = threadIdx.x & 31;
   const int sub = lane / 5, a = lane - 5 * sub;
   const int t = (blockIdx.x * blockDim.x + threadIdx.x) / 32 * 6 + sub;
   if (sub >= 6 || t >= n) return;
-  const int i = rows[t];
-  TF acc = from64<TF>(r[(size_t)a * nC + i]);
-  for (int s = rowptr[i]; s < diag[i]; s++) {
-    const TF* yk = yv + 8 * (size_t)col[s];
+  const int p = rows ? rows[t] : p0 + t;
+  TF acc = yv[8 * (size_t)p + a];
+  for (int s = prow[p]; s < pdiag[p]; s++) {
+    const TF* yq = yv + 8 * (size_t)pcol[s];
     const TF* B = LU + 25 * (size_t)s + 5 * a;
 #pragma unroll
-    for (int b = 0; b < 5; b++) acc -= __ldg(B + b) * yk[b];
+    for (int b = 0; b < 5; b++) acc -= __ldg(B + b) * yq[b];
   }
-  yv[8 * (size_t)i + a] = acc;
+  yv[8 * (size_t)p + a] = acc;
 }
 
 template <typename TF>
-__global__ void __launch_bounds__(kT) k_ilu_bwd5(int n, int nC, const int* __restrict__ rows,
-                                                 const int* __restrict__ rowptr,
-                                                 const int* __restrict__ col,
-                                                 const int* __restrict__ diag,
-                                                 const TF* __restrict__ LU,
-                                                 const TF* __restrict__ yv,
-                                                 TF* __restrict__ zv, double* __restrict__ z) {
+__global__ void __launch_bounds__(kT) k_ilu_bwd(int n, const int* __restrict__ rows, int p0,
+                                                const int* __restrict__ prow,
+                                                const int* __restrict__ pcol,
+                                                const int* __restrict__ pdiag,
+                                                const TF* __restrict__ LU,
+                                                const TF* __restrict__ yv, TF* __restrict__ zv) {
   const int lane = threadIdx.x & 31;
   const int sub = lane / 5, a = lane - 5 * sub;
   const int t = (blockIdx.x * blockDim.x + threadIdx.x) / 32 * 6 + sub;
   const bool active = sub < 6 && t < n;
-  const int i = active ? rows[t] : 0;
+  const int p = active ? (rows ? rows[t] : p0 + t) : 0;
   TF acc = TF(0);
   if (active) {
-    acc = yv[8 * (size_t)i + a];
-    for (int s = diag[i] + 1; s < rowptr[i + 1]; s++) {
-      const TF* zj = zv + 8 * (size_t)col[s];
+    acc = yv[8 * (size_t)p + a];
+    for (int s = pdiag[p] + 1; s < prow[p + 1]; s++) {
+      const TF* zq = zv + 8 * (size_t)pcol[s];
       const TF* B = LU + 25 * (size_t)s + 5 * a;
 #pragma unroll
-      for (int b = 0; b < 5; b++) acc -= __ldg(B + b) * zj[b];
+      for (int b = 0; b < 5; b++) acc -= __ldg(B + b) * zq[b];
     }
   }
   TF comp[5];
@@ -353,12 +393,11 @@ __global__ void __launch_bounds__(kT) k_ilu_bwd5(int n, int nC, const int* __res
 #pragma unroll
   for (int b = 0; b < 5; b++) comp[b] = __shfl_sync(0xffffffffu, acc, base + b < 32 ? base + b : 0);
   if (!active) return;
-  const TF* Dr = LU + 25 * (size_t)diag[i] + 5 * a;
+  const TF* Dr = LU + 25 * (size_t)pdiag[p] + 5 * a;
   TF zz = 0;
 #pragma unroll
   for (int b = 0; b < 5; b++) zz += __ldg(Dr + b) * comp[b];
-  zv[8 * (size_t)i + a] = zz;
-  z[(size_t)a * nC + i] = to64<TF>(zz);
+  zv[8 * (size_t)p + a] = zz;
 }
 
 }  // namespace
@@ -374,12 +413,9 @@ int up(T** dst, const std::vector<T>& v) {
 }
 }  // namespace
 
-// Block sparsity, ILU order, level sets and factor update lists (once per context).
-// Each block row holds its columns sorted by ILU position, so lower(i) = [rowptr, diag)
-// and upper(i) = (diag, rowptr+1) in the ILU order (identity = the internal RCM order;
-// FOS_ILU_COLOR = greedy colouring of the cell graph, colour-major).
+// Block sparsity in position space, ILU order, level sets and factor update lists (once).
 int fos_jac_setup(fos_ctx* c) {
-  if (c->d_rowptr) return 0;
+  if (c->d_prow) return 0;
   const int nC = c->nC, nFi = c->nFi;
   std::vector<int> deg(nC + 1, 0);
   for (int f = 0; f < nFi; f++) {
@@ -395,8 +431,14 @@ int fos_jac_setup(fos_ctx* c) {
       adj[pos[c->h_faceR[f]]++] = c->h_faceL[f];
     }
   }
+  for (int i = 0; i < nC; i++)
+    if (deg[i + 1] - deg[i] + 1 > kMaxBlocksPerRow) {
+      fos_set_error("fos_jac_setup: a cell has more than 6 neighbours");
+      return -2;
+    }
   // ILU position of every internal row
-  std::vector<int> ipos(nC);
+  std::vector<int> ipos(nC), ord(nC);
+  std::vector<int> cstart;
   c->ilu_colors = 0;
   if (c->flags & FOS_ILU_COLOR) {
     std::vector<int> color(nC, -1);
@@ -410,147 +452,168 @@ int fos_jac_setup(fos_ctx* c) {
       color[i] = k;
       ncol = std::max(ncol, k + 1);
     }
-    std::vector<int> cnt(ncol + 1, 0);
-    for (int i = 0; i < nC; i++) cnt[color[i] + 1]++;
-    for (int k = 0; k < ncol; k++) cnt[k + 1] += cnt[k];
-    for (int i = 0; i < nC; i++) ipos[i] = cnt[color[i]]++;
+    cstart.assign(ncol + 1, 0);
+    for (int i = 0; i < nC; i++) cstart[color[i] + 1]++;
+    for (int k = 0; k < ncol; k++) cstart[k + 1] += cstart[k];
+    std::vector<int> fill(cstart.begin(), cstart.end() - 1);
+    for (int i = 0; i < nC; i++) ipos[i] = fill[color[i]]++;
     c->ilu_colors = ncol;
   } else {
     for (int i = 0; i < nC; i++) ipos[i] = i;
   }
+  for (int i = 0; i < nC; i++) ord[ipos[i]] = i;
   c->h_ilu_pos = ipos;
-  std::vector<int> rowptr(nC + 1, 0), col, diag(nC);
-  col.reserve((size_t)nC + 2 * (size_t)nFi);
+  // block rows in position order, blocks sorted by position
+  std::vector<int> prow(nC + 1, 0), pcol, pdiag(nC), cdiag(nC);
+  pcol.reserve((size_t)nC + 2 * (size_t)nFi);
   std::vector<int> tmp;
-  for (int i = 0; i < nC; i++) {
-    tmp.assign(adj.begin() + deg[i], adj.begin() + deg[i + 1]);
-    tmp.push_back(i);
+  for (int p = 0; p < nC; p++) {
+    const int i = ord[p];
+    tmp.clear();
+    for (int e = deg[i]; e < deg[i + 1]; e++) tmp.push_back(ipos[adj[e]]);
+    tmp.push_back(p);
     std::sort(tmp.begin(), tmp.end());
     tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
-    std::sort(tmp.begin(), tmp.end(), [&](int a, int b) { return ipos[a] < ipos[b]; });
-    for (int j : tmp) {
-      if (j == i) diag[i] = (int)col.size();
-      col.push_back(j);
+    for (int q : tmp) {
+      if (q == p) pdiag[p] = (int)pcol.size();
+      pcol.push_back(q);
     }
-    rowptr[i + 1] = (int)col.size();
+    prow[p + 1] = (int)pcol.size();
   }
-  c->nnzb = (long)col.size();
-  auto slot_of = [&](int i, int j) -> int {
-    for (int s = rowptr[i]; s < rowptr[i + 1]; s++)
-      if (col[s] == j) return s;
+  for (int i = 0; i < nC; i++) cdiag[i] = pdiag[ipos[i]];
+  c->nnzb = (long)pcol.size();
+  auto slot_of = [&](int p, int q) -> int {
+    for (int s = prow[p]; s < prow[p + 1]; s++)
+      if (pcol[s] == q) return s;
     return -1;
   };
   std::vector<int> fslot(2 * (size_t)nFi);
   for (int f = 0; f < nFi; f++) {
-    fslot[2 * f] = slot_of(c->h_faceL[f], c->h_faceR[f]);
-    fslot[2 * f + 1] = slot_of(c->h_faceR[f], c->h_faceL[f]);
+    const int pL = ipos[c->h_faceL[f]], pR = ipos[c->h_faceR[f]];
+    fslot[2 * f] = slot_of(pL, pR);
+    fslot[2 * f + 1] = slot_of(pR, pL);
   }
-  // level sets in the ILU order
-  std::vector<int> order(nC);
-  for (int i = 0; i < nC; i++) order[ipos[i]] = i;
-  std::vector<int> lf(nC, 0), lb(nC, 0);
-  int nlf = 0, nlb = 0;
-  for (int q = 0; q < nC; q++) {
-    const int i = order[q];
-    int l = 0;
-    for (int s = rowptr[i]; s < diag[i]; s++) l = std::max(l, lf[col[s]] + 1);
-    lf[i] = l;
-    nlf = std::max(nlf, l + 1);
-  }
-  for (int q = nC - 1; q >= 0; q--) {
-    const int i = order[q];
-    int l = 0;
-    for (int s = diag[i] + 1; s < rowptr[i + 1]; s++) l = std::max(l, lb[col[s]] + 1);
-    lb[i] = l;
-    nlb = std::max(nlb, l + 1);
-  }
-  auto group = [&](const std::vector<int>& lev, int nl, std::vector<int>& ptr, std::vector<int>& rows) {
-    ptr.assign(nl + 1, 0);
-    for (int i = 0; i < nC; i++) ptr[lev[i] + 1]++;
-    for (int l = 0; l < nl; l++) ptr[l + 1] += ptr[l];
-    rows.assign(nC, 0);
-    std::vector<int> pos(ptr.begin(), ptr.end() - 1);
-    for (int i = 0; i < nC; i++) rows[pos[lev[i]]++] = i;
-  };
+  // schedule: colours (contiguous position ranges) or level sets (lists of positions)
   std::vector<int> rows_f, rows_b;
-  group(lf, nlf, c->lev_f, rows_f);
-  group(lb, nlb, c->lev_b, rows_b);
-  c->ilu_nlev_f = nlf;
-  c->ilu_nlev_b = nlb;
-  // factor update lists (IKJ): for k in lower(i) in ILU order: scale L_ik, then
-  // A_ij -= L_ik U_kj for every j in upper(k) that is also in row i
+  if (c->ilu_colors) {
+    c->lev_f = cstart;
+    c->lev_b = cstart;
+    c->ilu_nlev_f = c->ilu_nlev_b = c->ilu_colors;
+  } else {
+    std::vector<int> lf(nC, 0), lb(nC, 0);
+    int nlf = 0, nlb = 0;
+    for (int p = 0; p < nC; p++) {
+      int l = 0;
+      for (int s = prow[p]; s < pdiag[p]; s++) l = std::max(l, lf[pcol[s]] + 1);
+      lf[p] = l;
+      nlf = std::max(nlf, l + 1);
+    }
+    for (int p = nC - 1; p >= 0; p--) {
+      int l = 0;
+      for (int s = pdiag[p] + 1; s < prow[p + 1]; s++) l = std::max(l, lb[pcol[s]] + 1);
+      lb[p] = l;
+      nlb = std::max(nlb, l + 1);
+    }
+    auto group = [&](const std::vector<int>& lev, int nl, std::vector<int>& ptr,
+                     std::vector<int>& rows) {
+      ptr.assign(nl + 1, 0);
+      for (int p = 0; p < nC; p++) ptr[lev[p] + 1]++;
+      for (int l = 0; l < nl; l++) ptr[l + 1] += ptr[l];
+      rows.assign(nC, 0);
+      std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+      for (int p = 0; p < nC; p++) rows[fill[lev[p]]++] = p;
+    };
+    group(lf, nlf, c->lev_f, rows_f);
+    group(lb, nlb, c->lev_b, rows_b);
+    c->ilu_nlev_f = nlf;
+    c->ilu_nlev_b = nlb;
+  }
+  // factor update lists (IKJ): for q in lower(p) by position: scale L_pq, then
+  // P_pj -= L_pq U_qj for every j in upper(q) that is also in row p
   std::vector<int> upd_ptr(nC + 1, 0);
   std::vector<int3> upd;
   upd.reserve((size_t)nC * 8);
-  for (int i = 0; i < nC; i++) {
-    for (int s = rowptr[i]; s < diag[i]; s++) {
-      const int k = col[s];
-      upd.push_back(make_int3(s, diag[k], -1));
-      for (int t = diag[k] + 1; t < rowptr[k + 1]; t++) {
-        const int sij = slot_of(i, col[t]);
+  for (int p = 0; p < nC; p++) {
+    for (int s = prow[p]; s < pdiag[p]; s++) {
+      const int q = pcol[s];
+      upd.push_back(make_int3(s, pdiag[q], -1));
+      for (int t = pdiag[q] + 1; t < prow[q + 1]; t++) {
+        const int sij = slot_of(p, pcol[t]);
         if (sij >= 0) upd.push_back(make_int3(s, t, sij));
       }
     }
-    upd_ptr[i + 1] = (int)upd.size();
+    upd_ptr[p + 1] = (int)upd.size();
   }
-  c->h_rowptr = rowptr;
-  c->h_col = col;
-  if (up(&c->d_rowptr, rowptr) || up(&c->d_col, col) || up(&c->d_diag, diag) ||
-      up(&c->d_fslot, fslot) || up(&c->d_lrows_f, rows_f) || up(&c->d_lrows_b, rows_b) ||
-      up(&c->d_upd_ptr, upd_ptr) || up(&c->d_upd, upd))
+  c->h_prow = prow;
+  c->h_pcol = pcol;
+  if (up(&c->d_prow, prow) || up(&c->d_pcol, pcol) || up(&c->d_pdiag, pdiag) ||
+      up(&c->d_cdiag, cdiag) || up(&c->d_ipos, ipos) || up(&c->d_ord, ord) ||
+      up(&c->d_fslot, fslot) || up(&c->d_upd_ptr, upd_ptr) || up(&c->d_upd, upd))
     return -100;
-  FOS_CUDA(cudaMalloc((void**)&c->d_J, 25 * sizeof(double) * (size_t)c->nnzb));
-  FOS_CUDA(cudaMalloc((void**)&c->d_Jb, 25 * sizeof(double) * (size_t)std::max(c->nFb, 1)));
+  if (!rows_f.empty() && (up(&c->d_lrows_f, rows_f) || up(&c->d_lrows_b, rows_b))) return -100;
+  const bool f32 = (c->flags & FOS_ILU_FP32) != 0;
+  const size_t jb = f32 ? sizeof(float) : sizeof(double);
+  FOS_CUDA(cudaMalloc((void**)&c->d_Jraw, 25 * jb * (size_t)c->nnzb));
+  FOS_CUDA(cudaMalloc((void**)&c->d_Jb, 25 * jb * (size_t)std::max(c->nFb, 1)));
   FOS_CUDA(cudaMalloc((void**)&c->d_ilu_tmp, 16 * sizeof(double) * (size_t)nC));  // 2 AoS vectors
   FOS_CUDA(cudaMalloc((void**)&c->d_ierr, sizeof(int)));
-  if (c->flags & FOS_ILU_FP32)
+  if (f32)
     FOS_CUDA(cudaMalloc((void**)&c->d_LU32, 25 * sizeof(float) * (size_t)c->nnzb));
   else
     FOS_CUDA(cudaMalloc((void**)&c->d_LU, 25 * sizeof(double) * (size_t)c->nnzb));
   return 0;
 }
 
+template <typename T, typename TJ>
+static int jac_assemble_t(fos_ctx* c, const double* y) {
+  TJ* J = reinterpret_cast<TJ*>(c->d_Jraw);
+  TJ* Jb = reinterpret_cast<TJ*>(c->d_Jb);
+  fos_launch(c, k_jac_face<T, TJ>, nb(c->nF), kT, c->nFi, c->nF, c->nC,
+             (const int2*)c->d_faceLR, (const double2*)c->d_faceNA, (const double*)c->d_W, y,
+             (const int*)c->d_fslot, (const int*)c->d_bcT, (const double*)c->d_bcP, c->maxP,
+             c->gamm, c->r, J, Jb);
+  fos_launch(c, k_jac_diag<TJ>, nb(c->nC), kT, c->nC, c->nFi, (const int*)c->d_crow,
+             (const int*)c->d_cent, (const int*)c->d_fslot, (const int*)c->d_cdiag,
+             (const TJ*)Jb, J);
+  FOS_LAUNCH_CHECK();
+  return 0;
+}
+
 int fos_jac_assemble(fos_ctx* c, const double* y) {
   int rc = fos_prim_launch(c, y);
   if (rc) return rc;
-  if (c->flags & FOS_ILU_FP32)  // the FP32 preconditioner is assembled in FP32
-    fos_launch(c, k_jac_face<float>, nb(c->nF), kT, c->nFi, c->nF, c->nC,
-               (const int2*)c->d_faceLR, (const double2*)c->d_faceNA, (const double*)c->d_W, y,
-               (const int*)c->d_fslot, (const int*)c->d_bcT, (const double*)c->d_bcP, c->maxP,
-               c->gamm, c->r, c->d_J, c->d_Jb);
-  else
-    fos_launch(c, k_jac_face<double>, nb(c->nF), kT, c->nFi, c->nF, c->nC,
-               (const int2*)c->d_faceLR, (const double2*)c->d_faceNA, (const double*)c->d_W, y,
-               (const int*)c->d_fslot, (const int*)c->d_bcT, (const double*)c->d_bcP, c->maxP,
-               c->gamm, c->r, c->d_J, c->d_Jb);
-  fos_launch(c, k_jac_diag, nb(c->nC), kT, c->nC, c->nFi, (const int*)c->d_crow,
-             (const int*)c->d_cent, (const int*)c->d_fslot, (const int*)c->d_diag,
-             (const double*)c->d_Jb, c->d_J);
-  FOS_LAUNCH_CHECK();
+  // the FP32 preconditioner is assembled and stored in FP32
+  rc = (c->flags & FOS_ILU_FP32) ? jac_assemble_t<float, float>(c, y)
+                                 : jac_assemble_t<double, double>(c, y);
+  if (rc) return rc;
   c->has_jac = true;
+  return 0;
+}
+
+template <typename TF, typename TJ>
+static int ilu_factor_t(fos_ctx* c, double gamma, TF* LU) {
+  for (int l = 0; l < c->ilu_nlev_f; l++) {
+    const int n = c->lev_f[l + 1] - c->lev_f[l];
+    const int* rows = c->d_lrows_f ? c->d_lrows_f + c->lev_f[l] : nullptr;
+    fos_launch(c, k_ilu_factor<TF, TJ>, nb_rows5(n), kT, n, rows, c->lev_f[l],
+               (const int*)c->d_prow, (const int*)c->d_pdiag, (const int*)c->d_ord,
+               (const double*)c->d_invV, gamma, (const TJ*)c->d_Jraw, (const int*)c->d_upd_ptr,
+               (const int3*)c->d_upd, LU, c->d_ierr);
+  }
+  FOS_LAUNCH_CHECK();
   return 0;
 }
 
 int fos_ilu_factor(fos_ctx* c, double gamma) {
   const int big = 0x7fffffff;
   FOS_CUDA(cudaMemcpyAsync(c->d_ierr, &big, sizeof(int), cudaMemcpyHostToDevice, c->stream));
-  for (int l = 0; l < c->ilu_nlev_f; l++) {
-    const int n = c->lev_f[l + 1] - c->lev_f[l];
-    const int* rows = c->d_lrows_f + c->lev_f[l];
-    if (c->flags & FOS_ILU_FP32)
-      fos_launch(c, k_ilu_factor5<float>, nb_rows5(n), kT, n, rows, (const int*)c->d_rowptr,
-                 (const int*)c->d_diag, (const double*)c->d_invV, gamma, (const double*)c->d_J,
-                 (const int*)c->d_upd_ptr, (const int3*)c->d_upd, c->d_LU32, c->d_ierr);
-    else
-      fos_launch(c, k_ilu_factor5<double>, nb_rows5(n), kT, n, rows, (const int*)c->d_rowptr,
-                 (const int*)c->d_diag, (const double*)c->d_invV, gamma, (const double*)c->d_J,
-                 (const int*)c->d_upd_ptr, (const int3*)c->d_upd, c->d_LU, c->d_ierr);
-  }
-  FOS_LAUNCH_CHECK();
+  int rc = (c->flags & FOS_ILU_FP32) ? ilu_factor_t<float, float>(c, gamma, c->d_LU32)
+                                     : ilu_factor_t<double, double>(c, gamma, c->d_LU);
+  if (rc) return rc;
   int* h = (int*)c->h_scal;
   FOS_CUDA(cudaMemcpyAsync(h, c->d_ierr, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   FOS_CUDA(cudaStreamSynchronize(c->stream));
-  c->ilu_ierr = (*h == big) ? 0 : *h;  // 1-based internal row of the first zero pivot
+  c->ilu_ierr = (*h == big) ? 0 : *h;  // 1-based position of the first zero pivot
   c->has_factor = true;
   if (c->ilu_ierr) fos_set_error("block ILU(0): zero pivot");
   return 0;
@@ -560,18 +623,23 @@ template <typename TF>
 static int ilu_apply_t(fos_ctx* c, const TF* LU, const double* r, double* z) {
   TF* yv = reinterpret_cast<TF*>(c->d_ilu_tmp);
   TF* zv = yv + 8 * (size_t)c->nC;
+  fos_launch(c, k_ilu_in<TF>, nb(c->nC, 256), 256, c->nC, (const int*)c->d_ipos, r, yv);
   for (int l = 0; l < c->ilu_nlev_f; l++) {
     const int n = c->lev_f[l + 1] - c->lev_f[l];
-    fos_launch(c, k_ilu_fwd5<TF>, nb_rows5(n), kT, n, c->nC,
-               (const int*)(c->d_lrows_f + c->lev_f[l]), (const int*)c->d_rowptr,
-               (const int*)c->d_col, (const int*)c->d_diag, LU, r, yv);
+    const int* rows = c->d_lrows_f ? c->d_lrows_f + c->lev_f[l] : nullptr;
+    fos_launch(c, k_ilu_fwd<TF>, nb_rows5(n), kT, n, rows, c->lev_f[l], (const int*)c->d_prow,
+               (const int*)c->d_pcol, (const int*)c->d_pdiag, LU, yv);
   }
   for (int l = 0; l < c->ilu_nlev_b; l++) {
-    const int n = c->lev_b[l + 1] - c->lev_b[l];
-    fos_launch(c, k_ilu_bwd5<TF>, nb_rows5(n), kT, n, c->nC,
-               (const int*)(c->d_lrows_b + c->lev_b[l]), (const int*)c->d_rowptr,
-               (const int*)c->d_col, (const int*)c->d_diag, LU, (const TF*)yv, zv, z);
+    // colours run backwards for the upper sweep
+    const int lc = c->ilu_colors ? c->ilu_nlev_b - 1 - l : l;
+    const int n = c->lev_b[lc + 1] - c->lev_b[lc];
+    const int* rows = c->d_lrows_b ? c->d_lrows_b + c->lev_b[lc] : nullptr;
+    fos_launch(c, k_ilu_bwd<TF>, nb_rows5(n), kT, n, rows, c->lev_b[lc], (const int*)c->d_prow,
+               (const int*)c->d_pcol, (const int*)c->d_pdiag, LU, (const TF*)yv, zv);
   }
+  fos_launch(c, k_ilu_out<TF>, nb(c->nC, 256), 256, c->nC, (const int*)c->d_ipos,
+             (const TF*)zv, z);
   FOS_LAUNCH_CHECK();
   return 0;
 }
@@ -581,19 +649,31 @@ int fos_ilu_apply(fos_ctx* c, const double* r, double* z) {
   return ilu_apply_t<double>(c, c->d_LU, r, z);
 }
 
+// Block Jacobian in position space: rowptr (nC+1) / col (positions) / 25-value blocks.
 extern "C" long fos_euler_jac_copy(fos_ctx* c, int* rowptr, int* col, double* val) {
   if (!c) return -1;
   if (fos_jac_setup(c)) return -100;
-  if (rowptr) std::memcpy(rowptr, c->h_rowptr.data(), sizeof(int) * (c->nC + 1));
-  if (col) std::memcpy(col, c->h_col.data(), sizeof(int) * c->nnzb);
+  if (rowptr) std::memcpy(rowptr, c->h_prow.data(), sizeof(int) * (c->nC + 1));
+  if (col) std::memcpy(col, c->h_pcol.data(), sizeof(int) * c->nnzb);
   if (val) {
     if (!c->has_jac) {
       fos_set_error("fos_euler_jac_copy: no Jacobian assembled yet");
       return -2;
     }
-    if (cudaStreamSynchronize(c->stream) != cudaSuccess ||
-        cudaMemcpy(val, c->d_J, 25 * sizeof(double) * (size_t)c->nnzb, cudaMemcpyDeviceToHost) !=
-            cudaSuccess) {
+    const size_t n = 25 * (size_t)c->nnzb;
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
+      fos_set_error("fos_euler_jac_copy: stream error");
+      return -100;
+    }
+    if (c->flags & FOS_ILU_FP32) {
+      std::vector<float> tmp(n);
+      if (cudaMemcpy(tmp.data(), c->d_Jraw, n * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess) {
+        fos_set_error("fos_euler_jac_copy: copy failed");
+        return -100;
+      }
+      for (size_t k = 0; k < n; k++) val[k] = tmp[k];
+    } else if (cudaMemcpy(val, c->d_Jraw, n * sizeof(double), cudaMemcpyDeviceToHost) !=
+               cudaSuccess) {
       fos_set_error("fos_euler_jac_copy: copy failed");
       return -100;
     }

@@ -137,9 +137,10 @@ int fos_euler_jv_dev(fos_ctx* ctx, double t, const double* y, const double* fy, 
 int fos_euler_pset_dev(fos_ctx* ctx, double t, const double* y, int jok, int* jcur,
                        double gamma);
 int fos_euler_psol_dev(fos_ctx* ctx, const double* r, double* z);
-/* Block Jacobian J (5x5 blocks, before scaling by -gamma/v): copies out the
- * block-CSR in internal order.  rowptr nC+1, col nnzb, val 25*nnzb (row-major
- * blocks).  Pass NULL to query nnzb through the return value. */
+/* Block Jacobian J (5x5 blocks, before scaling by -gamma/v): copies out the block CSR
+ * whose rows and columns are ILU positions (fos_ctx_ilu_order maps reference cells to
+ * positions).  rowptr nC+1, col nnzb, val 25*nnzb (row-major blocks).  Pass NULL to
+ * query nnzb through the return value. */
 long fos_euler_jac_copy(fos_ctx* ctx, int* rowptr, int* col, double* val);
 
 /* ------------------------------------------------------------------ driver */

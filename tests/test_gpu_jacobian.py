@@ -33,16 +33,16 @@ def test_jacobian_blocks_match_oracle(case):
     rc, jcur = c.gpu.pset(0.0, y, None, 0, 1e-3)
     assert rc == 0 and jcur == 1
     rowptr, col, val = c.gpu.jacobian()
-    o2n = c.gpu.renumbering()
+    pos = c.gpu.ilu_order()  # block rows / columns are ILU positions
     scale = np.abs(ref).max()
     nblk = 0
     for cell in range(c.nC):
-        i = o2n[cell]
-        cols = col[rowptr[i]:rowptr[i + 1]]
+        p = pos[cell]
+        cols = list(col[rowptr[p]:rowptr[p + 1]])
         blocks = [(cell, 0)] + [(k - 1, j + 1) for j, k in enumerate(c.grid.neib[cell]) if 1 <= k <= c.nC]
         assert len(blocks) == len(cols)
         for other, j in blocks:
-            s = rowptr[i] + list(cols).index(o2n[other])
+            s = rowptr[p] + cols.index(pos[other])
             want = ref[cell, 5 * j:5 * j + 5, :].T
             assert np.abs(val[s] - want).max() <= 1e-12 * scale
             nblk += 1
