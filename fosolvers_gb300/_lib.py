@@ -63,9 +63,22 @@ _SIGS = {
     "fos_euler_pset_dev": (C.c_int, [_vp, C.c_double, _vp, C.c_int, _ip, C.c_double]),
     "fos_euler_psol_dev": (C.c_int, [_vp, _vp, _vp]),
     "fos_euler_jac_copy": (C.c_long, [_vp, _ip, _ip, _dp]),
+    "fos_gnn_create": (C.c_int, [C.POINTER(_vp), C.c_uint]),
+    "fos_gnn_destroy": (None, [_vp]),
+    "fos_gnn_num_params": (C.c_int, []),
+    "fos_gnn_get_params": (C.c_int, [_vp, C.POINTER(C.c_float)]),
+    "fos_gnn_set_params": (C.c_int, [_vp, C.POINTER(C.c_float)]),
+    "fos_gnn_apply_dev": (C.c_int, [_vp, _vp, _vp, _vp, C.c_double, _vp]),
+    "fos_gnn_zero_grad": (C.c_int, [_vp]),
+    "fos_gnn_loss_grad_dev": (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_double, _dp]),
+    "fos_gnn_get_grad": (C.c_int, [_vp, C.POINTER(C.c_float)]),
+    "fos_gnn_adam_step": (C.c_int, [_vp, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float]),
+    "fos_ctx_attach_gnn": (C.c_int, [_vp, _vp]),
     "fos_bdf_defaults": (None, [C.POINTER(BdfOpts)]),
     "fos_bdf_run": (C.c_int, [_vp, C.c_double, _vp, C.POINTER(BdfOpts), C.POINTER(BdfStats)]),
     "fos_bdf_run_host": (C.c_int, [_vp, C.c_double, _dp, C.POINTER(BdfOpts), C.POINTER(BdfStats)]),
+    "fos_linear_solve_dev": (C.c_int, [_vp, C.c_double, _vp, _vp, C.c_double, _vp, _vp,
+                                       C.POINTER(BdfOpts), C.POINTER(BdfStats)]),
 }
 
 _lib = None

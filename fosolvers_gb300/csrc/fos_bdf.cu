@@ -172,12 +172,13 @@ struct fos_bdf_work {
   long N = 0;
   int maxl = 0;
   bool has_hist = false;  // yn holds the last accepted state, ym the one before
+  int ilu_ref_its = -1;   // learned mode: iterations of the last ILU(0)-preconditioned solve
   double t_last = 0.0;
   double *V = nullptr, *Z = nullptr, *w = nullptr, *yn = nullptr, *ym = nullptr,
          *hist = nullptr, *f = nullptr, *b = nullptr, *d = nullptr, *part = nullptr,
-         *sc = nullptr, *yh = nullptr;
+         *sc = nullptr, *yh = nullptr, *u = nullptr;
   ~fos_bdf_work() {
-    for (double* p : {V, Z, w, yn, ym, hist, f, b, d, part, sc, yh})
+    for (double* p : {V, Z, w, yn, ym, hist, f, b, d, part, sc, yh, u})
       if (p) cudaFree(p);
   }
 };
@@ -201,7 +202,7 @@ int work_get(fos_ctx* c, int maxl, Work** out) {
   c->bdf = wk;
   FOS_CUDA(cudaMalloc(&wk->V, sizeof(double) * N * (maxl + 1)));
   FOS_CUDA(cudaMalloc(&wk->Z, sizeof(double) * N * maxl));
-  for (double** p : {&wk->w, &wk->yn, &wk->ym, &wk->hist, &wk->f, &wk->b, &wk->d, &wk->yh})
+  for (double** p : {&wk->w, &wk->yn, &wk->ym, &wk->hist, &wk->f, &wk->b, &wk->d, &wk->yh, &wk->u})
     FOS_CUDA(cudaMalloc(p, sizeof(double) * N));
   FOS_CUDA(cudaMalloc(&wk->part, sizeof(double) * kRedBlocks * kMaxVec));
   FOS_CUDA(cudaMalloc(&wk->sc, sizeof(double) * 6 * kMaxVec));
@@ -235,6 +236,14 @@ struct Driver {
   const fos_bdf_opts& o;
   fos_bdf_stats& st;
   double eps;
+  // preconditioner of the current linear solve: 0 none, 1 ILU(0), 2/3 learned network,
+  // 4/5 ILU(0) followed by the learned correction (2 and 4 fall back to ILU(0))
+  int pc = 0;
+  // learned mode: ILU(0) factorisation is made on demand (fallback) once per BDF step
+  bool pset_done = false;
+  double t_step = 0.0, gamma_step = 0.0;
+  const double* y_step = nullptr;
+  int ilu_ref_its = -1;  // Krylov iterations of the last ILU(0)-preconditioned solve
 
   int reduce(int nv, double* out) {  // k_final over wk.part into device out
     fos_launch(c, k_final, nv, 256, nv, kRedBlocks, wk.part, out);
@@ -278,14 +287,29 @@ struct Driver {
     FOS_CUDA(cudaStreamSynchronize(c->stream));
     return 0;
   }
+  double gamma_cur = 0.0;  // gamma of the current linear solve (input of the learned preconditioner)
   int psolve(const double* y, const double* r, double* z) {
     st.n_psol++;
-    if (o.precond == 0) {
+    if (pc == 0) {
       FOS_CUDA(cudaMemcpyAsync(z, r, sizeof(double) * wk.N, cudaMemcpyDeviceToDevice, c->stream));
       return 0;
     }
-    (void)y;
+    if (pc == 2 || pc == 3) return fos_gnn_precond(c, y, r, gamma_cur, z);
+    if (pc >= 4) {  // z = u + N(y; u), u = ILU(0) r
+      if (int rc = fos_ilu_apply(c, r, wk.u)) return rc;
+      return fos_gnn_precond(c, y, wk.u, gamma_cur, z);
+    }
     return fos_ilu_apply(c, r, z);
+  }
+  int ensure_pset() {
+    if (pset_done) return 0;
+    int jcur = 0;
+    const int jok = (o.jac_reuse && c->has_jac) ? 1 : 0;
+    int rc = fos_euler_pset_dev(c, t_step, y_step, jok, &jcur, gamma_step);
+    if (rc) return rc;
+    st.n_pset++;
+    pset_done = true;
+    return c->ilu_ierr ? 3 : 0;
   }
   // w = J_G v at state y with f(y) = fy
   int jv(const double* y, const double* fy, const double* v, double* w, double gamma,
@@ -300,18 +324,32 @@ struct Driver {
   }
 
   long reorth = 0;
-  // GMRES on J_G d = b; d starts at zero
+  // GMRES on J_G d = b; d starts at zero.  With a learned preconditioner (o.precond >= 2)
+  // this is flexible GMRES (Z_j = M_j(V_j) kept); in modes 2 and 4 it falls back to ILU(0)
+  // -- restarting from the current iterate -- when the residual estimate stagnates (> 0.9
+  // of the previous one) or the iteration count reaches that of the last
+  // ILU(0)-preconditioned solve.
   int gmres(const double* y, const double* fy, double gamma, double ynorm, double bnorm, int* its) {
     const long N = wk.N;
     const int m = o.maxl;
+    pc = o.precond;
+    gamma_cur = gamma;
+    const bool with_fallback = pc == 2 || pc == 4;
+    if (with_fallback && ilu_ref_its < 0) pc = 1;  // no ILU reference yet: this solve sets it
+    const bool pure_ilu = pc == 1;
+    if (pc == 1 || pc >= 4) {
+      if (int rc = ensure_pset()) return rc;
+    }
+    int extra_cycles = 0;
     std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), yv(m), hbuf(4 * kMaxVec);
     FOS_CUDA(cudaMemsetAsync(wk.d, 0, sizeof(double) * N, c->stream));
     *its = 0;
     if (bnorm == 0.0) return 0;
     const double* rvec = wk.b;
     double beta = bnorm;
-    for (int cyc = 0; cyc <= o.max_restarts; cyc++) {
+    for (int cyc = 0; cyc <= o.max_restarts + extra_cycles; cyc++) {
       fos_launch(c, k_scale, nb(N), kT, N, rvec, 1.0 / beta, wk.V);
+      bool fallback = false;
       std::fill(g.begin(), g.end(), 0.0);
       g[0] = beta;
       int kend = 0;
@@ -362,6 +400,10 @@ struct Driver {
         g[j] = cs[j] * g[j];
         kend = j + 1;
         if (std::fabs(g[j + 1]) <= o.lin_rtol * bnorm || hn == 0.0) { conv = true; break; }
+        if ((pc == 2 || pc == 4) && (*its >= ilu_ref_its || std::fabs(g[j + 1]) > 0.9 * std::fabs(g[j]))) {
+          fallback = true;
+          break;
+        }
       }
       for (int l = kend - 1; l >= 0; l--) {
         double s = g[l];
@@ -373,7 +415,18 @@ struct Driver {
       fos_launch(c, k_comb, nb(N), kT, N, kend, (const double*)wk.Z, N,
                  (const double*)(wk.sc + 4 * kMaxVec), wk.d);
       FOS_LAUNCH_CHECK();
-      if (conv || cyc == o.max_restarts) return conv ? 0 : 1;
+      if (conv) {
+        if (pure_ilu) ilu_ref_its = *its;
+        return 0;
+      }
+      if (fallback) {  // continue with ILU(0) from the current iterate
+        st.n_fallback++;
+        pc = 1;
+        if (int rc = ensure_pset()) return rc;
+        extra_cycles++;
+      } else if (cyc == o.max_restarts + extra_cycles) {
+        return 1;
+      }
       // restart from the true residual r = b - J_G d
       int rc = jv(y, fy, wk.d, wk.w, gamma, ynorm);
       if (rc) return rc;
@@ -382,7 +435,10 @@ struct Driver {
       if ((rc = fos_norm2_dev(c, wk.w, N, c->d_scal + 8))) return rc;
       if ((rc = fetch(c->d_scal + 8, hbuf.data(), 1))) return rc;
       beta = std::sqrt(hbuf[0]);
-      if (beta <= o.lin_rtol * bnorm) return 0;
+      if (beta <= o.lin_rtol * bnorm) {
+        if (pure_ilu) ilu_ref_its = *its;
+        return 0;
+      }
       rvec = wk.w;
       // V_0 = w / beta (k_scale reads w before the Arnoldi loop overwrites it)
     }
@@ -395,8 +451,9 @@ struct Driver {
 extern "C" int fos_bdf_run(fos_ctx* c, double t0, double* y, const fos_bdf_opts* opts,
                            fos_bdf_stats* stats) {
   if (!c || !y || !opts || opts->maxl < 1 || opts->maxl > kMaxVec - 1 || opts->nsteps < 0 ||
-      (opts->order != 1 && opts->order != 2) || !(opts->dt > 0.0)) {
-    fos_set_error("fos_bdf_run: bad arguments (maxl must be in [1, 31])");
+      (opts->order != 1 && opts->order != 2) || !(opts->dt > 0.0) || opts->precond < 0 ||
+      opts->precond > 5) {
+    fos_set_error("fos_bdf_run: bad arguments (maxl must be in [1, 31], precond in [0, 5])");
     return -1;
   }
   fos_bdf_stats dummy;
@@ -412,6 +469,7 @@ extern "C" int fos_bdf_run(fos_ctx* c, double t0, double* y, const fos_bdf_opts*
                : (c->flags & FOS_FLUX_FP32) ? std::sqrt((double)FLT_EPSILON)
                                             : std::sqrt(DBL_EPSILON);
   Driver dr{c, wk, *opts, st, eps};
+  dr.ilu_ref_its = wk.ilu_ref_its;
   double t = t0;
   double hb[4];
   FOS_CUDA(cudaMemcpyAsync(wk.yn, y, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
@@ -443,13 +501,11 @@ extern "C" int fos_bdf_run(fos_ctx* c, double t0, double* y, const fos_bdf_opts*
       st.last_gnorm = gn / gtol;
       if (gn <= gtol) { conv = true; break; }
       if (k == opts->max_newton) break;
-      if (k == 0 && opts->precond) {
-        int jcur = 0;
-        const int jok = (opts->jac_reuse && c->has_jac) ? 1 : 0;
-        rc = fos_euler_pset_dev(c, tn, y, jok, &jcur, gamma);
-        if (rc) return rc;
-        st.n_pset++;
-        if (c->ilu_ierr) { status = 3; break; }
+      if (k == 0) {
+        dr.pset_done = false;
+        dr.t_step = tn;
+        dr.gamma_step = gamma;
+        dr.y_step = y;
       }
       // ||G|| for the linear tolerance: ||b||^2 via the norm kernel
       if ((rc = fos_norm2_dev(c, wk.b, N, c->d_scal + 16))) return rc;
@@ -460,6 +516,7 @@ extern "C" int fos_bdf_run(fos_ctx* c, double t0, double* y, const fos_bdf_opts*
       st.n_lin_iters += its;
       st.n_newton++;
       if (rc < 0) return rc;
+      if (rc == 3) { status = 3; break; }  // zero pivot in the ILU(0) factorisation
       fos_launch(c, k_axpy, nb(N), kT, N, 1.0, wk.d, y);
       FOS_LAUNCH_CHECK();
     }
@@ -475,6 +532,7 @@ extern "C" int fos_bdf_run(fos_ctx* c, double t0, double* y, const fos_bdf_opts*
     wk.has_hist = true;
   }
   if (status) wk.has_hist = false;
+  wk.ilu_ref_its = dr.ilu_ref_its;
   st.t = t;
   FOS_CUDA(cudaStreamSynchronize(c->stream));
   return status;
@@ -495,6 +553,48 @@ extern "C" int fos_bdf_run_host(fos_ctx* c, double t0, double* y, const fos_bdf_
   if (rc < 0) return rc;
   if (int rc2 = fos_permute(c, wk->yh, c->d_stage, 1)) return rc2;
   FOS_CUDA(cudaMemcpyAsync(y, c->d_stage, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream));
+  FOS_CUDA(cudaStreamSynchronize(c->stream));
+  return rc;
+}
+
+// One linear solve J_G x = b at state y (f(y) = fy) with the driver's (F)GMRES and the
+// preconditioner of opts->precond; the ILU(0) factorisation is made for (y, gamma) when
+// needed.  Used to generate training pairs and to compare preconditioners.
+extern "C" int fos_linear_solve_dev(fos_ctx* c, double t, const double* y, const double* fy,
+                                    double gamma, const double* b, double* x,
+                                    const fos_bdf_opts* opts, fos_bdf_stats* stats) {
+  if (!c || !y || !fy || !b || !x || !opts || opts->maxl < 1 || opts->maxl > kMaxVec - 1 ||
+      opts->precond < 0 || opts->precond > 5) {
+    fos_set_error("fos_linear_solve_dev: bad arguments");
+    return -1;
+  }
+  fos_bdf_stats dummy;
+  fos_bdf_stats& st = stats ? *stats : dummy;
+  std::memset(&st, 0, sizeof(st));
+  Work* wkp = nullptr;
+  if (int rc = work_get(c, opts->maxl, &wkp)) return rc;
+  Work& wk = *wkp;
+  const long N = wk.N;
+  double eps = opts->jv_eps > 0.0 ? opts->jv_eps
+               : (c->flags & FOS_FLUX_FP32) ? std::sqrt((double)FLT_EPSILON)
+                                            : std::sqrt(DBL_EPSILON);
+  Driver dr{c, wk, *opts, st, eps};
+  dr.ilu_ref_its = wk.ilu_ref_its;
+  dr.t_step = t;
+  dr.gamma_step = gamma;
+  dr.y_step = y;
+  FOS_CUDA(cudaMemcpyAsync(wk.b, b, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+  if (int rc = fos_norm2_dev(c, y, N, c->d_scal + 24)) return rc;
+  if (int rc = fos_norm2_dev(c, b, N, c->d_scal + 25)) return rc;
+  double h2[2];
+  FOS_CUDA(cudaMemcpyAsync(h2, c->d_scal + 24, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  FOS_CUDA(cudaStreamSynchronize(c->stream));
+  int its = 0;
+  int rc = dr.gmres(y, fy, gamma, std::sqrt(h2[0]), std::sqrt(h2[1]), &its);
+  st.n_lin_iters = its;
+  wk.ilu_ref_its = dr.ilu_ref_its;
+  if (rc < 0) return rc;
+  FOS_CUDA(cudaMemcpyAsync(x, wk.d, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
   FOS_CUDA(cudaStreamSynchronize(c->stream));
   return rc;
 }

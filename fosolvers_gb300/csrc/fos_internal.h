@@ -33,6 +33,7 @@ constexpr int kRedBlocks = 608;  // 4 x 152 SMs
 constexpr int kRedThreads = 256;
 
 struct fos_bdf_work;
+struct fos_gnn;
 void fos_bdf_work_free(fos_bdf_work* w);
 
 struct fos_ctx {
@@ -102,6 +103,7 @@ struct fos_ctx {
   double* d_ilu_tmp = nullptr;  // two AoS sweep vectors, 8 values per row each
   fos_bdf_work* bdf = nullptr;  // driver workspace, kept between calls
   long n_launch = 0;            // kernels launched through fos_launch
+  fos_gnn* gnn = nullptr;       // learned preconditioner (not owned)
 
   ~fos_ctx();
 };
@@ -122,6 +124,7 @@ int fos_norm2_dev(fos_ctx* c, const double* x, long n, double* d_out_sq);
 int fos_permute(fos_ctx* c, const double* in, double* out, int dir);
 int fos_jv_sigma(fos_ctx* c, double* d_scal, double ynorm, double eps);
 int fos_prim_launch(fos_ctx* c, const double* y);
+int fos_gnn_precond(fos_ctx* c, const double* y, const double* r, double gamma, double* z);
 // fos_jacobian.cu
 int fos_jac_setup(fos_ctx* c);
 int fos_jac_assemble(fos_ctx* c, const double* y);

@@ -224,6 +224,20 @@ class FOEuler:
                    "fos_bdf_run")
         return rc, st.as_dict()
 
+    def attach_gnn(self, gnn):
+        """Learned preconditioner used by bdf_run / linear_solve when opts.precond == 2."""
+        check(_lib.lib().fos_ctx_attach_gnn(self._h, gnn.handle if gnn is not None else None),
+              "attach_gnn")
+        self._gnn = gnn
+
+    def linear_solve(self, y_dev, fy_dev, gamma, b_dev, x_dev, opts: BdfOpts, t: float = 0.0):
+        """One (F)GMRES solve of J_G x = b at state y; returns (rc, stats)."""
+        st = BdfStats()
+        rc = check(_lib.lib().fos_linear_solve_dev(self._h, t, y_dev.data_ptr(), fy_dev.data_ptr(),
+                                                   gamma, b_dev.data_ptr(), x_dev.data_ptr(),
+                                                   C.byref(opts), C.byref(st)), "linear_solve")
+        return rc, st.as_dict()
+
     def bdf_run_host(self, y: np.ndarray, opts: BdfOpts, t0: float = 0.0):
         """Same on a host array in reference order (copied in and out)."""
         st = BdfStats()

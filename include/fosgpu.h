@@ -143,6 +143,33 @@ int fos_euler_psol_dev(fos_ctx* ctx, const double* r, double* z);
  * query nnzb through the return value. */
 long fos_euler_jac_copy(fos_ctx* ctx, int* rowptr, int* col, double* val);
 
+/* ------------------------------------------------------------------ learned preconditioner */
+
+/* A message-passing graph network over the cell-face graph used as a variable
+ * (flexible-GMRES) preconditioner z = M(y; v); no counterpart in the reference.  Three
+ * layers of width 64, BF16 weights, FP32 accumulation on the tensor cores.  Untrained
+ * (fresh) networks are the identity.  Tetrahedral grids only. */
+typedef struct fos_gnn fos_gnn;
+int fos_gnn_create(fos_gnn** out, unsigned seed);
+void fos_gnn_destroy(fos_gnn* g);
+int fos_gnn_num_params(void);
+int fos_gnn_get_params(const fos_gnn* g, float* host); /* FP32 master weights */
+int fos_gnn_set_params(fos_gnn* g, const float* host);
+/* z = M(y, gamma; v) on the context's graph (device vectors, internal order); gamma is the
+ * BDF coefficient of J_G = I - gamma J (the network sees the local CFL number) */
+int fos_gnn_apply_dev(fos_gnn* g, fos_ctx* ctx, const double* y, const double* v, double gamma,
+                      double* z);
+/* training: loss = mean((z/s_v - t/s_v)^2) over cells and components for the target
+ * correction t; adds dloss/dweights to the gradient accumulator */
+int fos_gnn_zero_grad(fos_gnn* g);
+int fos_gnn_loss_grad_dev(fos_gnn* g, fos_ctx* ctx, const double* y, const double* v,
+                          const double* t, double gamma, double* loss);
+int fos_gnn_get_grad(const fos_gnn* g, float* host);
+int fos_gnn_adam_step(fos_gnn* g, float lr, float beta1, float beta2, float eps,
+                      float grad_scale);
+/* network used by fos_bdf_run when opts.precond == 2 (not owned by the context) */
+int fos_ctx_attach_gnn(fos_ctx* ctx, fos_gnn* g);
+
 /* ------------------------------------------------------------------ driver */
 
 typedef struct {
@@ -156,7 +183,12 @@ typedef struct {
   int max_restarts;
   double lin_rtol;    /* Krylov: ||r|| <= lin_rtol ||b|| */
   double jv_eps;      /* finite-difference increment scale (sqrt of machine epsilon) */
-  int precond;        /* 0 = none, 1 = block ILU(0), 2 = learned (GNN) with ILU(0) fallback */
+  int precond;        /* 0 = none, 1 = block ILU(0), 2 = learned network in flexible GMRES,
+                         falling back to ILU(0) when it stagnates or needs more iterations
+                         than the last ILU(0)-preconditioned solve; 3 = learned network
+                         without fallback (evaluation); 4 = ILU(0) followed by the learned
+                         correction, z = u + N(y; u) with u = ILU(0) r, with the fallback
+                         of 2; 5 = the same without fallback */
   int jac_reuse;      /* 0 = assemble J every BDF step (jok = 0), 1 = keep J from the first step */
   int resume;         /* 1 = continue the BDF history of the previous call (y must be its result) */
 } fos_bdf_opts;
@@ -168,6 +200,14 @@ typedef struct {
 } fos_bdf_stats;
 
 void fos_bdf_defaults(fos_bdf_opts* o);
+/* One linear solve J_G x = b at state y (fy = f(y), device vectors, internal order) with
+ * the driver's (F)GMRES(opts->maxl) to opts->lin_rtol and the preconditioner opts->precond
+ * (the ILU(0) factorisation for (y, gamma) is made when needed).  stats->n_lin_iters
+ * receives the Krylov iterations, stats->n_fallback the learned-to-ILU fallbacks.
+ * Returns 0 converged, 1 not converged, 3 zero pivot, < 0 error. */
+int fos_linear_solve_dev(fos_ctx* ctx, double t, const double* y, const double* fy,
+                         double gamma, const double* b, double* x, const fos_bdf_opts* opts,
+                         fos_bdf_stats* stats);
 /* Advance y (device, internal order, 5*nC) by opts->nsteps fixed BDF steps from t0.
  * Returns 0, > 0 if a step failed to converge (1), hit a non-finite residual (2) or a
  * zero pivot (3); < 0 on errors. */
