@@ -36,6 +36,10 @@ sys.path.insert(0, str(ROOT))
 METRIC = "BDF steps/s at 5.3M tets, 1 GB300: FP32+learned FGMRES vs FP64 ILU, tol 1e-8"
 UNIT = "BDF steps/s"
 FULL_CELLS = 96 ** 3 * 6
+# network apply, bytes per cell moved by the layer-by-layer kernels: scales (y, v, 1/V,
+# face geometry: 120), input layer (y, v, 1/V in, h0 out: 216), 3 message-passing layers
+# (h in and out in BF16, ELL row, face pair and geometry: 368 each), output (h3, v, z: 208)
+GNN_BYTES_PER_CELL = 120 + 216 + 3 * 368 + 208
 
 
 def parse():
@@ -48,7 +52,11 @@ def parse():
     ap.add_argument("--scale", type=int, default=None, help="hexes along x (small cases)")
     ap.add_argument("--mode", choices=["fp64", "fp32"], default="fp64",
                     help="fp64: FP64 flux + FP64 ILU(0); fp32: FP32 flux + FP32 ILU(0) apply")
-    ap.add_argument("--precond", choices=["ilu", "none"], default="ilu")
+    ap.add_argument("--precond", choices=["ilu", "none", "learned"], default="ilu",
+                    help="learned: the trained network in FGMRES with ILU(0) fallback")
+    ap.add_argument("--weights", default=None, help="network weights (.npy) for --precond learned")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="skip the FP64 ILU(0) reference arm on the same mesh")
     ap.add_argument("--ilu-order", choices=["rcm", "color"], default="color",
                     help="ILU(0) elimination order: internal RCM order or greedy colouring")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-oracle baseline")
@@ -208,6 +216,53 @@ def workload_desc(name: str) -> str:
 
 
 # ------------------------------------------------------------------ GPU arm
+PRECOND = {"none": 0, "ilu": 1, "learned": 2}
+
+
+def make_ctx(grid, ibc, wl, mode, ilu_order, stream):
+    from fosolvers_gb300.euler import FLUX_FP32, ILU_COLOR, ILU_FP32, FOEuler
+    flags = (FLUX_FP32 | ILU_FP32) if mode == "fp32" else 0
+    if ilu_order == "color":
+        flags |= ILU_COLOR
+    return FOEuler(grid, ibc, wl.bc_type, wl.bc_param, wl.gamm, wl.r, flags=flags, stream=stream)
+
+
+def timed_bdf(ctx, y0, mk, args, dev, stream, pg, clocks=None):
+    """W untimed BDF steps, then K BDF steps from the same initial state timed with CUDA
+    events on the library stream (barrier + synchronize on both sides)."""
+    import torch
+    y = y0.clone()
+    rc, _ = ctx.bdf_run(y, mk(args.warmup))
+    assert rc == 0, f"warm-up failed: {rc}"
+    torch.cuda.synchronize(dev)
+    y = y0.clone()
+    if pg is not None:
+        pg.barrier()
+    torch.cuda.synchronize(dev)
+    launches0 = ctx.info()["launches"]
+    if clocks:
+        clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    rc, st = ctx.bdf_run(y, mk(args.steps))
+    ev1.record(stream)
+    torch.cuda.synchronize(dev)
+    clk = clocks.stop() if clocks else None
+    if pg is not None:
+        pg.barrier()
+    assert rc == 0, f"timed run failed: {rc} {st}"
+    return ev0.elapsed_time(ev1), st, ctx.info()["launches"] - launches0, clk, y
+
+
+def field_rel_err(a, b, nC):
+    """max over density, momentum (as a vector) and energy of max|a-b| / max|b|."""
+    a, b = a.reshape(5, nC), b.reshape(5, nC)
+    e = [float((a[0] - b[0]).abs().max() / b[0].abs().max()),
+         float((a[1:4] - b[1:4]).norm(dim=0).max() / b[1:4].norm(dim=0).max()),
+         float((a[4] - b[4]).abs().max() / b[4].abs().max())]
+    return max(e)
+
+
 def main():
     args = parse()
     world, rank, local, pg = dist_setup(args)
@@ -220,7 +275,7 @@ def main():
     from __graft_entry__ import build
     build()
     from fosolvers_gb300 import mesh as M
-    from fosolvers_gb300.euler import FLUX_FP32, ILU_COLOR, ILU_FP32, FOEuler, PolyFvGrid
+    from fosolvers_gb300.euler import PolyFvGrid
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
@@ -228,48 +283,41 @@ def main():
     wl = M.make_workload(args.workload, scale=args.scale)
     grid = PolyFvGrid.from_mesh(wl.mesh)
     ibc = M.ibc_for(wl.mesh, wl.bc_gid)
-    flags = (FLUX_FP32 | ILU_FP32) if args.mode == "fp32" else 0
-    if args.ilu_order == "color":
-        flags |= ILU_COLOR
     stream = torch.cuda.current_stream(dev)
-    ctx = FOEuler(grid, ibc, wl.bc_type, wl.bc_param, wl.gamm, wl.r, flags=flags, stream=stream)
+    ctx = make_ctx(grid, ibc, wl, args.mode, args.ilu_order, stream)
     nC, nF = grid.nC, grid.nP
     N = 5 * nC
     y0_host = M.soa(wl.elem_state, nC)
     y0_ref = torch.from_numpy(y0_host).to(dev)
     y0 = torch.empty_like(y0_ref)
     ctx.to_internal(y0_ref, y0)
-    precond = 1 if args.precond == "ilu" else 0
-    mk = lambda n, **kw: ctx.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=n, precond=precond, **kw)
+    precond = PRECOND[args.precond]
+    gnn = None
+    if args.precond == "learned":
+        from fosolvers_gb300.learned import GNN
+        gnn = GNN(seed=0)
+        from fosolvers_gb300.learned import DEFAULT_WEIGHTS
+        gnn.load(args.weights or DEFAULT_WEIGHTS)
+        ctx.attach_gnn(gnn)
+
+    def mk_for(pc):
+        return lambda n, **kw: ctx.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=n, precond=pc, **kw)
+
+    mk = mk_for(precond)
     setup_s = time.perf_counter() - t_setup
 
-    # warm-up (also builds the block sparsity, level sets and the driver workspace)
-    y = y0.clone()
-    rc, _ = ctx.bdf_run(y, mk(args.warmup))
-    assert rc == 0, f"warm-up failed: {rc}"
-    torch.cuda.synchronize(dev)
-
-    # timed region: K BDF steps from the initial state (inputs > L2: state 0.2 GB, factors 5 GB)
-    y = y0.clone()
-    clocks = Clocks(local)
-    if pg is not None:
-        pg.barrier()
-    torch.cuda.synchronize(dev)
-    launches0 = ctx.info()["launches"]
-    clocks.start()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    rc, st = ctx.bdf_run(y, mk(args.steps))
-    ev1.record(stream)
-    torch.cuda.synchronize(dev)
-    clk = clocks.stop()
-    if pg is not None:
-        pg.barrier()
-    assert rc == 0, f"timed run failed: {rc} {st}"
-    launches = ctx.info()["launches"] - launches0
-    ms = ev0.elapsed_time(ev1)
+    # headline: K BDF steps with the state in HBM (inputs > L2: state 0.2 GB, factors ~3-5 GB)
+    ms, st, launches, clk, y = timed_bdf(ctx, y0, mk, args, dev, stream, pg, Clocks(local))
     ms_max = allmax(pg, ms, dev)
     value = world * args.steps / (ms_max / 1000.0)
+
+    # the same steps with ILU(0) alone in the same precision (learned runs only)
+    alt = {}
+    if args.precond == "learned" and not args.no_compare:
+        ms_i, st_i, _, _, _ = timed_bdf(ctx, y0, mk_for(1), args, dev, stream, pg)
+        alt[f"{args.mode}_ilu"] = {"value": world * args.steps / (allmax(pg, ms_i, dev) / 1e3),
+                                   "ms_per_step": ms_i / args.steps,
+                                   "n_lin_iters": st_i["n_lin_iters"]}
 
     # end to end: host buffer in the caller's cell order, copied in and out every step
     e2e = None
@@ -289,7 +337,6 @@ def main():
     # per-operation timing (CUDA events on the library stream)
     ops = {}
     if not args.no_ops:
-        import math
         f = torch.empty_like(y)
         v = torch.randn(N, dtype=torch.float64, device=dev)
         out = torch.empty_like(y)
@@ -317,16 +364,41 @@ def main():
         t_psol = timeit(lambda: ctx.psol_dev(v, out), R)
         lev = info["nlev_fwd"] + info["nlev_bwd"]
         a_, f_ = nC, nF
+        n_gnn = st["n_psol"] - st["n_fallback"] if gnn is not None else 0
         ops = {
             "residual": {"ms": t_rhs, "bytes": 88 * a_ + 40 * f_, "count": st["n_rhs"] - st["n_jv"]},
             "jv": {"ms": t_jv, "bytes": 168 * a_ + 40 * f_, "count": st["n_jv"]},
-            "ilu_apply": {"ms": t_psol, "bytes": 25 * fb * nnzb + 80 * a_, "count": st["n_psol"],
-                          "levels": lev},
+            "ilu_apply": {"ms": t_psol, "bytes": 25 * fb * nnzb + 80 * a_,
+                          "count": st["n_psol"] - n_gnn, "levels": lev},
             "pset": {"ms": t_pset, "bytes": 88 * a_ + 40 * f_ + 600 * nnzb, "count": st["n_pset"]},
         }
+        if gnn is not None:
+            t_gnn = timeit(lambda: gnn.apply_dev(ctx, y, v, out, gamma), R)
+            ops["gnn_apply"] = {"ms": t_gnn, "bytes": GNN_BYTES_PER_CELL * a_, "count": n_gnn}
         for k, o in ops.items():
             o["GBps"] = o["bytes"] / (o["ms"] * 1e-3) / 1e9
             o["ms_per_step"] = o["ms"] * o["count"] / args.steps
+    info = ctx.info()
+    y_out = torch.empty_like(y)
+    ctx.to_reference(y, y_out)
+    ctx.close()
+
+    # the plain FP64 ILU(0)-GMRES path on the same mesh and state: the target's denominator
+    vs64 = None
+    if args.mode == "fp32" and not args.no_compare:
+        ctx64 = make_ctx(grid, ibc, wl, "fp64", args.ilu_order, stream)
+        y064 = torch.empty_like(y0_ref)
+        ctx64.to_internal(y0_ref, y064)
+        mk64 = lambda n, **kw: ctx64.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=n, precond=1, **kw)
+        ms64, st64, _, _, y64 = timed_bdf(ctx64, y064, mk64, args, dev, stream, pg)
+        v64 = world * args.steps / (allmax(pg, ms64, dev) / 1000.0)
+        yb = torch.empty_like(y)
+        ctx64.to_reference(y64, yb)  # both states in the reference cell order
+        vs64 = {"value": v64, "ms_per_step": ms64 / args.steps, "ratio": value / v64,
+                "n_lin_iters": st64["n_lin_iters"],
+                "state_rel_err_vs_fp64": field_rel_err(y_out, yb, nC)}
+        ctx64.close()
+
     peaks = {}
     pk = ROOT / "MEASURED_PEAKS.json"
     if pk.exists():
@@ -363,18 +435,17 @@ def main():
             "config": {"workload": workload_desc(args.workload) if args.scale is None else
                        f"{args.workload} at scale {args.scale}",
                        "cells": nC, "faces": nF, "mode": args.mode, "precond": args.precond,
-                       "ilu_order": args.ilu_order, "ilu_levels": [ctx.info()["nlev_fwd"],
-                                                                  ctx.info()["nlev_bwd"]],
+                       "ilu_order": args.ilu_order, "ilu_levels": [info["nlev_fwd"], info["nlev_bwd"]],
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
-                       "l2": "inputs larger than L2 (state 0.2 GB, ILU factors ~5 GB); no flush",
+                       "l2": "inputs larger than L2 (state 0.2 GB, ILU factors ~3-5 GB); no flush",
                        "setup_s": round(setup_s, 2)},
             "clocks": clk, "e2e": e2e, "gpu_launches": launches,
             "roofline": roof, "cpu_baseline": cpu,
+            "vs_fp64_ilu": vs64, "same_precision_ilu": alt or None,
             "stats": {k: st[k] for k in ("n_rhs", "n_jv", "n_psol", "n_pset", "n_newton",
-                                          "n_lin_iters", "n_steps")},
+                                          "n_lin_iters", "n_steps", "n_fallback")},
         }
         print(json.dumps(line), flush=True)
-    ctx.close()
     if pg is not None:
         pg.barrier()
         pg.destroy_process_group()

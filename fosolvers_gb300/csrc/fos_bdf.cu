@@ -71,7 +71,9 @@ __global__ void __launch_bounds__(kT) k_mdot(long n, const double* __restrict__ 
   block_reduce_store<NA>(acc, NA, part);
 }
 
-// w -= sum_l h[l] V_l ; then part <- V_l . w (MODE 0, CGS2 second pass) or ||w||^2 (MODE 1)
+// w -= sum_l h[l] V_l ; then part <- V_l . w (MODE 0, CGS2 second pass), ||w||^2 (MODE 1),
+// or both (MODE 2: the DGKS test and, when it fails, the second pass's coefficients come
+// out of the same sweep over V)
 template <int NV, int MODE>
 __global__ void __launch_bounds__(kT) k_update(long n, const double* __restrict__ V, long ldv,
                                                const double* __restrict__ h,
@@ -80,7 +82,7 @@ __global__ void __launch_bounds__(kT) k_update(long n, const double* __restrict_
   __shared__ double hs[NV];
   if (threadIdx.x < NV) hs[threadIdx.x] = h[threadIdx.x];
   __syncthreads();
-  constexpr int NA = MODE == 0 ? NV : 1;
+  constexpr int NA = MODE == 0 ? NV : MODE == 1 ? 1 : NV + 1;
   double acc[NA];
 #pragma unroll
   for (int l = 0; l < NA; l++) acc[l] = 0.0;
@@ -93,12 +95,11 @@ __global__ void __launch_bounds__(kT) k_update(long n, const double* __restrict_
       wi -= hs[l] * vv[l];
     }
     w[i] = wi;
-    if (MODE == 0) {
+    if (MODE != 1) {
 #pragma unroll
-      for (int l = 0; l < NA; l++) acc[l] += vv[l] * wi;
-    } else {
-      acc[0] += wi * wi;
+      for (int l = 0; l < NV; l++) acc[l] += vv[l] * wi;
     }
+    if (MODE != 0) acc[NA - 1] += wi * wi;
   }
   block_reduce_store<NA>(acc, NA, part);
 }
@@ -173,6 +174,8 @@ struct fos_bdf_work {
   int maxl = 0;
   bool has_hist = false;  // yn holds the last accepted state, ym the one before
   int ilu_ref_its = -1;   // learned mode: iterations of the last ILU(0)-preconditioned solve
+  int learned_backoff = 0;  // learned mode: solves skipped after the last fallback
+  int learned_skip = 0;     // learned mode: solves still to run with ILU(0) alone
   double t_last = 0.0;
   double *V = nullptr, *Z = nullptr, *w = nullptr, *yn = nullptr, *ym = nullptr,
          *hist = nullptr, *f = nullptr, *b = nullptr, *d = nullptr, *part = nullptr,
@@ -324,6 +327,7 @@ struct Driver {
   }
 
   long reorth = 0;
+  bool last_reorth = false;  // the previous Arnoldi step needed the second Gram--Schmidt pass
   // GMRES on J_G d = b; d starts at zero.  With a learned preconditioner (o.precond >= 2)
   // this is flexible GMRES (Z_j = M_j(V_j) kept); in modes 2 and 4 it falls back to ILU(0)
   // -- restarting from the current iterate -- when the residual estimate stagnates (> 0.9
@@ -336,6 +340,10 @@ struct Driver {
     gamma_cur = gamma;
     const bool with_fallback = pc == 2 || pc == 4;
     if (with_fallback && ilu_ref_its < 0) pc = 1;  // no ILU reference yet: this solve sets it
+    if (with_fallback && pc != 1 && wk.learned_skip > 0) {  // back-off after a fallback
+      wk.learned_skip--;
+      pc = 1;
+    }
     const bool pure_ilu = pc == 1;
     if (pc == 1 || pc >= 4) {
       if (int rc = ensure_pset()) return rc;
@@ -365,21 +373,35 @@ struct Driver {
         const int nv = j + 1;
         // classical Gram--Schmidt, re-orthogonalised only when the first pass removed more
         // than 1 - 1/sqrt(2) of ||w|| (Daniel--Gragg--Kaufman--Stewart criterion)
+        // When the previous step needed the second pass, the first update also returns
+        // V^T w' (MODE 2) so the second pass needs no separate sweep over V for its
+        // coefficients; otherwise it returns ||w'||^2 only (MODE 1).
+        const bool fused = last_reorth;
         if ((rc = mdot<true>(nv, wk.V, N, wk.w))) return rc;           // h, ||w||^2
         if ((rc = reduce(nv + 1, wk.sc))) return rc;
-        if ((rc = update<1>(nv, wk.V, N, wk.sc, wk.w))) return rc;     // w -= V h, ||w||^2
-        if ((rc = reduce(1, wk.sc + kMaxVec))) return rc;
-        if ((rc = fetch(wk.sc, hbuf.data(), kMaxVec + 1))) return rc;
+        if (fused) {
+          if ((rc = update<2>(nv, wk.V, N, wk.sc, wk.w))) return rc;   // w -= V h; V^T w, ||w||^2
+          if ((rc = reduce(nv + 1, wk.sc + kMaxVec))) return rc;
+          if ((rc = fetch(wk.sc, hbuf.data(), 2 * kMaxVec))) return rc;
+        } else {
+          if ((rc = update<1>(nv, wk.V, N, wk.sc, wk.w))) return rc;   // w -= V h, ||w||^2
+          if ((rc = reduce(1, wk.sc + kMaxVec + nv))) return rc;
+          if ((rc = fetch(wk.sc, hbuf.data(), kMaxVec + nv + 1))) return rc;
+        }
         double* col = &H[(size_t)(m + 1) * j];
         for (int l = 0; l < nv; l++) col[l] = hbuf[l];
-        double hn2 = hbuf[kMaxVec];
-        if (hn2 < 0.5 * hbuf[nv]) {
-          if ((rc = mdot<false>(nv, wk.V, N, wk.w))) return rc;
-          if ((rc = reduce(nv, wk.sc + 2 * kMaxVec))) return rc;
-          if ((rc = update<1>(nv, wk.V, N, wk.sc + 2 * kMaxVec, wk.w))) return rc;
+        double hn2 = hbuf[kMaxVec + nv];
+        last_reorth = hn2 < 0.5 * hbuf[nv];
+        if (last_reorth) {
+          const double* h2 = wk.sc + kMaxVec;  // V^T w' (device), from MODE 2 or a sweep
+          if (!fused) {
+            if ((rc = mdot<false>(nv, wk.V, N, wk.w))) return rc;
+            if ((rc = reduce(nv, wk.sc + kMaxVec))) return rc;
+          }
+          if ((rc = update<1>(nv, wk.V, N, h2, wk.w))) return rc;
           if ((rc = reduce(1, wk.sc + 3 * kMaxVec))) return rc;
-          if ((rc = fetch(wk.sc + 2 * kMaxVec, hbuf.data() + 2 * kMaxVec, kMaxVec + 1))) return rc;
-          for (int l = 0; l < nv; l++) col[l] += hbuf[2 * kMaxVec + l];
+          if ((rc = fetch(wk.sc + kMaxVec, hbuf.data() + kMaxVec, 2 * kMaxVec + 1))) return rc;
+          for (int l = 0; l < nv; l++) col[l] += hbuf[kMaxVec + l];
           hn2 = hbuf[3 * kMaxVec];
           reorth++;
         }
@@ -417,10 +439,14 @@ struct Driver {
       FOS_LAUNCH_CHECK();
       if (conv) {
         if (pure_ilu) ilu_ref_its = *its;
+        if (with_fallback && pc != 1) wk.learned_backoff = 0;  // the network won this solve
         return 0;
       }
       if (fallback) {  // continue with ILU(0) from the current iterate
         st.n_fallback++;
+        // exponential back-off: skip the network for the next 1, 2, 4, ... 64 solves
+        wk.learned_backoff = wk.learned_backoff ? std::min(2 * wk.learned_backoff, 64) : 1;
+        wk.learned_skip = wk.learned_backoff;
         pc = 1;
         if (int rc = ensure_pset()) return rc;
         extra_cycles++;

@@ -131,6 +131,62 @@ __device__ __forceinline__ void split_hl_bits(double x, float& hi, float& lo) {
   lo = d2f_trunc(x - xh);
 }
 
+// ------------------------------------------------------------------ double-float
+// Unevaluated pairs x = h + l of binary32 numbers (|l| <= ulp(h)/2 after normalisation),
+// about 2^-46 relative precision, from the error-free transformations of Knuth (TwoSum),
+// Dekker (FastTwoSum) and the FMA form of Dekker's TwoProduct -- FP32 instructions only,
+// for arithmetic that needs more than FP32 but runs on GB300's full-rate FP32 pipe instead
+// of its 1/64-rate FP64 pipe.
+struct df2 {
+  float h, l;
+};
+__device__ __forceinline__ df2 df_fast_two_sum(float a, float b) {  // requires |a| >= |b|
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+__device__ __forceinline__ df2 df_two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ df2 df_add(df2 x, df2 y) {
+  const df2 s = df_two_sum(x.h, y.h);
+  return df_fast_two_sum(s.h, s.l + (x.l + y.l));
+}
+__device__ __forceinline__ df2 df_mul(df2 x, df2 y) {
+  const float p = x.h * y.h;
+  const float e = fmaf(x.h, y.l, fmaf(x.l, y.h, fmaf(x.h, y.h, -p)));
+  return df_fast_two_sum(p, e);
+}
+__device__ __forceinline__ df2 df_scale(df2 x, float k) {  // k a power of two: exact
+  return {x.h * k, x.l * k};
+}
+// 1/x: FP32 reciprocal of the head, one Newton correction r = 1 - x q0 carried in the tail
+__device__ __forceinline__ df2 df_rcp(df2 x) {
+  const float q0 = __frcp_rn(x.h);
+  const float r = fmaf(-x.l, q0, fmaf(-x.h, q0, 1.0f));
+  return df_fast_two_sum(q0, q0 * r);
+}
+// binary64 -> pair, exact to 48 bits: head = top 24 significand bits, tail = the next 24
+// (truncated); integer instructions only.  Magnitudes outside [2^-74, 2^127) lose the tail.
+__device__ __forceinline__ df2 df_from_double(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ffull);
+  const unsigned rem = (unsigned)(b & 0x1fffffffull);  // the 29 bits below the head
+  const int es = e - 948;  // binary32 exponent field of 2^(e - 1075)
+  float l = 0.0f;
+  if (rem != 0u && es >= 1 && es <= 254) {
+    l = __uint2float_rz(rem) * __uint_as_float((unsigned)es << 23);
+    if (b >> 63) l = -l;
+  }
+  return {d2f_trunc(x), l};
+}
+// finiteness from the exponent field (integer instructions, no FP64 compare)
+__device__ __forceinline__ bool finite_bits(double x) {
+  return ((unsigned long long)__double_as_longlong(x) & 0x7ff0000000000000ull) !=
+         0x7ff0000000000000ull;
+}
+
 // 1/a in FP64 by Newton--Raphson iteration x <- x (2 - a x) from an FP32 seed (two steps
 // take the ~2^-23 seed error to the FP64 rounding level); four FP64 FMAs
 __device__ __forceinline__ double rcp64(double a) {

@@ -63,15 +63,24 @@ __device__ __forceinline__ void mma16816(float c[4], const unsigned a[4], const 
 
 // Fragments of a row-major A tile (element (r, k) at A[r * lda + k]) and of a B tile given
 // as element (k, n) at B[k * sk + n * sn]; both in shared memory as BF16 bits.
+// (lda and k0 even, A 4-byte aligned: each register is one 32-bit shared load)
 __device__ __forceinline__ void load_a(const unsigned short* A, int lda, int r0, int k0,
                                        unsigned a[4]) {
   const int g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
-  const unsigned short* p0 = A + (r0 + g) * lda + k0 + 2 * t;
-  const unsigned short* p1 = A + (r0 + g + 8) * lda + k0 + 2 * t;
-  a[0] = pack2(p0[0], p0[1]);
-  a[1] = pack2(p1[0], p1[1]);
-  a[2] = pack2(p0[8], p0[9]);
-  a[3] = pack2(p1[8], p1[9]);
+  const unsigned* p0 = reinterpret_cast<const unsigned*>(A + (r0 + g) * lda + k0 + 2 * t);
+  const unsigned* p1 = reinterpret_cast<const unsigned*>(A + (r0 + g + 8) * lda + k0 + 2 * t);
+  a[0] = p0[0];
+  a[1] = p1[0];
+  a[2] = p0[4];
+  a[3] = p1[4];
+}
+// B fragment when k is contiguous: element (k, n) at B[n * ldn + k] (ldn, k0 even)
+__device__ __forceinline__ void load_b_kc(const unsigned short* B, int ldn, int k0, int n0,
+                                          unsigned b[2]) {
+  const int g = (threadIdx.x & 31) >> 2, t = threadIdx.x & 3;
+  const unsigned* p = reinterpret_cast<const unsigned*>(B + (n0 + g) * ldn + k0 + 2 * t);
+  b[0] = p[0];
+  b[1] = p[4];
 }
 __device__ __forceinline__ void load_b(const unsigned short* B, int sk, int sn, int k0, int n0,
                                        unsigned b[2]) {
@@ -99,7 +108,10 @@ __device__ __forceinline__ void gate2(const float* __restrict__ Gc, float ex, fl
 }
 
 // ------------------------------------------------------------------ forward
-// per-cell input features and h0 (thread per cell)
+// Input layer, 256 cells per CTA.  Phase 1: thread per cell computes the 16 features into
+// shared memory.  Phase 2: a warp per cell, lane l owns hidden channels 2l, 2l+1 with its
+// two rows of W0 (and b0) in registers as pairs: 16 packed FMAs per cell and lane, and the
+// BF16 row of h0 leaves as one coalesced 128-byte store.
 __global__ void __launch_bounds__(256) k_gnn_in(int nC, const double* __restrict__ y,
                                                 const double* __restrict__ v,
                                                 const double* __restrict__ invV, float gam_dt,
@@ -108,52 +120,79 @@ __global__ void __launch_bounds__(256) k_gnn_in(int nC, const double* __restrict
                                                 const GnnScales* __restrict__ sc,
                                                 float* __restrict__ X0,
                                                 unsigned short* __restrict__ h0) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nC) return;
-  const GnnScales s = *sc;
-  float x[NIN];
-  x[0] = d2f_trunc(y[i]) / s.sy[0];
-  x[1] = d2f_trunc(y[(size_t)nC + i]) / s.sy[1];
-  x[2] = d2f_trunc(y[2 * (size_t)nC + i]) / s.sy[1];
-  x[3] = d2f_trunc(y[3 * (size_t)nC + i]) / s.sy[1];
-  x[4] = d2f_trunc(y[4 * (size_t)nC + i]) / s.sy[2];
+  __shared__ __align__(16) float xs[256][NIN];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int f0 = 2 * lane;
+  float2 w[NIN];
 #pragma unroll
-  for (int q = 0; q < 5; q++) x[5 + q] = d2f_trunc(v[(size_t)q * nC + i]) / s.sv[q];
-  const float iv = d2f_trunc(invV[i]);
-  x[10] = -logf(iv) - s.lvmean;
+  for (int k = 0; k < NIN; k++) w[k] = make_float2(Wb[OFF_W0 + NIN * f0 + k], Wb[OFF_W0 + NIN * (f0 + 1) + k]);
+  const float2 bias = make_float2(Wb[OFF_B0 + f0], Wb[OFF_B0 + f0 + 1]);
+  const int nchunk = (nC + 255) / 256;
+  for (int chunk = blockIdx.x; chunk < nchunk; chunk += gridDim.x) {  // persistent
+  const int c0 = chunk * 256;
+  __syncthreads();  // the previous chunk's features are consumed
   {
-    const float r = d2f_trunc(y[i]);
-    const float mx = d2f_trunc(y[(size_t)nC + i]), my = d2f_trunc(y[2 * (size_t)nC + i]),
-                mz = d2f_trunc(y[3 * (size_t)nC + i]), E = d2f_trunc(y[4 * (size_t)nC + i]);
-    const float q2 = (mx * mx + my * my + mz * mz) / (r * r);
-    const float p = (gas_g - 1.0f) * (E - 0.5f * r * q2);
-    const float cs = sqrtf(fmaxf(gas_g * p / r, 0.0f));
-    const float cfl = gam_dt * (sqrtf(q2) + cs) * cbrtf(iv);
-    x[11] = logf(fmaxf(cfl, 1e-12f));
-  }
+    const int i = c0 + threadIdx.x;
+    float x[NIN];
 #pragma unroll
-  for (int k = 12; k < NIN; k++) x[k] = 0.0f;
-  if (X0) {
-    float4* xo = reinterpret_cast<float4*>(X0 + (size_t)NIN * i);
+    for (int k = 0; k < NIN; k++) x[k] = 0.0f;
+    if (i < nC) {
+      const GnnScales s = *sc;
+      x[0] = d2f_trunc(y[i]) / s.sy[0];
+      x[1] = d2f_trunc(y[(size_t)nC + i]) / s.sy[1];
+      x[2] = d2f_trunc(y[2 * (size_t)nC + i]) / s.sy[1];
+      x[3] = d2f_trunc(y[3 * (size_t)nC + i]) / s.sy[1];
+      x[4] = d2f_trunc(y[4 * (size_t)nC + i]) / s.sy[2];
 #pragma unroll
-    for (int k = 0; k < NIN / 4; k++) xo[k] = make_float4(x[4 * k], x[4 * k + 1], x[4 * k + 2], x[4 * k + 3]);
-  }
-  const float* W0 = Wb + OFF_W0;
-  const float* b0 = Wb + OFF_B0;
-  unsigned out[H / 2];
-#pragma unroll 4
-  for (int f = 0; f < H; f += 2) {
-    float a0 = b0[f], a1 = b0[f + 1];
+      for (int q = 0; q < 5; q++) x[5 + q] = d2f_trunc(v[(size_t)q * nC + i]) / s.sv[q];
+      const float iv = d2f_trunc(invV[i]);
+      x[10] = -logf(iv) - s.lvmean;
+      const float r = d2f_trunc(y[i]);
+      const float mx = d2f_trunc(y[(size_t)nC + i]), my = d2f_trunc(y[2 * (size_t)nC + i]),
+                  mz = d2f_trunc(y[3 * (size_t)nC + i]), E = d2f_trunc(y[4 * (size_t)nC + i]);
+      const float q2 = (mx * mx + my * my + mz * mz) / (r * r);
+      const float p = (gas_g - 1.0f) * (E - 0.5f * r * q2);
+      const float cs = sqrtf(fmaxf(gas_g * p / r, 0.0f));
+      const float cfl = gam_dt * (sqrtf(q2) + cs) * cbrtf(iv);
+      x[11] = logf(fmaxf(cfl, 1e-12f));
+      if (X0) {
+        float4* xo = reinterpret_cast<float4*>(X0 + (size_t)NIN * i);
 #pragma unroll
-    for (int k = 0; k < NIN; k++) {
-      a0 += W0[NIN * f + k] * x[k];
-      a1 += W0[NIN * (f + 1) + k] * x[k];
+        for (int k = 0; k < NIN / 4; k++) xo[k] = make_float4(x[4 * k], x[4 * k + 1], x[4 * k + 2], x[4 * k + 3]);
+      }
     }
-    out[f / 2] = pack2(bf(fmaxf(a0, 0.0f)), bf(fmaxf(a1, 0.0f)));
-  }
-  uint4* dst = reinterpret_cast<uint4*>(h0 + (size_t)H * i);
 #pragma unroll
-  for (int k = 0; k < H / 8; k++) dst[k] = make_uint4(out[4 * k], out[4 * k + 1], out[4 * k + 2], out[4 * k + 3]);
+    for (int k = 0; k < NIN / 4; k++)
+      *reinterpret_cast<float4*>(&xs[threadIdx.x][4 * k]) =
+          make_float4(x[4 * k], x[4 * k + 1], x[4 * k + 2], x[4 * k + 3]);
+  }
+  __syncthreads();
+  // four cells per step (rows r0, r0 + 8, r0 + 16, r0 + 24): independent FMA chains
+  constexpr int U = 4;
+  for (int r0 = warp; r0 < 256; r0 += 8 * U) {
+    float2 a[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) a[u] = bias;
+#pragma unroll
+    for (int k4 = 0; k4 < NIN / 4; k4++) {
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const float4 xv = *reinterpret_cast<const float4*>(&xs[r0 + 8 * u][4 * k4]);
+        a[u] = __ffma2_rn(w[4 * k4 + 0], make_float2(xv.x, xv.x), a[u]);
+        a[u] = __ffma2_rn(w[4 * k4 + 1], make_float2(xv.y, xv.y), a[u]);
+        a[u] = __ffma2_rn(w[4 * k4 + 2], make_float2(xv.z, xv.z), a[u]);
+        a[u] = __ffma2_rn(w[4 * k4 + 3], make_float2(xv.w, xv.w), a[u]);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int i = c0 + r0 + 8 * u;
+      if (i < nC)
+        reinterpret_cast<unsigned*>(h0 + (size_t)H * i)[lane] =
+            pack2(bf(fmaxf(a[u].x, 0.0f)), bf(fmaxf(a[u].y, 0.0f)));
+    }
+  }
+  }
 }
 
 // edge features of ELL entry ent seen from cell i; returns the neighbour cell or -1
@@ -174,117 +213,180 @@ __device__ __forceinline__ int edge_of(int ent, const int2* __restrict__ faceLR,
   return (ent & 1) ? lr.x : lr.y;
 }
 
-// One message-passing layer for a tile of 64 cells: gather + gate (CUDA cores, FP32),
-// [h; m] A^T on the tensor cores, bias + relu, BF16 store.  Optionally keeps bf16(m).
+// One message-passing layer, persistent over tiles of 64 cells (128 threads):
+//   A. edge phase: the 256 (cell, ELL slot) pairs of the tile -> neighbour index and edge
+//      features in shared memory (all independent loads, one pass);
+//   B. gather + gate (CUDA cores, FP32): warp w takes cells w, w+4, ..., four cells per
+//      step, so 20 rows of h (128 B each) are in flight per warp;
+//   C. [h; bf16(m)] A^T on the tensor cores (mma.sync m16n8k16, BF16 in, FP32 accumulate);
+//   D. bias + relu -> BF16 into the warp's own rows of the tile, then coalesced 16-byte stores.
+// The layer weights are loaded once per CTA.  HEAD (last layer) also applies the output
+// head z = s_v (v / s_v + D h3 + d) from the tile in shared memory, so h3 is stored only
+// when training keeps it.  Optionally keeps bf16(m) for the backward pass.
+template <bool HEAD>
 __global__ void __launch_bounds__(kT) k_gnn_layer(
     int nC, int nFi, const int* __restrict__ ell, const int2* __restrict__ faceLR,
     const float4* __restrict__ faceNA, const GnnScales* __restrict__ sc,
     const float* __restrict__ Wl,            // layer block of the bf16-rounded FP32 weights
     const unsigned short* __restrict__ Ab,   // layer A in BF16 bits, 64 x 128 row-major
     const unsigned short* __restrict__ hin, unsigned short* __restrict__ hout,
-    unsigned short* __restrict__ mkeep) {
-  __shared__ unsigned short Xs[kTile][2 * H + 8];   // [h ; m] rows (+8 pad)
-  __shared__ unsigned short As[H][2 * H + 8];
-  __shared__ float Gs[H * 4 + H];
+    unsigned short* __restrict__ mkeep, const float* __restrict__ Wb,
+    const double* __restrict__ v, double* __restrict__ z, float* __restrict__ zhat) {
+  constexpr int RS = 2 * H + 8;  // row stride (bf16) of the tiles: 272 B, 16-byte aligned
+  __shared__ __align__(16) unsigned short Xs[kTile][RS];   // [h ; m], then the layer output
+  __shared__ __align__(16) unsigned short As[H][RS];
+  __shared__ float bs[H];
+  __shared__ __align__(16) int nbr[kTile][4];
+  __shared__ float4 ef[kTile][4];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int k = threadIdx.x; k < H * 2 * H; k += kT) As[k / (2 * H)][k % (2 * H)] = Ab[k];
-  for (int k = threadIdx.x; k < H * 5; k += kT) Gs[k] = Wl[L_G + k];
-  __syncthreads();
-  const float inv_amean = 1.0f / sc->amean;
-  const int c0 = blockIdx.x * kTile;
-  const int f0 = 2 * lane;
-  // gather: warp w handles cells w, w+4, ...
-  for (int r = warp; r < kTile; r += kT / 32) {
-    const int i = c0 + r;
-    unsigned hs = 0, ms = 0;
-    if (i < nC) {
-      hs = reinterpret_cast<const unsigned*>(hin + (size_t)H * i)[lane];
-      const int4 e4 = reinterpret_cast<const int4*>(ell)[i];
-      const int ents[4] = {e4.x, e4.y, e4.z, e4.w};
-      float m0 = 0.0f, m1 = 0.0f;
-#pragma unroll
-      for (int k = 0; k < 4; k++) {
-        float ex, ey, ez, ea;
-        const int j = edge_of(ents[k], faceLR, nFi, faceNA, inv_amean, ex, ey, ez, ea);
-        if (j < 0) continue;
-        float g0, g1;
-        gate2(Gs, ex, ey, ez, ea, f0, g0, g1);
-        const unsigned hj = reinterpret_cast<const unsigned*>(hin + (size_t)H * j)[lane];
-        m0 += g0 * fb((unsigned short)(hj & 0xffff));
-        m1 += g1 * fb((unsigned short)(hj >> 16));
-      }
-      ms = pack2(bf(m0), bf(m1));
-      if (mkeep) reinterpret_cast<unsigned*>(mkeep + (size_t)H * i)[lane] = ms;
-    }
-    reinterpret_cast<unsigned*>(&Xs[r][0])[lane] = hs;
-    reinterpret_cast<unsigned*>(&Xs[r][H])[lane] = ms;
+  const int g = lane >> 2, t = lane & 3;
+  for (int k = threadIdx.x; k < H * (2 * H / 8); k += kT) {
+    const int r = k / (2 * H / 8), c = k % (2 * H / 8);
+    *reinterpret_cast<uint4*>(&As[r][8 * c]) = reinterpret_cast<const uint4*>(Ab)[k];
   }
-  __syncthreads();
-  // tensor cores: rows 16*warp .. +15 of the tile, all 64 outputs, K = 128
-  float acc[8][4];
+  for (int k = threadIdx.x; k < H; k += kT) bs[k] = Wl[L_B + k];
+  const GnnScales s = *sc;
+  const float inv_amean = 1.0f / s.amean;
+  const int f0 = 2 * lane;
+  // the lane's gate rows G[f0], G[f0 + 1] and c[f0], c[f0 + 1] in registers, as pairs
+  const float2 gx = make_float2(Wl[L_G + 4 * f0 + 0], Wl[L_G + 4 * f0 + 4]);
+  const float2 gy = make_float2(Wl[L_G + 4 * f0 + 1], Wl[L_G + 4 * f0 + 5]);
+  const float2 gz = make_float2(Wl[L_G + 4 * f0 + 2], Wl[L_G + 4 * f0 + 6]);
+  const float2 ga = make_float2(Wl[L_G + 4 * f0 + 3], Wl[L_G + 4 * f0 + 7]);
+  const float2 gc = make_float2(Wl[L_C + f0], Wl[L_C + f0 + 1]);
+  // output head (last layer): B fragments of D^T (k = hidden channel, n = field) and d
+  unsigned dfr[4][2] = {{0u, 0u}, {0u, 0u}, {0u, 0u}, {0u, 0u}};
+  float dq[2] = {0.0f, 0.0f};
+  if (HEAD) {
+    const int n = g;  // field of this lane's B column
 #pragma unroll
-  for (int nt = 0; nt < 8; nt++)
+    for (int kk = 0; kk < 4; kk++) {
+      const int k0 = 16 * kk + 2 * t;
+      auto w = [&](int k) { return n < 5 ? bf(Wb[OFF_D + H * n + k]) : (unsigned short)0; };
+      dfr[kk][0] = pack2(w(k0), w(k0 + 1));
+      dfr[kk][1] = pack2(w(k0 + 8), w(k0 + 9));
+    }
+    dq[0] = 2 * t < 5 ? Wb[OFF_DB + 2 * t] : 0.0f;
+    dq[1] = 2 * t + 1 < 5 ? Wb[OFF_DB + 2 * t + 1] : 0.0f;
+  }
+  const int ntiles = (nC + kTile - 1) / kTile;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int c0 = tile * kTile;
+    // A. edges of the tile
+    for (int p = threadIdx.x; p < kTile * 4; p += kT) {
+      const int r = p >> 2, k = p & 3, i = c0 + r;
+      int j = -1;
+      float4 e = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      if (i < nC) {
+        float ex, ey, ez, ea;
+        j = edge_of(ell[4 * (size_t)i + k], faceLR, nFi, faceNA, inv_amean, ex, ey, ez, ea);
+        if (j >= 0) e = make_float4(ex, ey, ez, ea);
+      }
+      nbr[r][k] = j;
+      ef[r][k] = e;
+    }
+    __syncthreads();  // edges ready; the previous tile's output rows are stored
+    // B. gather + gate, four cells per step; gate and message as packed FP32 FMAs
+    //    (missing neighbours contribute (c + 0) * 0, which leaves the sum unchanged)
+    constexpr int U = 4;
+    for (int r0 = warp; r0 < kTile; r0 += 4 * U) {
+      unsigned hv[U][4], hs[U];
 #pragma unroll
-    for (int q = 0; q < 4; q++) acc[nt][q] = 0.0f;
+      for (int u = 0; u < U; u++) {
+        const int r = r0 + 4 * u, i = c0 + r;
+        const int4 nb = *reinterpret_cast<const int4*>(&nbr[r][0]);
+        const int js[4] = {nb.x, nb.y, nb.z, nb.w};
+        hs[u] = i < nC ? reinterpret_cast<const unsigned*>(hin + (size_t)H * i)[lane] : 0u;
 #pragma unroll
-  for (int kk = 0; kk < 2 * H; kk += 16) {
-    unsigned a[4];
-    load_a(&Xs[0][0], 2 * H + 8, 16 * warp, kk, a);
+        for (int k = 0; k < 4; k++)
+          hv[u][k] = js[k] >= 0 ? reinterpret_cast<const unsigned*>(hin + (size_t)H * js[k])[lane] : 0u;
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int r = r0 + 4 * u, i = c0 + r;
+        float2 m = make_float2(0.0f, 0.0f);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          const float4 e = ef[r][k];
+          float2 gg = __ffma2_rn(gx, make_float2(e.x, e.x), gc);
+          gg = __ffma2_rn(gy, make_float2(e.y, e.y), gg);
+          gg = __ffma2_rn(gz, make_float2(e.z, e.z), gg);
+          gg = __ffma2_rn(ga, make_float2(e.w, e.w), gg);
+          const unsigned hb = hv[u][k];
+          m = __ffma2_rn(gg, make_float2(__uint_as_float(hb << 16), __uint_as_float(hb & 0xffff0000u)), m);
+        }
+        const unsigned ms = pack2(bf(m.x), bf(m.y));
+        if (mkeep && i < nC) reinterpret_cast<unsigned*>(mkeep + (size_t)H * i)[lane] = ms;
+        reinterpret_cast<unsigned*>(&Xs[r][0])[lane] = hs[u];
+        reinterpret_cast<unsigned*>(&Xs[r][H])[lane] = ms;
+      }
+    }
+    __syncthreads();
+    // C. tensor cores: rows 16*warp .. +15 of the tile, all 64 outputs, K = 128
+    float acc[8][4];
+#pragma unroll
+    for (int nt = 0; nt < 8; nt++)
+#pragma unroll
+      for (int q = 0; q < 4; q++) acc[nt][q] = 0.0f;
+#pragma unroll
+    for (int kk = 0; kk < 2 * H; kk += 16) {
+      unsigned a[4];
+      load_a(&Xs[0][0], RS, 16 * warp, kk, a);
+#pragma unroll
+      for (int nt = 0; nt < 8; nt++) {
+        unsigned b[2];
+        // B(k, n) = A_l(n, k): k contiguous along the rows of As
+        load_b_kc(&As[0][0], RS, kk, 8 * nt, b);
+        mma16816(acc[nt], a, b);
+      }
+    }
+    // D. bias + relu -> BF16.  The m16n8 accumulator layout of output columns 16 kk .. +15
+    //    is the A-fragment layout of k-chunk kk, so the head runs from registers.
+    unsigned ob[8][2];
 #pragma unroll
     for (int nt = 0; nt < 8; nt++) {
-      unsigned b[2];
-      // B(k, n) = A_l(n, k): k along As rows' columns, n along As rows
-      load_b(&As[0][0], 1, 2 * H + 8, kk, 8 * nt, b);
-      mma16816(acc[nt], a, b);
+      const int col = 8 * nt + 2 * t;
+      ob[nt][0] = pack2(bf(fmaxf(acc[nt][0] + bs[col], 0.0f)), bf(fmaxf(acc[nt][1] + bs[col + 1], 0.0f)));
+      ob[nt][1] = pack2(bf(fmaxf(acc[nt][2] + bs[col], 0.0f)), bf(fmaxf(acc[nt][3] + bs[col + 1], 0.0f)));
     }
-  }
-  const int g = lane >> 2, t = lane & 3;
-  const float* bl = Wl + L_B;
+    if (hout) {  // stage the warp's own rows (no other warp reads them in this tile)
+      __syncwarp();
+      const int ra = 16 * warp + g, rb = ra + 8;
 #pragma unroll
-  for (int nt = 0; nt < 8; nt++) {
-    const int col = 8 * nt + 2 * t;
-    const int ra = c0 + 16 * warp + g, rb = ra + 8;
-    if (ra < nC)
-      reinterpret_cast<unsigned*>(hout + (size_t)H * ra)[col / 2] =
-          pack2(bf(fmaxf(acc[nt][0] + bl[col], 0.0f)), bf(fmaxf(acc[nt][1] + bl[col + 1], 0.0f)));
-    if (rb < nC)
-      reinterpret_cast<unsigned*>(hout + (size_t)H * rb)[col / 2] =
-          pack2(bf(fmaxf(acc[nt][2] + bl[col], 0.0f)), bf(fmaxf(acc[nt][3] + bl[col + 1], 0.0f)));
-  }
-}
-
-// output head: z = s_v (v/s_v + D h3 + d)  (thread per cell), optional loss terms
-__global__ void __launch_bounds__(256) k_gnn_out(int nC, const unsigned short* __restrict__ h3,
-                                                 const float* __restrict__ Wb,
-                                                 const GnnScales* __restrict__ sc,
-                                                 const double* __restrict__ v,
-                                                 double* __restrict__ z, float* __restrict__ zhat) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nC) return;
-  const GnnScales s = *sc;
-  float h[H];
-  const uint4* src = reinterpret_cast<const uint4*>(h3 + (size_t)H * i);
+      for (int nt = 0; nt < 8; nt++) {
+        const int col = 8 * nt + 2 * t;
+        *reinterpret_cast<unsigned*>(&Xs[ra][col]) = ob[nt][0];
+        *reinterpret_cast<unsigned*>(&Xs[rb][col]) = ob[nt][1];
+      }
+      __syncwarp();
 #pragma unroll
-  for (int k = 0; k < H / 8; k++) {
-    const uint4 u = src[k];
-    const unsigned w[4] = {u.x, u.y, u.z, u.w};
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-      h[8 * k + 2 * q] = fb((unsigned short)(w[q] & 0xffff));
-      h[8 * k + 2 * q + 1] = fb((unsigned short)(w[q] >> 16));
+      for (int q = 0; q < 4; q++) {
+        const int idx = lane + 32 * q, row = idx >> 3, chunk = idx & 7;
+        const int i = c0 + 16 * warp + row;
+        if (i < nC)
+          reinterpret_cast<uint4*>(hout + (size_t)H * i)[chunk] =
+              *reinterpret_cast<const uint4*>(&Xs[16 * warp + row][8 * chunk]);
+      }
     }
-  }
-  const float* D = Wb + OFF_D;
-  const float* d = Wb + OFF_DB;
+    if (HEAD) {  // zhat = v / s_v + D h3 + d on the tensor cores (fields 0-4 of n = 8)
+      float o[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
-  for (int q = 0; q < 5; q++) {
-    float o = d[q];
+      for (int kk = 0; kk < 4; kk++) {
+        const unsigned a[4] = {ob[2 * kk][0], ob[2 * kk][1], ob[2 * kk + 1][0], ob[2 * kk + 1][1]};
+        mma16816(o, a, dfr[kk]);
+      }
 #pragma unroll
-    for (int k = 0; k < H; k++) o += D[H * q + k] * h[k];
-    const float vh = d2f_trunc(v[(size_t)q * nC + i]) / s.sv[q];
-    const float zh = vh + o;
-    if (zhat) zhat[(size_t)8 * i + q] = zh;
-    if (z) z[(size_t)q * nC + i] = f2d_bits(zh * s.sv[q]);
+      for (int e = 0; e < 4; e++) {
+        const int q = 2 * t + (e & 1);
+        const int i = c0 + 16 * warp + g + ((e & 2) ? 8 : 0);
+        if (q < 5 && i < nC) {
+          const float svq = sc->sv[q];
+          const float zh = d2f_trunc(v[(size_t)q * nC + i]) / svq + (o[e] + dq[e & 1]);
+          if (zhat) zhat[(size_t)8 * i + q] = zh;
+          if (z) z[(size_t)q * nC + i] = f2d_bits(zh * svq);
+        }
+      }
+    }
   }
 }
 
@@ -334,10 +436,15 @@ __global__ void __launch_bounds__(256) k_gnn_scale_part(int nC, int nF, const do
 }
 __global__ void k_gnn_scale_final(int nC, int nF, int np, const float* __restrict__ part,
                                   GnnScales* __restrict__ sc) {
-  if (threadIdx.x != 0) return;
+  // one warp: lane l sums partials l, l+32, ... (fixed order), then a shuffle tree
+  const int lane = threadIdx.x & 31;
   float s[10] = {0};
-  for (int b = 0; b < np; b++)
+  for (int b = lane; b < np; b += 32)
+#pragma unroll
     for (int k = 0; k < 10; k++) s[k] += part[10 * b + k];
+#pragma unroll
+  for (int k = 0; k < 10; k++) s[k] = warp_sumf(s[k]);
+  if (lane != 0) return;
   const float tiny = 1e-30f;
   GnnScales o;
   o.sy[0] = sqrtf(s[0] / nC) + tiny;
@@ -432,9 +539,9 @@ __global__ void __launch_bounds__(kT) k_gnn_layer_bwd(
     const unsigned short* __restrict__ hout, const float* __restrict__ dhout,
     const unsigned short* __restrict__ Ab, float* __restrict__ dhin, float* __restrict__ dm,
     float* __restrict__ part) {
-  __shared__ unsigned short Xs[kTile][2 * H + 8];   // [h_in ; m] rows
-  __shared__ unsigned short Ds[kTile][H + 8];       // bf16(delta) rows
-  __shared__ unsigned short As[H][2 * H + 8];
+  __shared__ __align__(16) unsigned short Xs[kTile][2 * H + 8];   // [h_in ; m] rows
+  __shared__ __align__(16) unsigned short Ds[kTile][H + 8];       // bf16(delta) rows
+  __shared__ __align__(16) unsigned short As[H][2 * H + 8];
   __shared__ float dbs[kT / 32][H];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int g = lane >> 2, tq = lane & 3;
@@ -704,6 +811,8 @@ struct fos_gnn {
   float* scp = nullptr;
   float* hs = nullptr;  // head partial sums
   int adam_t = 0;
+  int layer_ctas = 0;  // persistent grid of the layer kernel (resident CTAs on the device)
+  int in_ctas = 0;     // persistent grid of the input kernel
   ~fos_gnn() {
     void* ps[] = {w, wb, m1, m2, grad, Ab, X0, zhat, dh, dh2, dmb, part, sc, scp, hs};
     for (void* p : ps)
@@ -717,6 +826,7 @@ struct fos_gnn {
 
 namespace {
 constexpr int kPartBlocks = 304;  // persistent CTAs of the reductions (2 x 152 SMs)
+constexpr int kScaleBlocks = 1216;  // CTAs of the scale partial sums (8 x 152 SMs)
 
 int gnn_reserve(fos_gnn* g, long nC) {
   if (g->cap >= nC) return 0;
@@ -744,20 +854,25 @@ int gnn_forward(fos_gnn* g, fos_ctx* c, const double* y, const double* v, double
     return -2;
   }
   const int nC = c->nC;
-  fos_launch(c, k_gnn_scale_part, kPartBlocks, 256, nC, c->nF, y, v, (const double*)c->d_invV,
+  fos_launch(c, k_gnn_scale_part, kScaleBlocks, 256, nC, c->nF, y, v, (const double*)c->d_invV,
              (const float4*)c->d_faceNA32, g->scp);
-  fos_launch(c, k_gnn_scale_final, 1, 32, nC, c->nF, kPartBlocks, (const float*)g->scp, g->sc);
-  fos_launch(c, k_gnn_in, nblk(nC, 256), 256, nC, y, v, (const double*)c->d_invV,
+  fos_launch(c, k_gnn_scale_final, 1, 32, nC, c->nF, kScaleBlocks, (const float*)g->scp, g->sc);
+  fos_launch(c, k_gnn_in, std::max(1, std::min(nblk(nC, 256), g->in_ctas)), 256, nC, y, v, (const double*)c->d_invV,
              (float)gamma, (float)c->gamm, (const float*)g->wb, (const GnnScales*)g->sc, train ? g->X0 : (float*)nullptr,
              g->h[0]);
-  for (int l = 0; l < NL; l++)
-    fos_launch(c, k_gnn_layer, nblk(nC, kTile), kT, nC, c->nFi, (const int*)c->d_ell,
+  const int ntiles = (nC + kTile - 1) / kTile;
+  for (int l = 0; l < NL; l++) {
+    const bool last = l == NL - 1;
+    const int grid = std::max(1, std::min(ntiles, g->layer_ctas));
+    auto kern = last ? k_gnn_layer<true> : k_gnn_layer<false>;
+    fos_launch(c, kern, grid, kT, nC, c->nFi, (const int*)c->d_ell,
                (const int2*)c->d_faceLR, (const float4*)c->d_faceNA32, (const GnnScales*)g->sc,
                (const float*)(g->wb + OFF_L0 + l * L_SIZE),
                (const unsigned short*)(g->Ab + l * H * 2 * H), (const unsigned short*)g->h[l],
-               g->h[l + 1], train ? g->m[l] : (unsigned short*)nullptr);
-  fos_launch(c, k_gnn_out, nblk(nC, 256), 256, nC, (const unsigned short*)g->h[NL],
-             (const float*)g->wb, (const GnnScales*)g->sc, v, z, train ? g->zhat : (float*)nullptr);
+               (last && !train) ? (unsigned short*)nullptr : g->h[l + 1],
+               train ? g->m[l] : (unsigned short*)nullptr, (const float*)g->wb, v, z,
+               train ? g->zhat : (float*)nullptr);
+  }
   FOS_LAUNCH_CHECK();
   return 0;
 }
@@ -793,12 +908,22 @@ extern "C" int fos_gnn_create(fos_gnn** out, unsigned seed) {
       cudaMalloc(&g->m1, sizeof(float) * NPARAM) || cudaMalloc(&g->m2, sizeof(float) * NPARAM) ||
       cudaMalloc(&g->grad, sizeof(float) * NPARAM) ||
       cudaMalloc(&g->Ab, sizeof(unsigned short) * NL * H * 2 * H) ||
-      cudaMalloc(&g->sc, sizeof(GnnScales)) || cudaMalloc(&g->scp, sizeof(float) * 10 * kPartBlocks) ||
+      cudaMalloc(&g->sc, sizeof(GnnScales)) || cudaMalloc(&g->scp, sizeof(float) * 10 * kScaleBlocks) ||
       cudaMalloc(&g->hs, sizeof(float) * 512))
     return fail("cudaMalloc");
   g->part_len = (long)kPartBlocks * (H * 2 * H + H);
   g->part_len = std::max<long>(g->part_len, (long)kPartBlocks * (H * NIN + H));
   if (cudaMalloc(&g->part, sizeof(float) * g->part_len)) return fail("cudaMalloc");
+  {  // persistent grid of the layer kernel: every resident CTA of the device
+    int nsm = 0, per_t = 0, per_f = 0, per_in = 0;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, g->device) ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_t, k_gnn_layer<true>, kT, 0) ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_f, k_gnn_layer<false>, kT, 0) ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_in, k_gnn_in, 256, 0))
+      return fail("device attributes");
+    g->layer_ctas = std::max(1, nsm * std::max(1, std::min(per_t, per_f)));
+    g->in_ctas = std::max(1, nsm * std::max(1, per_in));
+  }
   cudaMemcpy(g->w, w.data(), sizeof(float) * NPARAM, cudaMemcpyHostToDevice);
   cudaMemset(g->m1, 0, sizeof(float) * NPARAM);
   cudaMemset(g->m2, 0, sizeof(float) * NPARAM);

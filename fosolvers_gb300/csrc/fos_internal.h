@@ -123,6 +123,7 @@ int fos_residual_launch(fos_ctx* c, const double* y, const double* v, const doub
 int fos_norm2_dev(fos_ctx* c, const double* x, long n, double* d_out_sq);
 int fos_permute(fos_ctx* c, const double* in, double* out, int dir);
 int fos_jv_sigma(fos_ctx* c, double* d_scal, double ynorm, double eps);
+int fos_prim_hl_launch(fos_ctx* c, const double* y);  // FP32 (hi, lo) primitives
 int fos_prim_launch(fos_ctx* c, const double* y);
 int fos_gnn_precond(fos_ctx* c, const double* y, const double* r, double gamma, double* z);
 // fos_jacobian.cu

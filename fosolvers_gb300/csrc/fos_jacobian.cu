@@ -65,7 +65,7 @@ __device__ __forceinline__ T nfj(int a, int b, const T n[3], const T u[3], T H, 
 // eulerANFJ as |vn| T0 + |vn - c| r- l-^T + |vn + c| r+ l+^T (row-major 25)
 template <typename T>
 __device__ __forceinline__ void anfj(const T n[3], const T u[3], T H, T c, T g, T out[25]) {
-  const T g1 = g - 1.0;
+  const T g1 = g - T(1);
   const T v2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
   const T vn = u[0] * n[0] + u[1] * n[1] + u[2] * n[2];
   const T ic = T(1) / c;
@@ -101,7 +101,70 @@ __device__ __forceinline__ void anfj(const T n[3], const T u[3], T H, T c, T g, 
   }
 }
 
+// primitives of one side of a face in the arithmetic type of the assembly
+template <typename T>
+struct PrimT {
+  T u[3], H, s;
+};
+
+// Blocks of face f from its two sides' primitives (Roe averages, Euler.f90:207-209): both
+// off-diagonal blocks of an interior face, or the boundary pair's diagonal term
 template <typename T, typename TJ>
+__device__ __forceinline__ void jac_face_blocks(int f, int nFi, const T n[3], T aP,
+                                                const PrimT<T>& L, const PrimT<T>& R, T gg,
+                                                const int* __restrict__ fslot,
+                                                TJ* __restrict__ J, TJ* __restrict__ Jb) {
+  const T inv = T(1) / (L.s + R.s);
+  const T ua[3] = {(L.s * L.u[0] + R.s * R.u[0]) * inv, (L.s * L.u[1] + R.s * R.u[1]) * inv,
+                   (L.s * L.u[2] + R.s * R.u[2]) * inv};
+  const T Ha = (L.s * L.H + R.s * R.H) * inv;
+  const T ca = sqrt((gg - T(1)) * (Ha - T(0.5) * (ua[0] * ua[0] + ua[1] * ua[1] + ua[2] * ua[2])));
+  T Ab[25];
+  anfj<T>(n, ua, Ha, ca, gg, Ab);
+  const T v2L = L.u[0] * L.u[0] + L.u[1] * L.u[1] + L.u[2] * L.u[2];
+  const T vnL = L.u[0] * n[0] + L.u[1] * n[1] + L.u[2] * n[2];
+  const T v2R = R.u[0] * R.u[0] + R.u[1] * R.u[1] + R.u[2] * R.u[2];
+  const T vnR = R.u[0] * n[0] + R.u[1] * n[1] + R.u[2] * n[2];
+  const T h = T(0.5) * aP;
+  if (f < nFi) {
+    TJ* oLR = J + 25 * (size_t)fslot[2 * f];      // block (L, R) = JacP(1:5,6:10)
+    TJ* oRL = J + 25 * (size_t)fslot[2 * f + 1];  // block (R, L) = JacP(6:10,1:5)
+#pragma unroll
+    for (int a = 0; a < 5; a++)
+#pragma unroll
+      for (int b = 0; b < 5; b++) {
+        oLR[5 * a + b] = (TJ)(-h * (nfj<T>(a, b, n, R.u, R.H, gg, v2R, vnR) - Ab[5 * a + b]));
+        oRL[5 * a + b] = (TJ)(h * (nfj<T>(a, b, n, L.u, L.H, gg, v2L, vnL) + Ab[5 * a + b]));
+      }
+  } else {
+    TJ* d = Jb + 25 * (size_t)(f - nFi);  // boundary pair's diagonal term
+#pragma unroll
+    for (int a = 0; a < 5; a++)
+#pragma unroll
+      for (int b = 0; b < 5; b++)
+        d[5 * a + b] = (TJ)(-h * (nfj<T>(a, b, n, L.u, L.H, gg, v2L, vnL) + Ab[5 * a + b]));
+  }
+}
+
+// ghost-side primitives of boundary face f (setBC, FP64; 1% of the faces)
+__device__ __forceinline__ void ghost_prim(int f, int nC, int2 lr, const double* __restrict__ y,
+                                           const int* __restrict__ bcT,
+                                           const double* __restrict__ bcP, int maxP, double nx,
+                                           double ny, double nz, double g, double r, Prim& R) {
+  double U[5], G[5];
+  for (int q = 0; q < 5; q++) U[q] = y[(size_t)q * nC + lr.x];
+  const int row = lr.y;
+  ghost_state(row > 0 ? bcT[row - 1] : FOS_BC_WALL,
+              row > 0 ? bcP + (size_t)maxP * (row - 1) : nullptr, U, nx, ny, nz, g, r, G);
+  const double inv = 1.0 / G[0];
+  R.rho = G[0]; R.u = G[1] * inv; R.v = G[2] * inv; R.w = G[3] * inv;
+  R.p = (g - 1.0) * (G[4] - 0.5 * (G[1] * G[1] + G[2] * G[2] + G[3] * G[3]) * inv);
+  R.H = (G[4] + R.p) * inv;
+  R.s = sqrt(G[0]);
+}
+
+// FP64 form: FP64 primitives and geometry
+template <typename TJ>
 __global__ void __launch_bounds__(kT) k_jac_face(int nFi, int nF, int nC,
                                                  const int2* __restrict__ faceLR,
                                                  const double2* __restrict__ faceNA,
@@ -116,54 +179,124 @@ __global__ void __launch_bounds__(kT) k_jac_face(int nFi, int nF, int nC,
   if (f >= nF) return;
   const int2 lr = faceLR[f];
   const double2 n01 = faceNA[2 * (size_t)f], n2a = faceNA[2 * (size_t)f + 1];
-  const T n[3] = {(T)n01.x, (T)n01.y, (T)n2a.x};
-  const T aP = (T)n2a.y;
+  const double n[3] = {n01.x, n01.y, n2a.x};
   Prim L, R;
   load_prim(W, lr.x, L);
-  if (f < nFi) {
-    load_prim(W, lr.y, R);
-  } else {
-    double U[5], G[5];
-    for (int q = 0; q < 5; q++) U[q] = y[(size_t)q * nC + lr.x];
-    const int row = lr.y;
-    ghost_state(row > 0 ? bcT[row - 1] : FOS_BC_WALL,
-                row > 0 ? bcP + (size_t)maxP * (row - 1) : nullptr, U, n01.x, n01.y, n2a.x, g, r, G);
-    const double inv = 1.0 / G[0];
-    R.rho = G[0]; R.u = G[1] * inv; R.v = G[2] * inv; R.w = G[3] * inv;
-    R.p = (g - 1.0) * (G[4] - 0.5 * (G[1] * G[1] + G[2] * G[2] + G[3] * G[3]) * inv);
-    R.H = (G[4] + R.p) * inv;
-    R.s = sqrt(G[0]);
-  }
-  // Roe averages (Euler.f90:207-209), arithmetic in T (FP64, or FP32 for the FP32 form)
-  const T gg = (T)g;
-  const T sL = (T)L.s, sR = (T)R.s;
-  const T inv = T(1) / (sL + sR);
-  const T ua[3] = {(sL * (T)L.u + sR * (T)R.u) * inv, (sL * (T)L.v + sR * (T)R.v) * inv,
-                   (sL * (T)L.w + sR * (T)R.w) * inv};
-  const T Ha = (sL * (T)L.H + sR * (T)R.H) * inv;
-  const T ca = sqrt((gg - T(1)) * (Ha - T(0.5) * (ua[0] * ua[0] + ua[1] * ua[1] + ua[2] * ua[2])));
-  T Ab[25];
-  anfj<T>(n, ua, Ha, ca, gg, Ab);
-  const T uL[3] = {(T)L.u, (T)L.v, (T)L.w}, uR[3] = {(T)R.u, (T)R.v, (T)R.w};
-  const T HL = (T)L.H, HR = (T)R.H;
-  const T v2L = uL[0] * uL[0] + uL[1] * uL[1] + uL[2] * uL[2];
-  const T vnL = uL[0] * n[0] + uL[1] * n[1] + uL[2] * n[2];
-  const T v2R = uR[0] * uR[0] + uR[1] * uR[1] + uR[2] * uR[2];
-  const T vnR = uR[0] * n[0] + uR[1] * n[1] + uR[2] * n[2];
-  const T h = T(0.5) * aP;
-  if (f < nFi) {
-    TJ* oLR = J + 25 * (size_t)fslot[2 * f];      // block (L, R) = JacP(1:5,6:10)
-    TJ* oRL = J + 25 * (size_t)fslot[2 * f + 1];  // block (R, L) = JacP(6:10,1:5)
-    for (int a = 0; a < 5; a++)
-      for (int b = 0; b < 5; b++) {
-        oLR[5 * a + b] = (TJ)(-h * (nfj<T>(a, b, n, uR, HR, gg, v2R, vnR) - Ab[5 * a + b]));
-        oRL[5 * a + b] = (TJ)(h * (nfj<T>(a, b, n, uL, HL, gg, v2L, vnL) + Ab[5 * a + b]));
+  if (f < nFi) load_prim(W, lr.y, R);
+  else ghost_prim(f, nC, lr, y, bcT, bcP, maxP, n01.x, n01.y, n2a.x, g, r, R);
+  const PrimT<double> PL = {{L.u, L.v, L.w}, L.H, L.s}, PR = {{R.u, R.v, R.w}, R.H, R.s};
+  jac_face_blocks<double, TJ>(f, nFi, n, n2a.y, PL, PR, g, fslot, J, Jb);
+}
+
+// FP32 form: FP32 arithmetic from the per-cell FP32 (hi, lo) primitives of the residual
+// (rounded to FP32) and the FP32 face geometry, so no FP64 instruction runs on interior
+// faces (the FP32 preconditioner is assembled and stored in FP32)
+__device__ __forceinline__ PrimT<float> load_prim_f32(const float* __restrict__ Whl, int c) {
+  const float4* w4 = reinterpret_cast<const float4*>(Whl + 16 * (size_t)c);
+  const float4 a = __ldg(w4), b = __ldg(w4 + 1), d = __ldg(w4 + 2), e = __ldg(w4 + 3);
+  // hi: (rho, u, v, w) = a, (H, p) = b.xy; lo: (rho, u) = b.zw, (v, w, H, p) = d
+  return {{a.y + b.w, a.z + d.x, a.w + d.y}, b.x + d.z, e.x};
+}
+
+// Cell-centric FP32 assembly: one thread per cell, cells in the internal (bandwidth-
+// reduced) order, so neighbouring cells' primitives and face data are L2 hits.  A thread
+// evaluates each face of its cell in the face's orientation (Roe average, |A~|, both
+// normal flux Jacobians -- the same expressions for both cells of the face) and keeps
+//   off-diagonal block:  cell L: block (L, R) = -aP/2 (A(u_R) - |A~|)
+//                        cell R: block (R, L) =  aP/2 (A(u_L) + |A~|)
+//   diagonal:            minus the column's off-diagonal blocks, plus the boundary pairs'
+//                        terms -aP/2 (A(u_m) + |A~|), in ELL order, in registers,
+// staging its block row (contiguous in position space) in shared memory; the warp then
+// stores the 32 rows one after another, each as contiguous 128-byte pieces.  Each face is
+// evaluated by both of its cells: FP32 arithmetic is cheap next to the scattered block
+// stores and the re-read of every off-diagonal block that a face-then-diagonal assembly
+// costs.
+template <int kW>
+__global__ void __launch_bounds__(64) k_jac_cell32(
+    int nC, int nFi, const int* __restrict__ ipos, const int* __restrict__ prow,
+    const int* __restrict__ cdiag, const int* __restrict__ ell, const int2* __restrict__ faceLR,
+    const float4* __restrict__ faceNA32, const int* __restrict__ fslot,
+    const float* __restrict__ Whl, const double* __restrict__ y, const int* __restrict__ bcT,
+    const double* __restrict__ bcP, int maxP, double g, double r, float* __restrict__ J) {
+  constexpr int kRow = (kW + 1) * 25;  // floats of a full block row
+  __shared__ float stg[2][32][kRow];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int c = (blockIdx.x * 2 + warp) * 32 + lane;
+  float* st = stg[warp][lane];
+  int s0 = 0, nbk = 0;
+  if (c < nC) {
+    const int p = ipos[c];
+    s0 = prow[p];
+    nbk = prow[p + 1] - s0;
+    const float gg = d2f_trunc(g);
+    const PrimT<float> P = load_prim_f32(Whl, c);
+    float D[25];
+#pragma unroll
+    for (int k = 0; k < 25; k++) D[k] = 0.0f;
+#pragma unroll 1
+    for (int k = 0; k < kW; k++) {
+      const int ek = __ldg(ell + (size_t)kW * c + k);
+      if (ek < 0) continue;
+      const int f = ek >> 1;
+      const bool isR = ek & 1;
+      const int2 lr = __ldg(faceLR + f);
+      const float4 na = __ldg(faceNA32 + f);
+      const float n[3] = {na.x, na.y, na.z};
+      PrimT<float> Q;
+      if (f < nFi) {
+        Q = load_prim_f32(Whl, isR ? lr.x : lr.y);
+      } else {
+        Prim R;
+        ghost_prim(f, nC, lr, y, bcT, bcP, maxP, f2d_bits(na.x), f2d_bits(na.y), f2d_bits(na.z),
+                   g, r, R);
+        Q = {{d2f_trunc(R.u), d2f_trunc(R.v), d2f_trunc(R.w)}, d2f_trunc(R.H), d2f_trunc(R.s)};
       }
-  } else {
-    TJ* d = Jb + 25 * (size_t)(f - nFi);  // boundary pair's diagonal term
-    for (int a = 0; a < 5; a++)
-      for (int b = 0; b < 5; b++)
-        d[5 * a + b] = (TJ)(-h * (nfj<T>(a, b, n, uL, HL, gg, v2L, vnL) + Ab[5 * a + b]));
+      const PrimT<float>& L = (f < nFi && isR) ? Q : P;
+      const PrimT<float>& R = (f < nFi && isR) ? P : Q;
+      const float inv = 1.0f / (L.s + R.s);
+      const float ua[3] = {(L.s * L.u[0] + R.s * R.u[0]) * inv, (L.s * L.u[1] + R.s * R.u[1]) * inv,
+                           (L.s * L.u[2] + R.s * R.u[2]) * inv};
+      const float Ha = (L.s * L.H + R.s * R.H) * inv;
+      const float ca =
+          sqrtf((gg - 1.0f) * (Ha - 0.5f * (ua[0] * ua[0] + ua[1] * ua[1] + ua[2] * ua[2])));
+      float Ab[25];
+      anfj<float>(n, ua, Ha, ca, gg, Ab);
+      const float v2L = L.u[0] * L.u[0] + L.u[1] * L.u[1] + L.u[2] * L.u[2];
+      const float vnL = L.u[0] * n[0] + L.u[1] * n[1] + L.u[2] * n[2];
+      const float v2R = R.u[0] * R.u[0] + R.u[1] * R.u[1] + R.u[2] * R.u[2];
+      const float vnR = R.u[0] * n[0] + R.u[1] * n[1] + R.u[2] * n[2];
+      const float h = 0.5f * na.w;
+      if (f >= nFi) {  // boundary pair: diagonal term only
+#pragma unroll
+        for (int a = 0; a < 5; a++)
+#pragma unroll
+          for (int b = 0; b < 5; b++)
+            D[5 * a + b] += -h * (nfj<float>(a, b, n, L.u, L.H, gg, v2L, vnL) + Ab[5 * a + b]);
+        continue;
+      }
+      float* off = st + 25 * (fslot[2 * f + (isR ? 1 : 0)] - s0);
+#pragma unroll
+      for (int a = 0; a < 5; a++)
+#pragma unroll
+        for (int b = 0; b < 5; b++) {
+          const float bLR = -h * (nfj<float>(a, b, n, R.u, R.H, gg, v2R, vnR) - Ab[5 * a + b]);
+          const float bRL = h * (nfj<float>(a, b, n, L.u, L.H, gg, v2L, vnL) + Ab[5 * a + b]);
+          off[5 * a + b] = isR ? bRL : bLR;
+          D[5 * a + b] -= isR ? bLR : bRL;
+        }
+    }
+    float* dg = st + 25 * (cdiag[c] - s0);
+#pragma unroll
+    for (int k = 0; k < 25; k++) dg[k] = D[k];
+  }
+  __syncwarp();
+  // the warp's rows, one after another: row r = [25 s0_r, 25 (s0_r + nbk_r)) of J
+  for (int rr = 0; rr < 32; rr++) {
+    const int sr = __shfl_sync(0xffffffffu, s0, rr);
+    const int nr = 25 * __shfl_sync(0xffffffffu, nbk, rr);
+    float* dst = J + 25 * (size_t)sr;
+    const float* src = stg[warp][rr];
+    for (int k = lane; k < nr; k += 32) dst[k] = src[k];
   }
 }
 
@@ -230,6 +363,15 @@ __device__ __forceinline__ bool inv5(T a[25]) {
 // A lane only touches its own row of row p's blocks and reads finished blocks of earlier
 // rows from global memory, so the lanes of a row need no synchronisation until the
 // diagonal inversion (warp shuffles).
+template <typename TF>
+__device__ __forceinline__ TF from64(double x) {
+  if constexpr (sizeof(TF) == 4) return d2f_trunc(x); else return (TF)x;
+}
+template <typename TF>
+__device__ __forceinline__ double to64(TF x) {
+  if constexpr (sizeof(TF) == 4) return f2d_bits(x); else return (double)x;
+}
+
 constexpr int kRowsPerCta = 6 * (kT / 32);
 constexpr int kMaxBlocksPerRow = 7;  // diagonal + up to 6 neighbours (hexahedra)
 
@@ -239,7 +381,11 @@ __global__ void __launch_bounds__(kT) k_ilu_factor(
     const int* __restrict__ pdiag, const int* __restrict__ ord, const double* __restrict__ invV,
     double gamma, const TJ* __restrict__ J, const int* __restrict__ upd_ptr,
     const int3* __restrict__ upd, TF* __restrict__ LU, int* __restrict__ ierr) {
+  // update operands (inv(D_q), U_qj of earlier levels) of the first kPre operations of a row
+  // are fetched into shared memory before the elimination, all loads in flight at once
+  constexpr int kPre = sizeof(TF) == 4 ? 8 : 0;
   __shared__ TF sm[kRowsPerCta][kMaxBlocksPerRow][25];
+  __shared__ TF bsm[kRowsPerCta][kPre > 0 ? kPre : 1][25];
   const int lane = threadIdx.x & 31;
   const int sub = lane / 5, a = lane - 5 * sub;
   const int lrow = (threadIdx.x >> 5) * 6 + (sub < 6 ? sub : 0);
@@ -247,26 +393,50 @@ __global__ void __launch_bounds__(kT) k_ilu_factor(
   const bool active = sub < 6 && t < n;
   const int p = active ? (rows ? rows[t] : p0 + t) : 0;
   TF D[5] = {TF(0), TF(0), TF(0), TF(0), TF(0)};
-  int s0 = 0, sd = 0;
+  int s0 = 0, sd = 0, o0 = 0, no = 0;
   if (active) {
     s0 = prow[p];
     sd = pdiag[p];
+    o0 = upd_ptr[p];
+    no = upd_ptr[p + 1] - o0;
     const int nb = prow[p + 1] - s0;
-    const double s = gamma * invV[ord[p]];
-    for (int b = 0; b < nb; b++) {
+    if (kPre > 0) {
+      TF pre[kPre > 0 ? kPre : 1][5];
+#pragma unroll
+      for (int o = 0; o < kPre; o++)
+        if (o < no) {
+          const TF* B = LU + 25 * (size_t)upd[o0 + o].y + 5 * a;
+#pragma unroll
+          for (int k = 0; k < 5; k++) pre[o][k] = B[k];
+        }
+#pragma unroll
+      for (int o = 0; o < kPre; o++)
+        if (o < no) {
+#pragma unroll
+          for (int k = 0; k < 5; k++) bsm[lrow][o][5 * a + k] = pre[o][k];
+        }
+    }
+    // P = I - (gamma / v) J in the factor's precision (FP32 arithmetic in the FP32 form)
+    const TF sc = from64<TF>(gamma * invV[ord[p]]);
+#pragma unroll
+    for (int b = 0; b < kMaxBlocksPerRow; b++) {
+      if (b >= nb) break;
       const TJ* src = J + 25 * (size_t)(s0 + b) + 5 * a;
       const bool dg = (s0 + b) == sd;
 #pragma unroll
       for (int k = 0; k < 5; k++)
-        sm[lrow][b][5 * a + k] = (TF)(((dg && k == a) ? 1.0 : 0.0) - s * (double)src[k]);
+        sm[lrow][b][5 * a + k] = ((dg && k == a) ? TF(1) : TF(0)) - sc * (TF)src[k];
     }
-    for (int o = upd_ptr[p]; o < upd_ptr[p + 1]; o++) {
-      const int3 op = upd[o];
+  }
+  __syncwarp();  // the five lanes of a row see each other's operand rows
+  if (active) {
+    for (int o = 0; o < no; o++) {
+      const int3 op = upd[o0 + o];
       TF A[5];
       TF* Ar = &sm[lrow][op.x - s0][5 * a];
 #pragma unroll
       for (int k = 0; k < 5; k++) A[k] = Ar[k];
-      const TF* B = LU + 25 * (size_t)op.y;
+      const TF* B = (o < kPre) ? &bsm[lrow][o < kPre ? o : 0][0] : LU + 25 * (size_t)op.y;
       TF* dst = &sm[lrow][(op.z < 0 ? op.x : op.z) - s0][5 * a];
 #pragma unroll
       for (int b = 0; b < 5; b++) {
@@ -308,15 +478,6 @@ __global__ void __launch_bounds__(kT) k_ilu_factor(
 #pragma unroll
     for (int k = 0; k < 5; k++) dst[k] = sm[lrow][b][5 * a + k];
   }
-}
-
-template <typename TF>
-__device__ __forceinline__ TF from64(double x) {
-  if constexpr (sizeof(TF) == 4) return d2f_trunc(x); else return (TF)x;
-}
-template <typename TF>
-__device__ __forceinline__ double to64(TF x) {
-  if constexpr (sizeof(TF) == 4) return f2d_bits(x); else return (double)x;
 }
 
 // r (FP64 SoA, internal order) -> rv (AoS, 8 per row, position order)
@@ -564,14 +725,34 @@ int fos_jac_setup(fos_ctx* c) {
   return 0;
 }
 
-template <typename T, typename TJ>
+template <typename TJ>
 static int jac_assemble_t(fos_ctx* c, const double* y) {
   TJ* J = reinterpret_cast<TJ*>(c->d_Jraw);
   TJ* Jb = reinterpret_cast<TJ*>(c->d_Jb);
-  fos_launch(c, k_jac_face<T, TJ>, nb(c->nF), kT, c->nFi, c->nF, c->nC,
-             (const int2*)c->d_faceLR, (const double2*)c->d_faceNA, (const double*)c->d_W, y,
-             (const int*)c->d_fslot, (const int*)c->d_bcT, (const double*)c->d_bcP, c->maxP,
-             c->gamm, c->r, J, Jb);
+  if constexpr (sizeof(TJ) == sizeof(float)) {
+    if (int rc = fos_prim_hl_launch(c, y)) return rc;
+    const int grid = (c->nC + 63) / 64;
+    if (c->ell_w == 4)
+      fos_launch(c, k_jac_cell32<4>, grid, 64, c->nC, c->nFi, (const int*)c->d_ipos,
+                 (const int*)c->d_prow, (const int*)c->d_cdiag, (const int*)c->d_ell,
+                 (const int2*)c->d_faceLR, (const float4*)c->d_faceNA32, (const int*)c->d_fslot,
+                 (const float*)c->d_Whl, y, (const int*)c->d_bcT, (const double*)c->d_bcP,
+                 c->maxP, c->gamm, c->r, J);
+    else
+      fos_launch(c, k_jac_cell32<6>, grid, 64, c->nC, c->nFi, (const int*)c->d_ipos,
+                 (const int*)c->d_prow, (const int*)c->d_cdiag, (const int*)c->d_ell,
+                 (const int2*)c->d_faceLR, (const float4*)c->d_faceNA32, (const int*)c->d_fslot,
+                 (const float*)c->d_Whl, y, (const int*)c->d_bcT, (const double*)c->d_bcP,
+                 c->maxP, c->gamm, c->r, J);
+    FOS_LAUNCH_CHECK();
+    return 0;
+  } else {
+    if (int rc = fos_prim_launch(c, y)) return rc;
+    fos_launch(c, k_jac_face<TJ>, nb(c->nF), kT, c->nFi, c->nF, c->nC,
+               (const int2*)c->d_faceLR, (const double2*)c->d_faceNA, (const double*)c->d_W, y,
+               (const int*)c->d_fslot, (const int*)c->d_bcT, (const double*)c->d_bcP, c->maxP,
+               c->gamm, c->r, J, Jb);
+  }
   fos_launch(c, k_jac_diag<TJ>, nb(c->nC), kT, c->nC, c->nFi, (const int*)c->d_crow,
              (const int*)c->d_cent, (const int*)c->d_fslot, (const int*)c->d_cdiag,
              (const TJ*)Jb, J);
@@ -580,11 +761,9 @@ static int jac_assemble_t(fos_ctx* c, const double* y) {
 }
 
 int fos_jac_assemble(fos_ctx* c, const double* y) {
-  int rc = fos_prim_launch(c, y);
-  if (rc) return rc;
   // the FP32 preconditioner is assembled and stored in FP32
-  rc = (c->flags & FOS_ILU_FP32) ? jac_assemble_t<float, float>(c, y)
-                                 : jac_assemble_t<double, double>(c, y);
+  const int rc = (c->flags & FOS_ILU_FP32) ? jac_assemble_t<float>(c, y)
+                                           : jac_assemble_t<double>(c, y);
   if (rc) return rc;
   c->has_jac = true;
   return 0;

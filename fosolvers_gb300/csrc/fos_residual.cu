@@ -11,8 +11,11 @@
 //   k_gather  per cell   deterministic CSR gather of -flow (cell is L) / +flow (cell
 //                         is R) in ascending face order, times 1/v; Jv epilogue
 //                         out = a v + b (f(y+sv) - fy)/s in FP64
-// The FP32-flux variant (FOS_FLUX_FP32) computes the same flow in FP32 from FP64 means
-// and jumps, in flux-difference form, and accumulates it in FP64 (see roe_split_mixed).
+// The FP32-flux variant (FOS_FLUX_FP32) computes the same flow in FP32, in flux-difference
+// form, from per-cell FP32 (hi, lo) primitive pairs (k_prim_hl), and fuses the interior
+// faces into the cell gather (k_cell32: each interior face evaluated by both of its cells,
+// bit-identically); boundary faces go through k_face32b (ghost state in FP64).  Sums are in
+// FP64 in both variants.
 #include <cmath>
 #include <mutex>
 #include <string>
@@ -167,17 +170,19 @@ __device__ __forceinline__ void load_ell(const int* __restrict__ ell, int c, int
   }
 }
 
+// out = acc / v (mode 0) or the Jv combination a v + (b / s)(acc / v - fy) (mode 1), in
+// FP64; non-finite results are flagged from the exponent bits (no FP64 compares)
 __device__ __forceinline__ void gather_epilogue(int nC, int c, const double acc[5], double iv,
                                                 int mode, const double* __restrict__ vv,
                                                 const double* __restrict__ fy,
                                                 const double* __restrict__ d_s, double a, double b,
                                                 double* __restrict__ out, int* __restrict__ flag) {
-  bool bad = false;
+  bool ok = true;
   if (mode == 0) {
 #pragma unroll
     for (int q = 0; q < 5; q++) {
       const double o = acc[q] * iv;
-      bad |= !isfinite(o);
+      ok &= finite_bits(o);
       out[(size_t)q * nC + c] = o;
     }
   } else {
@@ -185,12 +190,13 @@ __device__ __forceinline__ void gather_epilogue(int nC, int c, const double acc[
 #pragma unroll
     for (int q = 0; q < 5; q++) {
       const size_t k = (size_t)q * nC + c;
-      const double o = fma(bs, fma(acc[q], iv, -fy[k]), a * vv[k]);
-      bad |= !isfinite(o);
+      const double t = fma(acc[q], iv, -fy[k]);
+      const double o = a == 1.0 ? fma(bs, t, vv[k]) : a == 0.0 ? bs * t : fma(bs, t, a * vv[k]);
+      ok &= finite_bits(o);
       out[k] = o;
     }
   }
-  if (bad && flag) atomicOr(flag, 1);
+  if (!ok && flag) atomicOr(flag, 1);
 }
 
 template <int kW>
@@ -217,10 +223,12 @@ __global__ void __launch_bounds__(kThreads) k_gather(
 }
 
 // ------------------------------------------------------------------ FP32 flux
-// Per-cell primitives for the FP32 flux as FP32 (hi, lo) pairs: x = hi + lo to ~48 bits,
-// so a face jump (hR - hL) + (lR - lL) keeps FP32 relative accuracy of the jump itself
-// while the face kernel issues FP32 instructions only.  Layout: 16 floats (64 B) per cell
-// = (rho, u, v, w, H, p) hi, (rho, u, v, w, H, p) lo, sqrt(rho), 0, 0, 0.
+// Per-cell primitives for the FP32 flux as FP32 (hi, lo) pairs x = hi + lo (~46 bits), so
+// a face jump (hR - hL) + (lR - lL) keeps FP32 relative accuracy of the jump itself while
+// the face arithmetic issues FP32 instructions only.  The primitives are formed in
+// double-float arithmetic (df_*: FP32 pipe); only the Jv perturbation y + s v is FP64.
+// Layout: 16 floats (64 B) per cell = (rho, u, v, w, H, p) hi, (rho, u, v, w, H, p) lo,
+// sqrt(rho), 0, 0, 0.
 __global__ void __launch_bounds__(kThreads) k_prim_hl(int nC, const double* __restrict__ y,
                                                       const double* __restrict__ v,
                                                       const double* __restrict__ d_s, double gm1,
@@ -235,22 +243,18 @@ __global__ void __launch_bounds__(kThreads) k_prim_hl(int nC, const double* __re
 #pragma unroll
     for (int q = 0; q < 5; q++) U[q] = fma(s, v[(size_t)q * nC + c], U[q]);
   }
-  const double inv = rcp64(U[0]);
-  const double u = U[1] * inv, vv = U[2] * inv, w = U[3] * inv;
-  const double p = gm1 * (U[4] - 0.5 * (U[1] * u + U[2] * vv + U[3] * w));
-  const double H = (U[4] + p) * inv;
-  float h[6], l[6];
-  split_hl_bits(U[0], h[0], l[0]);
-  split_hl_bits(u, h[1], l[1]);
-  split_hl_bits(vv, h[2], l[2]);
-  split_hl_bits(w, h[3], l[3]);
-  split_hl_bits(H, h[4], l[4]);
-  split_hl_bits(p, h[5], l[5]);
+  const df2 r = df_from_double(U[0]), mx = df_from_double(U[1]), my = df_from_double(U[2]),
+            mz = df_from_double(U[3]), E = df_from_double(U[4]), g = df_from_double(gm1);
+  const df2 inv = df_rcp(r);
+  const df2 u = df_mul(mx, inv), vv = df_mul(my, inv), w = df_mul(mz, inv);
+  const df2 ke = df_add(df_add(df_mul(mx, u), df_mul(my, vv)), df_mul(mz, w));  // rho |u|^2
+  const df2 p = df_mul(g, df_add(E, df_scale(ke, -0.5f)));
+  const df2 H = df_mul(df_add(E, p), inv);
   float4* w4 = reinterpret_cast<float4*>(W + 16 * (size_t)c);
-  w4[0] = make_float4(h[0], h[1], h[2], h[3]);
-  w4[1] = make_float4(h[4], h[5], l[0], l[1]);
-  w4[2] = make_float4(l[2], l[3], l[4], l[5]);
-  w4[3] = make_float4(sqrtf(h[0] + l[0]), 0.0f, 0.0f, 0.0f);
+  w4[0] = make_float4(r.h, u.h, vv.h, w.h);
+  w4[1] = make_float4(H.h, p.h, r.l, u.l);
+  w4[2] = make_float4(vv.l, w.l, H.l, p.l);
+  w4[3] = make_float4(sqrtf(r.h + r.l), 0.0f, 0.0f, 0.0f);
 }
 
 struct PHL {
@@ -312,30 +316,6 @@ __device__ __forceinline__ void store_f32(float* __restrict__ F, int f, const fl
   F4[2] = make_float4(dF[4], dw[4], 0.0f, 0.0f);
 }
 
-// interior faces [0, nFi): FP32 instructions only
-__global__ void __launch_bounds__(kThreads) k_face32i(int nFi, const int2* __restrict__ faceLR,
-                                                      const float4* __restrict__ faceNA,
-                                                      const float* __restrict__ W, float gm1,
-                                                      float* __restrict__ F) {
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
-  if (f >= nFi) return;
-  const int2 lr = __ldg(faceLR + f);
-  const float4 na = __ldg(faceNA + f);
-  PHL L, R;
-  load_hl(W, lr.x, L);
-  load_hl(W, lr.y, R);
-  float m[6], d[6];
-#pragma unroll
-  for (int k = 0; k < 6; k++) {
-    m[k] = 0.5f * (L.h[k] + R.h[k]) + 0.5f * (L.l[k] + R.l[k]);
-    d[k] = (R.h[k] - L.h[k]) + (R.l[k] - L.l[k]);
-  }
-  float dF[5], dw[5];
-  roe_split_mj(m[0], d[0], m[1], d[1], m[2], d[2], m[3], d[3], m[4], d[4], d[5], L.s, R.s, na.x,
-               na.y, na.z, na.w, gm1, dF, dw);
-  store_f32(F, f, dF, dw);
-}
-
 // boundary faces [nFi, nF): ghost state and means/jumps in FP64 (1% of the faces)
 __global__ void __launch_bounds__(kThreads) k_face32b(
     int nFi, int nF, int nC, const int2* __restrict__ faceLR, const float4* __restrict__ faceNA,
@@ -370,29 +350,60 @@ __global__ void __launch_bounds__(kThreads) k_face32b(
   store_f32(F, f, dF, dw);
 }
 
-// FP64 accumulation of the FP32 face terms: cell L gets -(dF - dw), cell R gets -(dF + dw)
+// Fused interior flux + cell gather for the FP32 flux (one pass, no face-flow array for
+// interior faces).  Thread per cell: each interior face of the cell is evaluated in the
+// face's own orientation (L = faceLR.x, R = faceLR.y) from the FP32 (hi, lo) means and
+// jumps, FP32 instructions only, so
+// the two cells of a face compute bit-identical (dF, dw) and the scheme stays exactly
+// conservative; the cell then takes -(dF - dw) (cell is L) or -(dF + dw) (cell is R) in
+// FP64, in ascending ELL order.  Boundary faces read the flows k_face32b wrote.  Each face
+// is evaluated twice -- cheap FP32 arithmetic in exchange for the 2 x 48 B per face a
+// face-flow array costs in HBM traffic.
 template <int kW>
-__global__ void __launch_bounds__(kThreads) k_gather32(
-    int nC, const int* __restrict__ ell, const float* __restrict__ F,
-    const double* __restrict__ invV, int mode, const double* __restrict__ vv,
-    const double* __restrict__ fy, const double* __restrict__ d_s, double a, double b,
-    double* __restrict__ out, int* __restrict__ flag) {
+__global__ void __launch_bounds__(kThreads) k_cell32(
+    int nC, int nFi, const int* __restrict__ ell, const int2* __restrict__ faceLR,
+    const float4* __restrict__ faceNA, const float* __restrict__ W, float gm1,
+    const float* __restrict__ Fb, const double* __restrict__ invV, int mode,
+    const double* __restrict__ vv, const double* __restrict__ fy, const double* __restrict__ d_s,
+    double a, double b, double* __restrict__ out, int* __restrict__ flag) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nC) return;
   int e[kW];
   load_ell<kW>(ell, c, e);
+  PHL P;
+  load_hl(W, c, P);
   double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
 #pragma unroll
   for (int k = 0; k < kW; k++) {
     if (e[k] < 0) continue;
-    const float sw = (e[k] & 1) ? 1.0f : -1.0f;  // R: -(dF + dw), L: -(dF - dw)
-    const float4* F4 = reinterpret_cast<const float4*>(F + 12 * (size_t)(e[k] >> 1));
-    const float4 a0 = __ldg(F4), a1 = __ldg(F4 + 1), a2 = __ldg(F4 + 2);
-    acc[0] -= f2d_bits(fmaf(sw, a0.y, a0.x));
-    acc[1] -= f2d_bits(fmaf(sw, a0.w, a0.z));
-    acc[2] -= f2d_bits(fmaf(sw, a1.y, a1.x));
-    acc[3] -= f2d_bits(fmaf(sw, a1.w, a1.z));
-    acc[4] -= f2d_bits(fmaf(sw, a2.y, a2.x));
+    const int f = e[k] >> 1;
+    const bool isR = e[k] & 1;
+    const float sw = isR ? 1.0f : -1.0f;  // R: -(dF + dw), L: -(dF - dw)
+    float dF[5], dw[5];
+    if (f < nFi) {
+      const int2 lr = __ldg(faceLR + f);
+      const float4 na = __ldg(faceNA + f);
+      PHL Q;
+      load_hl(W, isR ? lr.x : lr.y, Q);
+      const PHL& L = isR ? Q : P;
+      const PHL& R = isR ? P : Q;
+      float m[6], d[6];
+#pragma unroll
+      for (int j = 0; j < 6; j++) {
+        m[j] = 0.5f * (L.h[j] + R.h[j]) + 0.5f * (L.l[j] + R.l[j]);
+        d[j] = (R.h[j] - L.h[j]) + (R.l[j] - L.l[j]);
+      }
+      roe_split_mj(m[0], d[0], m[1], d[1], m[2], d[2], m[3], d[3], m[4], d[4], d[5], L.s, R.s,
+                   na.x, na.y, na.z, na.w, gm1, dF, dw);
+    } else {
+      const float4* F4 = reinterpret_cast<const float4*>(Fb + 12 * (size_t)f);
+      const float4 a0 = __ldg(F4), a1 = __ldg(F4 + 1), a2 = __ldg(F4 + 2);
+      dF[0] = a0.x; dw[0] = a0.y; dF[1] = a0.z; dw[1] = a0.w;
+      dF[2] = a1.x; dw[2] = a1.y; dF[3] = a1.z; dw[3] = a1.w;
+      dF[4] = a2.x; dw[4] = a2.y;
+    }
+#pragma unroll
+    for (int q = 0; q < 5; q++) acc[q] -= f2d_bits(fmaf(sw, dw[q], dF[q]));
   }
   gather_epilogue(nC, c, acc, __ldg(invV + c), mode, vv, fy, d_s, a, b, out, flag);
 }
@@ -459,22 +470,21 @@ int fos_residual_launch(fos_ctx* c, const double* y, const double* v, const doub
   const double gm1 = c->gamm - 1.0;
   if (c->flags & FOS_FLUX_FP32) {
     fos_launch(c, k_prim_hl, nblk(c->nC), kThreads, c->nC, y, v, d_s, gm1, c->d_Whl);
-    fos_launch(c, k_face32i, nblk(c->nFi), kThreads, c->nFi, (const int2*)c->d_faceLR,
-               (const float4*)c->d_faceNA32, (const float*)c->d_Whl, (float)gm1,
-               reinterpret_cast<float*>(c->d_F));
     if (c->nFb)
       fos_launch(c, k_face32b, nblk(c->nFb), kThreads, c->nFi, c->nF, c->nC,
                  (const int2*)c->d_faceLR, (const float4*)c->d_faceNA32, y, v, d_s,
                  (const int*)c->d_bcT, (const double*)c->d_bcP, c->maxP, c->gamm, c->r,
                  reinterpret_cast<float*>(c->d_F));
     if (c->ell_w == 4)
-      fos_launch(c, k_gather32<4>, nblk(c->nC), kThreads, c->nC, (const int*)c->d_ell,
-                 reinterpret_cast<const float*>(c->d_F), (const double*)c->d_invV, mode, v, fy,
-                 d_s, a, b, out, c->d_flag);
+      fos_launch(c, k_cell32<4>, nblk(c->nC), kThreads, c->nC, c->nFi, (const int*)c->d_ell,
+                 (const int2*)c->d_faceLR, (const float4*)c->d_faceNA32, (const float*)c->d_Whl,
+                 (float)gm1, reinterpret_cast<const float*>(c->d_F), (const double*)c->d_invV,
+                 mode, v, fy, d_s, a, b, out, c->d_flag);
     else
-      fos_launch(c, k_gather32<6>, nblk(c->nC), kThreads, c->nC, (const int*)c->d_ell,
-                 reinterpret_cast<const float*>(c->d_F), (const double*)c->d_invV, mode, v, fy,
-                 d_s, a, b, out, c->d_flag);
+      fos_launch(c, k_cell32<6>, nblk(c->nC), kThreads, c->nC, c->nFi, (const int*)c->d_ell,
+                 (const int2*)c->d_faceLR, (const float4*)c->d_faceNA32, (const float*)c->d_Whl,
+                 (float)gm1, reinterpret_cast<const float*>(c->d_F), (const double*)c->d_invV,
+                 mode, v, fy, d_s, a, b, out, c->d_flag);
   } else {
     fos_launch(c, k_prim64, nblk(c->nC), kThreads, c->nC, y, v, d_s, gm1, c->d_W);
     fos_launch(c, k_face64, nblk(c->nF), kThreads, c->nFi, c->nF, c->nC,
@@ -490,6 +500,13 @@ int fos_residual_launch(fos_ctx* c, const double* y, const double* v, const doub
                  (const double*)c->d_F, (const double*)c->d_invV, mode, v, fy, d_s, a, b, out,
                  c->d_flag);
   }
+  FOS_LAUNCH_CHECK();
+  return 0;
+}
+
+int fos_prim_hl_launch(fos_ctx* c, const double* y) {
+  fos_launch(c, k_prim_hl, nblk(c->nC), kThreads, c->nC, y, nullptr, nullptr, c->gamm - 1.0,
+             c->d_Whl);
   FOS_LAUNCH_CHECK();
   return 0;
 }
@@ -590,18 +607,20 @@ extern "C" int fos_euler_rhs_dev_static(const fos_ctx* c, double t, const double
     float* Whl = reinterpret_cast<float*>(bytes);
     float* F = reinterpret_cast<float*>(bytes + kStaticCellBytes);
     k_prim_hl<<<nblk(c->nC), kThreads, 0, s>>>(c->nC, y, nullptr, nullptr, gm1, Whl);
-    k_face32i<<<nblk(c->nFi), kThreads, 0, s>>>(c->nFi, c->d_faceLR, c->d_faceNA32, Whl,
-                                                (float)gm1, F);
     if (c->nFb)
       k_face32b<<<nblk(c->nFb), kThreads, 0, s>>>(c->nFi, c->nF, c->nC, c->d_faceLR,
                                                   c->d_faceNA32, y, nullptr, nullptr, c->d_bcT,
                                                   c->d_bcP, c->maxP, c->gamm, c->r, F);
     if (c->ell_w == 4)
-      k_gather32<4><<<nblk(c->nC), kThreads, 0, s>>>(c->nC, c->d_ell, F, c->d_invV, 0, nullptr,
-                                                     nullptr, nullptr, 0.0, 0.0, ydot, nullptr);
+      k_cell32<4><<<nblk(c->nC), kThreads, 0, s>>>(c->nC, c->nFi, c->d_ell, c->d_faceLR,
+                                                   c->d_faceNA32, Whl, (float)gm1, F, c->d_invV,
+                                                   0, nullptr, nullptr, nullptr, 0.0, 0.0, ydot,
+                                                   nullptr);
     else
-      k_gather32<6><<<nblk(c->nC), kThreads, 0, s>>>(c->nC, c->d_ell, F, c->d_invV, 0, nullptr,
-                                                     nullptr, nullptr, 0.0, 0.0, ydot, nullptr);
+      k_cell32<6><<<nblk(c->nC), kThreads, 0, s>>>(c->nC, c->nFi, c->d_ell, c->d_faceLR,
+                                                   c->d_faceNA32, Whl, (float)gm1, F, c->d_invV,
+                                                   0, nullptr, nullptr, nullptr, 0.0, 0.0, ydot,
+                                                   nullptr);
   } else {
     double* W = reinterpret_cast<double*>(bytes);
     double* F = reinterpret_cast<double*>(bytes + kStaticCellBytes);

@@ -185,7 +185,9 @@ typedef struct {
   double jv_eps;      /* finite-difference increment scale (sqrt of machine epsilon) */
   int precond;        /* 0 = none, 1 = block ILU(0), 2 = learned network in flexible GMRES,
                          falling back to ILU(0) when it stagnates or needs more iterations
-                         than the last ILU(0)-preconditioned solve; 3 = learned network
+                         than the last ILU(0)-preconditioned solve, after which the next
+                         1, 2, 4, ... 64 solves (doubling per consecutive fallback, reset
+                         when the network converges a solve) use ILU(0) alone; 3 = learned network
                          without fallback (evaluation); 4 = ILU(0) followed by the learned
                          correction, z = u + N(y; u) with u = ILU(0) r, with the fallback
                          of 2; 5 = the same without fallback */
