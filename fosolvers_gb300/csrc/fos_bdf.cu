@@ -174,6 +174,7 @@ struct fos_bdf_work {
   int maxl = 0;
   bool has_hist = false;  // yn holds the last accepted state, ym the one before
   int ilu_ref_its = -1;   // learned mode: iterations of the last ILU(0)-preconditioned solve
+  double ilu_ref_rate = 1.0;  // learned mode: its mean residual reduction per iteration
   int learned_backoff = 0;  // learned mode: solves skipped after the last fallback
   int learned_skip = 0;     // learned mode: solves still to run with ILU(0) alone
   double t_last = 0.0;
@@ -247,6 +248,12 @@ struct Driver {
   double t_step = 0.0, gamma_step = 0.0;
   const double* y_step = nullptr;
   int ilu_ref_its = -1;  // Krylov iterations of the last ILU(0)-preconditioned solve
+  double ilu_ref_rate = 1.0;  // and its mean residual reduction per iteration
+  // an ILU(0)-preconditioned solve reached residual res after its iterations
+  void set_ilu_ref(int its, double res, double bnorm) {
+    ilu_ref_its = its;
+    ilu_ref_rate = (its > 0 && bnorm > 0.0 && res > 0.0) ? std::pow(res / bnorm, 1.0 / its) : 0.0;
+  }
 
   int reduce(int nv, double* out) {  // k_final over wk.part into device out
     fos_launch(c, k_final, nv, 256, nv, kRedBlocks, wk.part, out);
@@ -297,6 +304,7 @@ struct Driver {
       FOS_CUDA(cudaMemcpyAsync(z, r, sizeof(double) * wk.N, cudaMemcpyDeviceToDevice, c->stream));
       return 0;
     }
+    if (pc >= 2) st.n_learned++;
     if (pc == 2 || pc == 3) return fos_gnn_precond(c, y, r, gamma_cur, z);
     if (pc >= 4) {  // z = u + N(y; u), u = ILU(0) r
       if (int rc = fos_ilu_apply(c, r, wk.u)) return rc;
@@ -422,7 +430,11 @@ struct Driver {
         g[j] = cs[j] * g[j];
         kend = j + 1;
         if (std::fabs(g[j + 1]) <= o.lin_rtol * bnorm || hn == 0.0) { conv = true; break; }
-        if ((pc == 2 || pc == 4) && (*its >= ilu_ref_its || std::fabs(g[j + 1]) > 0.9 * std::fabs(g[j]))) {
+        // learned modes fall back when they stagnate, reach the ILU(0) iteration count, or
+        // fall behind the ILU(0) solve's mean reduction per iteration
+        if ((pc == 2 || pc == 4) &&
+            (*its >= ilu_ref_its || std::fabs(g[j + 1]) > 0.9 * std::fabs(g[j]) ||
+             std::fabs(g[j + 1]) > beta * std::pow(ilu_ref_rate, j + 1))) {
           fallback = true;
           break;
         }
@@ -438,7 +450,7 @@ struct Driver {
                  (const double*)(wk.sc + 4 * kMaxVec), wk.d);
       FOS_LAUNCH_CHECK();
       if (conv) {
-        if (pure_ilu) ilu_ref_its = *its;
+        if (pure_ilu) set_ilu_ref(*its, std::fabs(g[kend]), bnorm);
         if (with_fallback && pc != 1) wk.learned_backoff = 0;  // the network won this solve
         return 0;
       }
@@ -462,7 +474,7 @@ struct Driver {
       if ((rc = fetch(c->d_scal + 8, hbuf.data(), 1))) return rc;
       beta = std::sqrt(hbuf[0]);
       if (beta <= o.lin_rtol * bnorm) {
-        if (pure_ilu) ilu_ref_its = *its;
+        if (pure_ilu) set_ilu_ref(*its, beta, bnorm);
         return 0;
       }
       rvec = wk.w;
@@ -496,6 +508,7 @@ extern "C" int fos_bdf_run(fos_ctx* c, double t0, double* y, const fos_bdf_opts*
                                             : std::sqrt(DBL_EPSILON);
   Driver dr{c, wk, *opts, st, eps};
   dr.ilu_ref_its = wk.ilu_ref_its;
+  dr.ilu_ref_rate = wk.ilu_ref_rate;
   double t = t0;
   double hb[4];
   FOS_CUDA(cudaMemcpyAsync(wk.yn, y, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
@@ -559,6 +572,7 @@ extern "C" int fos_bdf_run(fos_ctx* c, double t0, double* y, const fos_bdf_opts*
   }
   if (status) wk.has_hist = false;
   wk.ilu_ref_its = dr.ilu_ref_its;
+  wk.ilu_ref_rate = dr.ilu_ref_rate;
   st.t = t;
   FOS_CUDA(cudaStreamSynchronize(c->stream));
   return status;
@@ -606,6 +620,7 @@ extern "C" int fos_linear_solve_dev(fos_ctx* c, double t, const double* y, const
                                             : std::sqrt(DBL_EPSILON);
   Driver dr{c, wk, *opts, st, eps};
   dr.ilu_ref_its = wk.ilu_ref_its;
+  dr.ilu_ref_rate = wk.ilu_ref_rate;
   dr.t_step = t;
   dr.gamma_step = gamma;
   dr.y_step = y;
@@ -619,6 +634,7 @@ extern "C" int fos_linear_solve_dev(fos_ctx* c, double t, const double* y, const
   int rc = dr.gmres(y, fy, gamma, std::sqrt(h2[0]), std::sqrt(h2[1]), &its);
   st.n_lin_iters = its;
   wk.ilu_ref_its = dr.ilu_ref_its;
+  wk.ilu_ref_rate = dr.ilu_ref_rate;
   if (rc < 0) return rc;
   FOS_CUDA(cudaMemcpyAsync(x, wk.d, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
   FOS_CUDA(cudaStreamSynchronize(c->stream));

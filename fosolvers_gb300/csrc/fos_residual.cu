@@ -372,10 +372,12 @@ __global__ void __launch_bounds__(kThreads) k_cell32(
   load_ell<kW>(ell, c, e);
   PHL P;
   load_hl(W, c, P);
-  double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  // FP64 accumulation in ELL order; the first face initialises the sums (every cell has
+  // at least one face, and ELL rows are padded at the end)
+  double acc[5];
 #pragma unroll
   for (int k = 0; k < kW; k++) {
-    if (e[k] < 0) continue;
+    if (k > 0 && e[k] < 0) continue;
     const int f = e[k] >> 1;
     const bool isR = e[k] & 1;
     const float sw = isR ? 1.0f : -1.0f;  // R: -(dF + dw), L: -(dF - dw)
@@ -403,7 +405,10 @@ __global__ void __launch_bounds__(kThreads) k_cell32(
       dF[4] = a2.x; dw[4] = a2.y;
     }
 #pragma unroll
-    for (int q = 0; q < 5; q++) acc[q] -= f2d_bits(fmaf(sw, dw[q], dF[q]));
+    for (int q = 0; q < 5; q++) {
+      const float term = fmaf(sw, dw[q], dF[q]);
+      acc[q] = k == 0 ? f2d_bits(-term) : acc[q] - f2d_bits(term);
+    }
   }
   gather_epilogue(nC, c, acc, __ldg(invV + c), mode, vv, fy, d_s, a, b, out, flag);
 }

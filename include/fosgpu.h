@@ -184,8 +184,9 @@ typedef struct {
   double lin_rtol;    /* Krylov: ||r|| <= lin_rtol ||b|| */
   double jv_eps;      /* finite-difference increment scale (sqrt of machine epsilon) */
   int precond;        /* 0 = none, 1 = block ILU(0), 2 = learned network in flexible GMRES,
-                         falling back to ILU(0) when it stagnates or needs more iterations
-                         than the last ILU(0)-preconditioned solve, after which the next
+                         falling back to ILU(0) when it stagnates, falls behind the mean
+                         residual reduction per iteration of the last ILU(0)-preconditioned
+                         solve, or needs more iterations than that solve, after which the next
                          1, 2, 4, ... 64 solves (doubling per consecutive fallback, reset
                          when the network converges a solve) use ILU(0) alone; 3 = learned network
                          without fallback (evaluation); 4 = ILU(0) followed by the learned
@@ -199,6 +200,7 @@ typedef struct {
   long n_rhs, n_jv, n_psol, n_pset, n_newton, n_lin_iters, n_steps, fails, n_fallback;
   double last_gnorm;
   double t;
+  long n_learned;     /* applications of the learned preconditioner (of n_psol) */
 } fos_bdf_stats;
 
 void fos_bdf_defaults(fos_bdf_opts* o);
