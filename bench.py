@@ -61,8 +61,10 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="sine96")
     ap.add_argument("--scale", type=int, default=None, help="hexes along x (small cases)")
-    ap.add_argument("--mode", choices=["fp64", "fp32"], default="fp32",
-                    help="fp64: FP64 flux + FP64 ILU(0); fp32: FP32 flux + FP32 ILU(0) apply")
+    ap.add_argument("--mode", choices=["fp64", "fp32", "fp32ilu"], default="fp32",
+                    help="fp64: FP64 flux + FP64 ILU(0); fp32: FP32 flux + FP32 ILU(0); "
+                         "fp32ilu: FP64 flux + FP32 ILU(0) (shocked flows, where the FP32 flux's "
+                         "rounding floor reaches the Newton tolerance)")
     ap.add_argument("--precond", choices=["ilu", "none", "learned"], default="learned",
                     help="learned: the trained network in FGMRES with ILU(0) fallback")
     ap.add_argument("--weights", default=None, help="network weights (.npy) for --precond learned")
@@ -270,7 +272,7 @@ PRECOND = {"none": 0, "ilu": 1, "learned": 2}
 
 def make_ctx(grid, ibc, wl, mode, ilu_order, stream):
     from fosolvers_gb300.euler import FLUX_FP32, ILU_COLOR, ILU_FP32, FOEuler
-    flags = (FLUX_FP32 | ILU_FP32) if mode == "fp32" else 0
+    flags = {"fp32": FLUX_FP32 | ILU_FP32, "fp32ilu": ILU_FP32, "fp64": 0}[mode]
     if ilu_order == "color":
         flags |= ILU_COLOR
     return FOEuler(grid, ibc, wl.bc_type, wl.bc_param, wl.gamm, wl.r, flags=flags, stream=stream)
@@ -396,7 +398,7 @@ def main():
         gamma = wl.dt * (2.0 / 3.0 if wl.order == 2 else 1.0)
         info = ctx.info()
         nnzb = info["nnzb"]
-        fb = 4 if args.mode == "fp32" else 8
+        fb = 8 if args.mode == "fp64" else 4
 
         def timeit(fn, reps):
             fn()
@@ -445,7 +447,7 @@ def main():
 
     # the plain FP64 ILU(0)-GMRES path on the same mesh and state: the target's denominator
     vs64 = None
-    if args.mode == "fp32" and not args.no_compare:
+    if args.mode != "fp64" and not args.no_compare:
         ctx64 = make_ctx(grid, ibc, wl, "fp64", args.ilu_order, stream)
         y064 = torch.empty_like(y0_ref)
         ctx64.to_internal(y0_ref, y064)
@@ -497,7 +499,8 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if args.mode == "fp64" else "f32 flux/ILU, f64 Newton+Krylov",
+            "dtype": {"fp64": "f64", "fp32": "f32 flux/ILU, f64 Newton+Krylov",
+                      "fp32ilu": "f64 flux, f32 ILU, f64 Newton+Krylov"}[args.mode],
             "data": "synthetic (seeded mesh and state)",
             "config": {"workload": workload_desc(args.workload) if args.scale is None else
                        f"{args.workload} at scale {args.scale}",

@@ -1,0 +1,54 @@
+"""A foeuler case directory end to end on the GPU: Gmsh mesh, condition table, initial
+condition, run control and gas files in; fixed BDF2 steps with GMRES(30) + ILU(0) in FP64;
+rst_<k>.vtk files out.  The final state must match the oracle's BDF run of the same case
+within 1e-10 (per conserved variable, relative to its largest value), and the written files
+must carry that state."""
+import numpy as np
+import pytest
+
+from fosolvers_gb300 import mesh as M
+from fosolvers_gb300.case import primitives, run_case, workload_from_case
+from fosolvers_gb300.meshio import read_vtk
+from helpers import Case, rel_err
+from oracle import pyoracle as O
+from test_meshio import _write_case
+
+pytestmark = pytest.mark.gpu
+
+
+def test_case_directory_matches_oracle_and_writes_results(cuda, tmp_path):
+    m = M.box_mesh(10, 6, 6, jitter=0.1, seed=4, extent=(1.0, 0.6, 0.6))
+    dt = 2e-5  # CFL ~ 0.07 on 347 m/s at h = 0.1
+    # subsonic duct-like set-up in SI units: total-pressure inflow at x-min, static-pressure
+    # outflow at x-max, walls elsewhere
+    _write_case(tmp_path, m, [(M.GID_XMIN, 11, [1.05e5, 300.0, 1.0, 0.0, 0.0]),
+                              (M.GID_XMAX, 20, [0.95e5])],
+                ic=(1.0e5, 300.0, 0.0, 0.0, 0.0), sim=(6 * dt, 3 * dt))
+    out = tmp_path / "out"
+    res = run_case(tmp_path, out, dt=dt, order=2, log=lambda s: None)
+    assert res["steps"] == 6 and res["outputs"] == 2
+
+    wl = workload_from_case(tmp_path, dt=dt, order=2, nsteps=6)
+    c = Case(wl)
+    c.match_ilu_order()
+    rhs, pset, psol = c.oracle.callbacks()
+    y_ref = c.y0.copy()
+    rc, st = O.bdf_run(c.N, rhs, pset, psol, c.oracle.h, y_ref,
+                       O.bdf_defaults(order=2, dt=dt, nsteps=6, use_prec=1))
+    assert rc == 0, st
+    err = rel_err(res["y"], y_ref)
+    print("case parity", err)
+    assert err <= 1e-10
+    # the flow moved: inflow total pressure above the initial static pressure
+    assert np.abs(res["y"][c.nC:2 * c.nC]).max() > 0.0
+
+    nC = c.nC
+    for k in range(3):
+        assert (out / f"rst_{k}.vtk").exists()
+    mesh_out, data = read_vtk(out / "rst_2.vtk")
+    assert mesh_out.nE == wl.mesh.nE
+    rho, u, p, T = primitives(res["y"], nC, wl.r, wl.gamm)
+    np.testing.assert_array_equal(data["cell"]["density"][:nC], rho)
+    np.testing.assert_array_equal(data["cell"]["velocity"][:nC], u)
+    np.testing.assert_array_equal(data["cell"]["pressure"][:nC], p)
+    np.testing.assert_array_equal(data["cell"]["temperature"][:nC], T)
