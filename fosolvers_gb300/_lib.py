@@ -37,6 +37,23 @@ class BdfStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class AdaptOpts(C.Structure):
+    _fields_ = [("rtol", C.c_double), ("atol", C.c_double), ("h0", C.c_double),
+                ("hmin", C.c_double), ("hmax", C.c_double), ("qmax", C.c_int),
+                ("max_steps", C.c_int)]
+
+
+class AdaptStats(C.Structure):
+    _fields_ = [("n_accepted", C.c_long), ("n_err_fails", C.c_long),
+                ("n_newton_fails", C.c_long), ("h_last", C.c_double), ("t", C.c_double),
+                ("q_last", C.c_int), ("steps_at_order", C.c_long * 6)]
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "steps_at_order"}
+        d["steps_at_order"] = list(self.steps_at_order)
+        return d
+
+
 # name -> (restype, argtypes)
 _SIGS = {
     "fos_grid_build": (C.c_int, [C.POINTER(_vp), C.c_int, _dp, C.c_int, C.c_int, _ip, _ip, _ip, _ip]),
@@ -77,6 +94,10 @@ _SIGS = {
     "fos_bdf_defaults": (None, [C.POINTER(BdfOpts)]),
     "fos_bdf_run": (C.c_int, [_vp, C.c_double, _vp, C.POINTER(BdfOpts), C.POINTER(BdfStats)]),
     "fos_bdf_run_host": (C.c_int, [_vp, C.c_double, _dp, C.POINTER(BdfOpts), C.POINTER(BdfStats)]),
+    "fos_bdf_adapt_defaults": (None, [C.POINTER(AdaptOpts)]),
+    "fos_bdf_adaptive": (C.c_int, [_vp, C.c_double, C.c_double, _vp, C.POINTER(BdfOpts),
+                                   C.POINTER(AdaptOpts), C.POINTER(BdfStats),
+                                   C.POINTER(AdaptStats)]),
     "fos_linear_solve_dev": (C.c_int, [_vp, C.c_double, _vp, _vp, C.c_double, _vp, _vp,
                                        C.POINTER(BdfOpts), C.POINTER(BdfStats)]),
 }

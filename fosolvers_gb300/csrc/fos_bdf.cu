@@ -165,6 +165,31 @@ __global__ void __launch_bounds__(kT) k_newton_res(long n, const double* __restr
   block_reduce_store<2>(acc, 2, part);
 }
 
+// out = sum_l c[l] p[l] (up to 8 vectors, summed in order l = 0, 1, ...)
+struct Comb8 {
+  const double* p[8];
+  double c[8];
+  int nv;
+};
+__global__ void k_lincomb(long n, Comb8 cb, double* __restrict__ out) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0.0;
+  for (int l = 0; l < cb.nv; l++) s += cb.c[l] * cb.p[l][i];
+  out[i] = s;
+}
+// part <- sum of (a_i / (rtol |w_i| + atol))^2 (weighted RMS norm, before the mean)
+__global__ void __launch_bounds__(kT) k_wrms_part(long n, const double* __restrict__ a,
+                                                  const double* __restrict__ w, double rtol,
+                                                  double atol, double* __restrict__ part) {
+  double acc[1] = {0.0};
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const double e = a[i] / (rtol * fabs(w[i]) + atol);
+    acc[0] += e * e;
+  }
+  block_reduce_store<1>(acc, 1, part);
+}
+
 inline int nb(long n) { return (int)((n + kT - 1) / kT); }
 
 }  // namespace
@@ -181,8 +206,14 @@ struct fos_bdf_work {
   double *V = nullptr, *Z = nullptr, *w = nullptr, *yn = nullptr, *ym = nullptr,
          *hist = nullptr, *f = nullptr, *b = nullptr, *d = nullptr, *part = nullptr,
          *sc = nullptr, *yh = nullptr, *u = nullptr;
+  // adaptive driver only (allocated on first use): solution history, predictor, error
+  // vectors of this and the previous step, scratch
+  double* ay[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  double *ypred = nullptr, *E = nullptr, *Eprev = nullptr, *atmp = nullptr;
   ~fos_bdf_work() {
-    for (double* p : {V, Z, w, yn, ym, hist, f, b, d, part, sc, yh, u})
+    for (double* p : {V, Z, w, yn, ym, hist, f, b, d, part, sc, yh, u, ypred, E, Eprev, atmp})
+      if (p) cudaFree(p);
+    for (double* p : ay)
       if (p) cudaFree(p);
   }
 };
@@ -336,6 +367,53 @@ struct Driver {
 
   long reorth = 0;
   bool last_reorth = false;  // the previous Arnoldi step needed the second Gram--Schmidt pass
+
+  // Newton iteration for G(y) = y - gamma f(y) - hist = 0 at time tn from the initial
+  // iterate y_0 in y, until ||G||_2 <= newton_rtol ||y_0||_2 + newton_atol sqrt(N); the
+  // preconditioner is set up (lazily) once for the solve.  Returns 0 converged, 1 not
+  // converged in max_newton, 2 non-finite residual, 3 zero pivot in ILU(0), < 0 error.
+  int newton(double* y, double gamma, const double* hist, double tn) {
+    const long N = wk.N;
+    double hb[2], gtol = 0.0;
+    for (int k = 0; k <= o.max_newton; k++) {
+      FOS_CUDA(cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream));
+      int rc = fos_residual_launch(c, y, nullptr, nullptr, nullptr, wk.f, 0.0, 0.0, 0);
+      if (rc) return rc;
+      st.n_rhs++;
+      fos_launch(c, k_newton_res, kRedBlocks, kT, N, (const double*)y, (const double*)wk.f,
+                 hist, gamma, wk.b, wk.part);
+      if ((rc = reduce(2, wk.sc))) return rc;
+      FOS_CUDA(cudaMemcpyAsync(hb, wk.sc, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+      FOS_CUDA(cudaMemcpyAsync(c->h_scal, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+      FOS_CUDA(cudaStreamSynchronize(c->stream));
+      if (*(int*)c->h_scal) return 2;  // non-finite residual
+      // the first pass also gives ||y_0||
+      if (k == 0) gtol = o.newton_rtol * std::sqrt(hb[1]) + o.newton_atol * std::sqrt((double)N);
+      const double gn = std::sqrt(hb[0]);
+      st.last_gnorm = gn / gtol;
+      if (gn <= gtol) return 0;
+      if (k == o.max_newton) break;
+      if (k == 0) {
+        pset_done = false;
+        t_step = tn;
+        gamma_step = gamma;
+        y_step = y;
+      }
+      // ||G|| for the linear tolerance: ||b||^2 via the norm kernel
+      if ((rc = fos_norm2_dev(c, wk.b, N, c->d_scal + 16))) return rc;
+      double bn2 = 0.0;
+      if ((rc = fetch(c->d_scal + 16, &bn2, 1))) return rc;
+      int its = 0;
+      rc = gmres(y, wk.f, gamma, std::sqrt(hb[1]), std::sqrt(bn2), &its);
+      st.n_lin_iters += its;
+      st.n_newton++;
+      if (rc < 0) return rc;
+      if (rc == 3) return 3;  // zero pivot in the ILU(0) factorisation
+      fos_launch(c, k_axpy, nb(N), kT, N, 1.0, wk.d, y);
+      FOS_LAUNCH_CHECK();
+    }
+    return 1;
+  }
   // GMRES on J_G d = b; d starts at zero.  With a learned preconditioner (o.precond >= 2)
   // this is flexible GMRES (Z_j = M_j(V_j) kept); in modes 2 and 4 it falls back to ILU(0)
   // -- restarting from the current iterate -- when the residual estimate stagnates (> 0.9
@@ -510,7 +588,6 @@ extern "C" int fos_bdf_run(fos_ctx* c, double t0, double* y, const fos_bdf_opts*
   dr.ilu_ref_its = wk.ilu_ref_its;
   dr.ilu_ref_rate = wk.ilu_ref_rate;
   double t = t0;
-  double hb[4];
   FOS_CUDA(cudaMemcpyAsync(wk.yn, y, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
   if (!resume) wk.has_hist = false;
   int status = 0;
@@ -520,45 +597,10 @@ extern "C" int fos_bdf_run(fos_ctx* c, double t0, double* y, const fos_bdf_opts*
     const double tn = t + opts->dt;
     fos_launch(c, k_hist, nb(N), kT, N, q, wk.yn, wk.ym, wk.hist);
     FOS_CUDA(cudaMemcpyAsync(y, wk.yn, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
-    bool conv = false;
-    double gtol = 0.0;
-    for (int k = 0; k <= opts->max_newton; k++) {
-      FOS_CUDA(cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream));
-      int rc = fos_residual_launch(c, y, nullptr, nullptr, nullptr, wk.f, 0.0, 0.0, 0);
-      if (rc) return rc;
-      st.n_rhs++;
-      fos_launch(c, k_newton_res, kRedBlocks, kT, N, (const double*)y, (const double*)wk.f,
-                 (const double*)wk.hist, gamma, wk.b, wk.part);
-      if ((rc = dr.reduce(2, wk.sc))) return rc;
-      FOS_CUDA(cudaMemcpyAsync(hb, wk.sc, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-      FOS_CUDA(cudaMemcpyAsync(c->h_scal, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-      FOS_CUDA(cudaStreamSynchronize(c->stream));
-      if (*(int*)c->h_scal) { status = 2; break; }  // non-finite residual
-      // y_0 = y_n, so the first pass also gives ||y_n||
-      if (k == 0) gtol = opts->newton_rtol * std::sqrt(hb[1]) + opts->newton_atol * std::sqrt((double)N);
-      const double gn = std::sqrt(hb[0]);
-      st.last_gnorm = gn / gtol;
-      if (gn <= gtol) { conv = true; break; }
-      if (k == opts->max_newton) break;
-      if (k == 0) {
-        dr.pset_done = false;
-        dr.t_step = tn;
-        dr.gamma_step = gamma;
-        dr.y_step = y;
-      }
-      // ||G|| for the linear tolerance: ||b||^2 via the norm kernel
-      if ((rc = fos_norm2_dev(c, wk.b, N, c->d_scal + 16))) return rc;
-      double bn2 = 0.0;
-      if ((rc = dr.fetch(c->d_scal + 16, &bn2, 1))) return rc;
-      int its = 0;
-      rc = dr.gmres(y, wk.f, gamma, std::sqrt(hb[1]), std::sqrt(bn2), &its);
-      st.n_lin_iters += its;
-      st.n_newton++;
-      if (rc < 0) return rc;
-      if (rc == 3) { status = 3; break; }  // zero pivot in the ILU(0) factorisation
-      fos_launch(c, k_axpy, nb(N), kT, N, 1.0, wk.d, y);
-      FOS_LAUNCH_CHECK();
-    }
+    const int nrc = dr.newton(y, gamma, wk.hist, tn);  // from y_0 = y_n
+    if (nrc < 0) return nrc;
+    const bool conv = nrc == 0;
+    if (nrc >= 2) status = nrc;
     if (!conv) {
       st.fails++;
       if (!status) status = 1;
@@ -595,6 +637,256 @@ extern "C" int fos_bdf_run_host(fos_ctx* c, double t0, double* y, const fos_bdf_
   FOS_CUDA(cudaMemcpyAsync(y, c->d_stage, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream));
   FOS_CUDA(cudaStreamSynchronize(c->stream));
   return rc;
+}
+
+// ------------------------------------------------------------------ adaptive BDF
+namespace {
+
+// Lagrange basis at x on nodes t[0..m-1]: w[j] = prod_{k != j} (x - t_k) / (t_j - t_k)
+void lagrange_at(const double* t, int m, double x, double* w) {
+  for (int j = 0; j < m; j++) {
+    double v = 1.0;
+    for (int k = 0; k < m; k++)
+      if (k != j) v *= (x - t[k]) / (t[j] - t[k]);
+    w[j] = v;
+  }
+}
+// derivatives of the Lagrange basis at the first node t[0]
+void lagrange_deriv_at_first(const double* t, int m, double* d) {
+  double d0 = 0.0;
+  for (int k = 1; k < m; k++) d0 += 1.0 / (t[0] - t[k]);
+  d[0] = d0;
+  for (int j = 1; j < m; j++) {
+    double v = 1.0 / (t[j] - t[0]);
+    for (int k = 1; k < m; k++)
+      if (k != j) v *= (t[0] - t[k]) / (t[j] - t[k]);
+    d[j] = v;
+  }
+}
+// CVODE's step factor from an error estimate at order k with bias b
+double eta_of(double err, int k, double bias) {
+  return 1.0 / (std::pow(bias * err, 1.0 / (k + 1)) + 1e-6);
+}
+
+int adapt_alloc(Work& wk, int qmax) {
+  const long N = wk.N;
+  for (int k = 0; k <= qmax; k++)
+    if (!wk.ay[k]) FOS_CUDA(cudaMalloc(&wk.ay[k], sizeof(double) * N));
+  for (double** p : {&wk.ypred, &wk.E, &wk.Eprev, &wk.atmp})
+    if (!*p) FOS_CUDA(cudaMalloc(p, sizeof(double) * N));
+  return 0;
+}
+
+struct Adapt {
+  fos_ctx* c;
+  Work& wk;
+  Driver& dr;
+  long N;
+  int comb(double* out, int nv, const double* const* p, const double* coef) {
+    Comb8 cb;
+    cb.nv = nv;
+    for (int l = 0; l < nv; l++) { cb.p[l] = p[l]; cb.c[l] = coef[l]; }
+    fos_launch(c, k_lincomb, nb(N), kT, N, cb, out);
+    FOS_LAUNCH_CHECK();
+    return 0;
+  }
+  // ||a||_WRMS with weights from w
+  int wrms(const double* a, const double* w, double rtol, double atol, double* out) {
+    fos_launch(c, k_wrms_part, kRedBlocks, kT, N, a, w, rtol, atol, wk.part);
+    if (int rc = dr.reduce(1, wk.sc + 5 * kMaxVec)) return rc;
+    double h = 0.0;
+    if (int rc = dr.fetch(wk.sc + 5 * kMaxVec, &h, 1)) return rc;
+    *out = std::sqrt(h / (double)N);
+    return 0;
+  }
+};
+
+}  // namespace
+
+extern "C" void fos_bdf_adapt_defaults(fos_bdf_adapt_opts* o) {
+  o->rtol = 1e-6;
+  o->atol = 1e-12;
+  o->h0 = 1e-4;
+  o->hmin = 0.0;
+  o->hmax = 0.0;
+  o->qmax = 5;
+  o->max_steps = 0;
+}
+
+// Variable-order, variable-step BDF from t0 to tout (see fosgpu.h).  History: the last
+// qmax + 1 accepted solutions Y[0] (newest) .. at times T[0] ..; a step of order q from
+// t = T[0] with size h:
+//   predictor   y_pred = sum_j L_j(t + h) Y[j], Lagrange on T[0..q] (the first step:
+//               y_0 + h f(y_0)), error factor h / (t + h - T[q]) (first step 1/2);
+//   corrector   Newton on y - gamma f(y) - hist = 0 with l_j the Lagrange derivatives at
+//               t + h on the nodes (t + h, T[0..q-1]): gamma = 1 / l_0,
+//               hist = -gamma sum_{j >= 1} l_j Y[j-1];
+//   error test  err = factor ||y - y_pred||_WRMS <= 1.
+extern "C" int fos_bdf_adaptive(fos_ctx* c, double t0, double tout, double* y,
+                                const fos_bdf_opts* nk, const fos_bdf_adapt_opts* ad,
+                                fos_bdf_stats* nk_stats, fos_bdf_adapt_stats* ad_stats) {
+  if (!c || !y || !nk || !ad || nk->maxl < 1 || nk->maxl > kMaxVec - 1 || nk->precond < 0 ||
+      nk->precond > 5 || ad->qmax < 1 || ad->qmax > 5 || !(ad->h0 > 0.0) || !(tout > t0) ||
+      !(ad->rtol >= 0.0) || !(ad->atol > 0.0)) {
+    fos_set_error("fos_bdf_adaptive: bad arguments (qmax in [1, 5], h0 > 0, tout > t0, atol > 0)");
+    return -1;
+  }
+  fos_bdf_stats dummy;
+  fos_bdf_stats& st = nk_stats ? *nk_stats : dummy;
+  std::memset(&st, 0, sizeof(st));
+  fos_bdf_adapt_stats adummy;
+  fos_bdf_adapt_stats& as = ad_stats ? *ad_stats : adummy;
+  std::memset(&as, 0, sizeof(as));
+  Work* wkp = nullptr;
+  if (int rc = work_get(c, nk->maxl, &wkp)) return rc;
+  Work& wk = *wkp;
+  if (int rc = adapt_alloc(wk, ad->qmax)) return rc;
+  const long N = wk.N;
+  const int qmax = ad->qmax;
+  const long max_steps = ad->max_steps > 0 ? ad->max_steps : 100000;
+  double eps = nk->jv_eps > 0.0 ? nk->jv_eps
+               : (c->flags & FOS_FLUX_FP32) ? std::sqrt((double)FLT_EPSILON)
+                                            : std::sqrt(DBL_EPSILON);
+  Driver dr{c, wk, *nk, st, eps};
+  dr.ilu_ref_its = wk.ilu_ref_its;
+  dr.ilu_ref_rate = wk.ilu_ref_rate;
+  Adapt A{c, wk, dr, N};
+  double* Y[6];
+  double T[6];
+  for (int k = 0; k <= qmax; k++) Y[k] = wk.ay[k];
+  FOS_CUDA(cudaMemcpyAsync(Y[0], y, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+  T[0] = t0;
+  int nh = 1;  // solutions in the history
+  // f(t0, y0) for the first predictor
+  if (int rc = fos_residual_launch(c, Y[0], nullptr, nullptr, nullptr, wk.atmp, 0.0, 0.0, 0)) return rc;
+  st.n_rhs++;
+  double t = t0;
+  double h = ad->h0;
+  if (ad->hmax > 0.0) h = std::min(h, ad->hmax);
+  int q = 1, nq = 0, nef = 0, ncf = 0;
+  double h_prev = 0.0;
+  bool have_eprev = false;
+  long attempts = 0;
+  int status = 0;
+  while (t < tout) {
+    if (++attempts > max_steps) { status = 5; break; }
+    if (t + h >= tout) h = tout - t;
+    const double tn = t + h;
+    // predictor
+    double errfac;
+    if (nh == 1) {
+      const double* p[2] = {Y[0], wk.atmp};
+      const double cf[2] = {1.0, h};
+      if (int rc = A.comb(wk.ypred, 2, p, cf)) return rc;
+      errfac = 0.5;
+    } else {
+      double w[6];
+      lagrange_at(T, q + 1, tn, w);
+      if (int rc = A.comb(wk.ypred, q + 1, Y, w)) return rc;
+      errfac = h / (tn - T[q]);
+    }
+    FOS_CUDA(cudaMemcpyAsync(y, wk.ypred, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+    // corrector coefficients
+    double tau[6], dl[6];
+    tau[0] = tn;
+    for (int j = 0; j < q; j++) tau[j + 1] = T[j];
+    lagrange_deriv_at_first(tau, q + 1, dl);
+    const double gamma = 1.0 / dl[0];
+    {
+      double cf[5];
+      for (int j = 1; j <= q; j++) cf[j - 1] = -gamma * dl[j];
+      if (int rc = A.comb(wk.hist, q, Y, cf)) return rc;
+    }
+    const int nrc = dr.newton(y, gamma, wk.hist, tn);
+    if (nrc < 0) return nrc;
+    if (nrc != 0) {  // Newton failure (no convergence, non-finite residual, zero pivot)
+      as.n_newton_fails++;
+      if (++ncf > 10 || 0.25 * h < ad->hmin) { status = 4; break; }
+      h *= 0.25;
+      continue;
+    }
+    // local error estimate
+    {
+      const double* p[2] = {y, wk.ypred};
+      const double cf[2] = {1.0, -1.0};
+      if (int rc = A.comb(wk.E, 2, p, cf)) return rc;
+    }
+    double en = 0.0;
+    if (int rc = A.wrms(wk.E, Y[0], ad->rtol, ad->atol, &en)) return rc;
+    const double err = errfac * en;
+    if (err > 1.0) {  // error-test failure: retry with a smaller step
+      as.n_err_fails++;
+      if (++nef > 7) { status = 4; break; }
+      double eta;
+      if (nef >= 3) {
+        eta = 0.1;
+        if (q > 1) { q = 1; nq = 0; have_eprev = false; }
+      } else {
+        eta = std::max(0.2, std::min(0.9, eta_of(err, q, 6.0)));
+      }
+      h *= eta;
+      if (h < ad->hmin) { status = 4; break; }
+      continue;
+    }
+    // accepted: step factor for this order, and for orders q -/+ 1 after q + 1 steps
+    nef = ncf = 0;
+    nq++;
+    double eta = eta_of(err, q, 6.0);
+    int qnew = q;
+    if (nq >= q + 1) {
+      if (q > 1) {  // order q - 1: its predictor on T[0..q-1]
+        double w[6];
+        lagrange_at(T, q, tn, w);
+        if (int rc = A.comb(wk.atmp, q, Y, w)) return rc;
+        const double* p[2] = {y, wk.atmp};
+        const double cf[2] = {1.0, -1.0};
+        if (int rc = A.comb(wk.atmp, 2, p, cf)) return rc;
+        double e1 = 0.0;
+        if (int rc = A.wrms(wk.atmp, Y[0], ad->rtol, ad->atol, &e1)) return rc;
+        const double eta_dn = eta_of(h / (tn - T[q - 1]) * e1, q - 1, 6.0);
+        if (eta_dn > eta) { eta = eta_dn; qnew = q - 1; }
+      }
+      if (q < qmax && have_eprev) {  // order q + 1: the change of the error vectors
+        const double r = h / h_prev;
+        const double* p[2] = {wk.E, wk.Eprev};
+        const double cf[2] = {1.0, -std::pow(r, q + 1)};
+        if (int rc = A.comb(wk.atmp, 2, p, cf)) return rc;
+        double e2 = 0.0;
+        if (int rc = A.wrms(wk.atmp, Y[0], ad->rtol, ad->atol, &e2)) return rc;
+        const double eta_up = eta_of(e2 / (q + 2), q + 1, 10.0);
+        if (eta_up > eta) { eta = eta_up; qnew = q + 1; }
+      }
+    }
+    // history: the new solution becomes Y[0]
+    double* last = Y[qmax];
+    for (int k = qmax; k > 0; k--) { Y[k] = Y[k - 1]; T[k] = T[k - 1]; }
+    Y[0] = last;
+    T[0] = tn;
+    FOS_CUDA(cudaMemcpyAsync(Y[0], y, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+    nh = std::min(nh + 1, qmax + 1);
+    std::swap(wk.E, wk.Eprev);
+    have_eprev = true;
+    h_prev = h;
+    as.n_accepted++;
+    as.steps_at_order[q]++;
+    as.q_last = q;
+    as.h_last = h;
+    st.n_steps++;
+    t = tn;
+    if (qnew != q) { q = qnew; nq = 0; have_eprev = false; }
+    if (q > nh - 1) q = nh - 1;
+    if (eta < 1.5) eta = 1.0;
+    h *= std::min(eta, 10.0);
+    if (ad->hmax > 0.0) h = std::min(h, ad->hmax);
+  }
+  FOS_CUDA(cudaMemcpyAsync(y, Y[0], sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+  wk.ilu_ref_its = dr.ilu_ref_its;
+  wk.ilu_ref_rate = dr.ilu_ref_rate;
+  wk.has_hist = false;  // the fixed-step history does not continue an adaptive run
+  as.t = t;
+  st.t = t;
+  FOS_CUDA(cudaStreamSynchronize(c->stream));
+  return status;
 }
 
 // One linear solve J_G x = b at state y (f(y) = fy) with the driver's (F)GMRES and the

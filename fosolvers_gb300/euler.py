@@ -224,6 +224,23 @@ class FOEuler:
                    "fos_bdf_run")
         return rc, st.as_dict()
 
+    @staticmethod
+    def adapt_defaults(**kw):
+        o = _lib.AdaptOpts()
+        _lib.lib().fos_bdf_adapt_defaults(C.byref(o))
+        for k, v in kw.items():
+            setattr(o, k, v)
+        return o
+
+    def bdf_adaptive(self, y_dev, t0: float, tout: float, nk: BdfOpts, ad):
+        """Advance the device state (internal order) from t0 to tout with the variable-order,
+        variable-step BDF driver; returns (rc, Newton-Krylov stats, step-control stats)."""
+        st, ast = BdfStats(), _lib.AdaptStats()
+        rc = check(_lib.lib().fos_bdf_adaptive(self._h, t0, tout, y_dev.data_ptr(), C.byref(nk),
+                                               C.byref(ad), C.byref(st), C.byref(ast)),
+                   "fos_bdf_adaptive")
+        return rc, st.as_dict(), ast.as_dict()
+
     def attach_gnn(self, gnn):
         """Learned preconditioner used by bdf_run / linear_solve when opts.precond == 2."""
         check(_lib.lib().fos_ctx_attach_gnn(self._h, gnn.handle if gnn is not None else None),

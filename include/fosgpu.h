@@ -222,6 +222,42 @@ int fos_bdf_run(fos_ctx* ctx, double t0, double* y, const fos_bdf_opts* opts,
 int fos_bdf_run_host(fos_ctx* ctx, double t0, double* y, const fos_bdf_opts* opts,
                      fos_bdf_stats* stats);
 
+/* ---------------------------------------------------------------- adaptive BDF
+ * Variable-order (1..qmax <= 5), variable-step BDF with local error control, the time
+ * stepping CVODE gives foeuler (CVodeCreate(CV_BDF), CVodeSStolerances, CVode to tout;
+ * SUNDIALS.f90:745-845, foeuler.f90:14-15,171-174,450), restated from SUNDIALS' published
+ * algorithm for the device driver: variable-coefficient BDF formulas at the actual past
+ * times, an extrapolation predictor, the local error estimate
+ * h / (t_{n+1} - t_{n-q}) ||y_{n+1} - y_pred|| in the weighted RMS norm with
+ * weights 1 / (rtol |y_n| + atol), step factors 1 / ((b err)^(1/(k+1)) + 1e-6) with biases
+ * b = 6 (orders q-1, q) and 10 (order q+1), order changes considered after q + 1 steps at
+ * one order, steps changed only by factors >= 1.5, and on an error-test failure a factor
+ * in [0.2, 0.9] (order 1 and 0.1 after three failures), on a Newton failure 0.25.  Each
+ * step's nonlinear system is solved by the fixed-step driver's Newton--(F)GMRES with
+ * `nk` (newton_rtol, maxl, precond, ...; nk->order, dt, nsteps and resume are unused).
+ * The last step is shortened to land on tout.  No reference counterpart for the
+ * interface; CVODE's adaptivity is the behaviour it restates. */
+typedef struct {
+  double rtol, atol;  /* local error tolerances (CVODE's RTOL 1e-6, ATOL 1e-12 in foeuler) */
+  double h0;          /* first step size (> 0) */
+  double hmin, hmax;  /* step bounds (hmax <= 0: unbounded) */
+  int qmax;           /* maximum order, 1..5 */
+  int max_steps;      /* attempted steps before giving up (<= 0: 100000) */
+} fos_bdf_adapt_opts;
+typedef struct {
+  long n_accepted, n_err_fails, n_newton_fails;
+  double h_last, t;
+  int q_last;
+  long steps_at_order[6];  /* accepted steps per order (index = order) */
+} fos_bdf_adapt_stats;
+void fos_bdf_adapt_defaults(fos_bdf_adapt_opts* o);
+/* Advance y (device, internal order) from t0 to tout.  Returns 0 on reaching tout, 4 if
+ * the step size fell below hmin or too many failures occurred at one step, 5 if
+ * max_steps was exceeded, < 0 on errors.  nk_stats accumulates the Newton--Krylov work. */
+int fos_bdf_adaptive(fos_ctx* ctx, double t0, double tout, double* y,
+                     const fos_bdf_opts* nk, const fos_bdf_adapt_opts* ad,
+                     fos_bdf_stats* nk_stats, fos_bdf_adapt_stats* ad_stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1192,6 +1192,44 @@ void o_bdf_defaults(o_bdf_opts* o) {
 }
 
 
+/* Newton on G(y) = y - gamma f(tn, y) - hist = 0 from the initial iterate in y, until
+ * ||G||_2 <= newton_rtol ||y_0||_2 + newton_atol sqrt(n); pset once, at the first linear
+ * solve.  Work arrays: f, G, d, ytmp, ftmp (n each).  Returns 0 converged, 1 not
+ * converged, 2 non-finite residual or rhs failure, 3 pset failure, 4 GMRES failure. */
+static int o_newton(int n, o_rhs_fn rhs, o_pset_fn pset, o_psol_fn psol, void* ud, double tn,
+                    double* y, double gamma, const double* hist, const o_bdf_opts* opts,
+                    o_bdf_stats* st, double* f, double* G, double* d, double* ytmp, double* ftmp) {
+  double gtol = 0.0;
+  for (int k = 0; k <= opts->max_newton; k++) {
+    int rc = rhs(tn, y, f, ud);
+    st->n_rhs++;
+    if (rc) return 2;
+    for (int i = 0; i < n; i++) G[i] = y[i] - gamma * f[i] - hist[i];
+    if (k == 0) gtol = opts->newton_rtol * sqrt(vdot(n, y, y)) + opts->newton_atol * sqrt((double)n);
+    double gn = sqrt(vdot(n, G, G));
+    if (!isfinite(gn)) return 2;
+    st->last_gnorm = gn / gtol;
+    if (gn <= gtol) return 0;
+    if (k == opts->max_newton) break;
+    if (k == 0 && opts->use_prec) {
+      int jcur = 0;
+      rc = pset(tn, y, f, 0, &jcur, gamma, ud);
+      st->n_pset++;
+      if (rc) return 3;
+    }
+    nk_op op = {n, rhs, psol, ud, tn, gamma, 1.0, -gamma, sqrt(vdot(n, y, y)), opts->jv_eps,
+                y, f, ytmp, ftmp, st, opts->use_prec};
+    for (int i = 0; i < n; i++) G[i] = -G[i];
+    int its = 0;
+    rc = nk_gmres(&op, G, d, opts->maxl, opts->max_restarts, opts->lin_rtol, &its);
+    st->n_lin_iters += its;
+    st->n_newton++;
+    if (rc < 0) return 4;
+    for (int i = 0; i < n; i++) y[i] += d[i];
+  }
+  return 1;
+}
+
 int o_bdf_run(int n, o_rhs_fn rhs, o_pset_fn pset, o_psol_fn psol, void* ud, double t0,
               double* y, const o_bdf_opts* opts, o_bdf_stats* st) {
   o_bdf_stats dummy;
@@ -1216,36 +1254,10 @@ int o_bdf_run(int n, o_rhs_fn rhs, o_pset_fn pset, o_psol_fn psol, void* ud, dou
     }
     double tn = t + opts->dt;
     memcpy(y, yn, sizeof(double) * n); /* predictor: previous state */
-    const double gtol = opts->newton_rtol * sqrt(vdot(n, yn, yn)) + opts->newton_atol * sqrt((double)n);
-    int conv = 0;
-    for (int k = 0; k <= opts->max_newton; k++) {
-      int rc = rhs(tn, y, f, ud);
-      st->n_rhs++;
-      if (rc) { status = 2; break; }
-      for (int i = 0; i < n; i++) G[i] = y[i] - gamma * f[i] - hist[i];
-      double gn = sqrt(vdot(n, G, G));
-      st->last_gnorm = gn / gtol;
-      if (gn <= gtol) { conv = 1; break; }
-      if (k == opts->max_newton) break;
-      if (k == 0 && opts->use_prec) {
-        int jcur = 0;
-        rc = pset(tn, y, f, 0, &jcur, gamma, ud);
-        st->n_pset++;
-        if (rc) { status = 3; break; }
-      }
-      nk_op op = {n, rhs, psol, ud, tn, gamma, 1.0, -gamma, sqrt(vdot(n, y, y)), opts->jv_eps,
-                  y, f, ytmp, ftmp, st, opts->use_prec};
-      for (int i = 0; i < n; i++) G[i] = -G[i];
-      int its = 0;
-      rc = nk_gmres(&op, G, d, opts->maxl, opts->max_restarts, opts->lin_rtol, &its);
-      st->n_lin_iters += its;
-      st->n_newton++;
-      if (rc < 0) { status = 4; break; }
-      for (int i = 0; i < n; i++) y[i] += d[i];
-    }
-    if (!conv) {
+    int nrc = o_newton(n, rhs, pset, psol, ud, tn, y, gamma, hist, opts, st, f, G, d, ytmp, ftmp);
+    if (nrc) {
       st->fails++;
-      if (!status) status = 1;
+      status = nrc == 1 ? 1 : nrc;
       break;
     }
     memcpy(ynm1, yn, sizeof(double) * n);
@@ -1254,6 +1266,186 @@ int o_bdf_run(int n, o_rhs_fn rhs, o_pset_fn pset, o_psol_fn psol, void* ud, dou
     st->n_steps++;
   }
   free(yn); free(ynm1); free(hist); free(f); free(G); free(d); free(ytmp); free(ftmp);
+  return status;
+}
+
+/* ---------------------------------------------------------------------- adaptive BDF
+ * Variable-order (1..qmax), variable-step BDF with local error control: the restatement of
+ * CVODE's published step and order selection that the GPU driver uses too (predictor by
+ * Lagrange extrapolation on the last q + 1 solutions -- the first step y0 + h f(y0) --,
+ * corrector from the Lagrange derivatives on (t + h, T[0..q-1]), error
+ * h / (t + h - T[q]) ||y - y_pred||_WRMS, weights 1/(rtol |y_n| + atol), step factors
+ * 1 / ((b err)^(1/(k+1)) + 1e-6), b = 6 for orders q, q - 1 and 10 for q + 1, order
+ * changes after q + 1 steps at one order, factor < 1.5 -> keep h, at most 10; error-test
+ * failure: factor in [0.2, 0.9], order 1 and 0.1 from the third; Newton failure: 0.25). */
+static void o_lagrange_at(const double* t, int m, double x, double* w) {
+  for (int j = 0; j < m; j++) {
+    double v = 1.0;
+    for (int k = 0; k < m; k++)
+      if (k != j) v *= (x - t[k]) / (t[j] - t[k]);
+    w[j] = v;
+  }
+}
+static void o_lagrange_deriv_first(const double* t, int m, double* dl) {
+  double d0 = 0.0;
+  for (int k = 1; k < m; k++) d0 += 1.0 / (t[0] - t[k]);
+  dl[0] = d0;
+  for (int j = 1; j < m; j++) {
+    double v = 1.0 / (t[j] - t[0]);
+    for (int k = 1; k < m; k++)
+      if (k != j) v *= (t[0] - t[k]) / (t[j] - t[k]);
+    dl[j] = v;
+  }
+}
+static double o_eta(double err, int k, double bias) {
+  return 1.0 / (pow(bias * err, 1.0 / (k + 1)) + 1e-6);
+}
+static double o_wrms(int n, const double* a, const double* w, double rtol, double atol) {
+  double s = 0.0;
+  for (int i = 0; i < n; i++) {
+    const double e = a[i] / (rtol * fabs(w[i]) + atol);
+    s += e * e;
+  }
+  return sqrt(s / (double)n);
+}
+static void o_comb(int n, double* out, int nv, double* const* p, const double* c) {
+  for (int i = 0; i < n; i++) {
+    double s = 0.0;
+    for (int l = 0; l < nv; l++) s += c[l] * p[l][i];
+    out[i] = s;
+  }
+}
+
+void o_adapt_defaults(o_adapt_opts* o) {
+  o->rtol = 1e-6; o->atol = 1e-12; o->h0 = 1e-4; o->hmin = 0.0; o->hmax = 0.0;
+  o->qmax = 5; o->max_steps = 0;
+}
+
+int o_bdf_adaptive(int n, o_rhs_fn rhs, o_pset_fn pset, o_psol_fn psol, void* ud, double t0,
+                   double tout, double* y, const o_bdf_opts* nk, const o_adapt_opts* ad,
+                   o_bdf_stats* st, o_adapt_stats* as) {
+  o_bdf_stats dummy;
+  o_adapt_stats adummy;
+  if (!st) st = &dummy;
+  if (!as) as = &adummy;
+  memset(st, 0, sizeof(*st));
+  memset(as, 0, sizeof(*as));
+  if (ad->qmax < 1 || ad->qmax > 5 || !(ad->h0 > 0.0) || !(tout > t0)) return -1;
+  const int qmax = ad->qmax;
+  const long max_steps = ad->max_steps > 0 ? ad->max_steps : 100000;
+  double* Y[6];
+  double T[6];
+  for (int k = 0; k <= qmax; k++) Y[k] = (double*)xcalloc(n, sizeof(double));
+  double *ypred = (double*)xcalloc(n, sizeof(double)), *E = (double*)xcalloc(n, sizeof(double));
+  double *Eprev = (double*)xcalloc(n, sizeof(double)), *tmp = (double*)xcalloc(n, sizeof(double));
+  double *hist = (double*)xcalloc(n, sizeof(double)), *f = (double*)xcalloc(n, sizeof(double));
+  double *G = (double*)xcalloc(n, sizeof(double)), *d = (double*)xcalloc(n, sizeof(double));
+  double *ytmp = (double*)xcalloc(n, sizeof(double)), *ftmp = (double*)xcalloc(n, sizeof(double));
+  double *f0 = (double*)xcalloc(n, sizeof(double));
+  memcpy(Y[0], y, sizeof(double) * n);
+  T[0] = t0;
+  int nh = 1, status = 0;
+  if (rhs(t0, Y[0], f0, ud)) status = 2;
+  st->n_rhs++;
+  double t = t0, h = ad->h0, h_prev = 0.0;
+  if (ad->hmax > 0.0 && h > ad->hmax) h = ad->hmax;
+  int q = 1, nq = 0, nef = 0, ncf = 0, have_eprev = 0;
+  long attempts = 0;
+  while (!status && t < tout) {
+    if (++attempts > max_steps) { status = 5; break; }
+    if (t + h >= tout) h = tout - t;
+    const double tn = t + h;
+    double errfac;
+    if (nh == 1) {
+      for (int i = 0; i < n; i++) ypred[i] = 1.0 * Y[0][i] + h * f0[i];
+      errfac = 0.5;
+    } else {
+      double w[6];
+      o_lagrange_at(T, q + 1, tn, w);
+      o_comb(n, ypred, q + 1, Y, w);
+      errfac = h / (tn - T[q]);
+    }
+    memcpy(y, ypred, sizeof(double) * n);
+    double tau[6], dl[6], cf[5];
+    tau[0] = tn;
+    for (int j = 0; j < q; j++) tau[j + 1] = T[j];
+    o_lagrange_deriv_first(tau, q + 1, dl);
+    const double gamma = 1.0 / dl[0];
+    for (int j = 1; j <= q; j++) cf[j - 1] = -gamma * dl[j];
+    o_comb(n, hist, q, Y, cf);
+    int nrc = o_newton(n, rhs, pset, psol, ud, tn, y, gamma, hist, nk, st, f, G, d, ytmp, ftmp);
+    if (nrc) {
+      as->n_newton_fails++;
+      if (++ncf > 10 || 0.25 * h < ad->hmin) { status = 4; break; }
+      h *= 0.25;
+      continue;
+    }
+    for (int i = 0; i < n; i++) E[i] = 1.0 * y[i] + -1.0 * ypred[i];
+    const double err = errfac * o_wrms(n, E, Y[0], ad->rtol, ad->atol);
+    if (err > 1.0) {
+      as->n_err_fails++;
+      if (++nef > 7) { status = 4; break; }
+      double eta;
+      if (nef >= 3) {
+        eta = 0.1;
+        if (q > 1) { q = 1; nq = 0; have_eprev = 0; }
+      } else {
+        eta = o_eta(err, q, 6.0);
+        eta = eta < 0.9 ? eta : 0.9;
+        eta = eta > 0.2 ? eta : 0.2;
+      }
+      h *= eta;
+      if (h < ad->hmin) { status = 4; break; }
+      continue;
+    }
+    nef = ncf = 0;
+    nq++;
+    double eta = o_eta(err, q, 6.0);
+    int qnew = q;
+    if (nq >= q + 1) {
+      if (q > 1) {
+        double w[6];
+        o_lagrange_at(T, q, tn, w);
+        o_comb(n, tmp, q, Y, w);
+        for (int i = 0; i < n; i++) tmp[i] = 1.0 * y[i] + -1.0 * tmp[i];
+        const double e1 = o_wrms(n, tmp, Y[0], ad->rtol, ad->atol);
+        const double eta_dn = o_eta(h / (tn - T[q - 1]) * e1, q - 1, 6.0);
+        if (eta_dn > eta) { eta = eta_dn; qnew = q - 1; }
+      }
+      if (q < qmax && have_eprev) {
+        const double r = h / h_prev, c2 = -pow(r, q + 1);
+        for (int i = 0; i < n; i++) tmp[i] = 1.0 * E[i] + c2 * Eprev[i];
+        const double e2 = o_wrms(n, tmp, Y[0], ad->rtol, ad->atol);
+        const double eta_up = o_eta(e2 / (q + 2), q + 1, 10.0);
+        if (eta_up > eta) { eta = eta_up; qnew = q + 1; }
+      }
+    }
+    double* last = Y[qmax];
+    for (int k = qmax; k > 0; k--) { Y[k] = Y[k - 1]; T[k] = T[k - 1]; }
+    Y[0] = last;
+    T[0] = tn;
+    memcpy(Y[0], y, sizeof(double) * n);
+    nh = nh + 1 < qmax + 1 ? nh + 1 : qmax + 1;
+    double* sw = E; E = Eprev; Eprev = sw;
+    have_eprev = 1;
+    h_prev = h;
+    as->n_accepted++;
+    as->steps_at_order[q]++;
+    as->q_last = q;
+    as->h_last = h;
+    st->n_steps++;
+    t = tn;
+    if (qnew != q) { q = qnew; nq = 0; have_eprev = 0; }
+    if (q > nh - 1) q = nh - 1;
+    if (eta < 1.5) eta = 1.0;
+    h *= eta < 10.0 ? eta : 10.0;
+    if (ad->hmax > 0.0 && h > ad->hmax) h = ad->hmax;
+  }
+  memcpy(y, Y[0], sizeof(double) * n);
+  as->t = t;
+  for (int k = 0; k <= qmax; k++) free(Y[k]);
+  free(ypred); free(E); free(Eprev); free(tmp); free(hist); free(f); free(G); free(d);
+  free(ytmp); free(ftmp); free(f0);
   return status;
 }
 

@@ -130,6 +130,22 @@ void o_bdf_defaults(o_bdf_opts* o);
 int o_bdf_run(int n, o_rhs_fn rhs, o_pset_fn pset, o_psol_fn psol, void* ud, double t0,
               double* y, const o_bdf_opts* opts, o_bdf_stats* st);
 /* Newton--GMRES on a steady G(x) = 0 written as the rhs callback (G = rhs(t=0,x)). */
+typedef struct {
+  double rtol, atol, h0, hmin, hmax;
+  int qmax, max_steps;
+} o_adapt_opts;
+typedef struct {
+  long n_accepted, n_err_fails, n_newton_fails;
+  double h_last, t;
+  int q_last;
+  long steps_at_order[6];
+} o_adapt_stats;
+void o_adapt_defaults(o_adapt_opts* o);
+/* variable-order, variable-step BDF from t0 to tout (0 ok, 2 rhs failure, 4 step failures,
+ * 5 too many steps) */
+int o_bdf_adaptive(int n, o_rhs_fn rhs, o_pset_fn pset, o_psol_fn psol, void* ud, double t0,
+                   double tout, double* y, const o_bdf_opts* nk, const o_adapt_opts* ad,
+                   o_bdf_stats* st, o_adapt_stats* as);
 int o_newton_solve(int n, o_rhs_fn G, void* ud, double* x, double rtol, double atol,
                    int max_newton, int maxl, double lin_rtol, o_bdf_stats* st);
 

@@ -28,6 +28,23 @@ class BdfOpts(C.Structure):
                 ("lin_rtol", C.c_double), ("jv_eps", C.c_double), ("use_prec", C.c_int)]
 
 
+class AdaptOpts(C.Structure):
+    _fields_ = [("rtol", C.c_double), ("atol", C.c_double), ("h0", C.c_double),
+                ("hmin", C.c_double), ("hmax", C.c_double), ("qmax", C.c_int),
+                ("max_steps", C.c_int)]
+
+
+class AdaptStats(C.Structure):
+    _fields_ = [("n_accepted", C.c_long), ("n_err_fails", C.c_long),
+                ("n_newton_fails", C.c_long), ("h_last", C.c_double), ("t", C.c_double),
+                ("q_last", C.c_int), ("steps_at_order", C.c_long * 6)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "steps_at_order"}
+        d["steps_at_order"] = list(self.steps_at_order)
+        return d
+
+
 class BdfStats(C.Structure):
     _fields_ = [("n_rhs", C.c_long), ("n_jv", C.c_long), ("n_psol", C.c_long),
                 ("n_pset", C.c_long), ("n_newton", C.c_long), ("n_lin_iters", C.c_long),
@@ -71,6 +88,10 @@ _SIGS = {
                             C.POINTER(BdfStats)]),
     "o_newton_solve": (C.c_int, [C.c_int, _vp, _vp, _dp, C.c_double, C.c_double, C.c_int, C.c_int,
                                  C.c_double, C.POINTER(BdfStats)]),
+    "o_adapt_defaults": (None, [C.POINTER(AdaptOpts)]),
+    "o_bdf_adaptive": (C.c_int, [C.c_int, _vp, _vp, _vp, _vp, C.c_double, C.c_double, _dp,
+                                 C.POINTER(BdfOpts), C.POINTER(AdaptOpts), C.POINTER(BdfStats),
+                                 C.POINTER(AdaptStats)]),
 }
 
 _lib = None
@@ -224,3 +245,20 @@ def bdf_run(n, rhs, pset, psol, ud, y, opts, t0=0.0):
     rc = lib().o_bdf_run(n, as_vp(rhs), as_vp(pset), as_vp(psol), ud, t0, dp(y), C.byref(opts),
                          C.byref(st))
     return rc, st.as_dict()
+
+
+def adapt_defaults(**kw) -> AdaptOpts:
+    o = AdaptOpts()
+    lib().o_adapt_defaults(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def bdf_adaptive(n, rhs, pset, psol, ud, y, t0, tout, nk, ad):
+    """Variable-order, variable-step BDF from t0 to tout; returns (rc, stats, step stats)."""
+    st, ast = BdfStats(), AdaptStats()
+    as_vp = lambda f: f if isinstance(f, (C.c_void_p, int)) or f is None else C.cast(f, _vp)
+    rc = lib().o_bdf_adaptive(n, as_vp(rhs), as_vp(pset), as_vp(psol), ud, t0, tout, dp(y),
+                              C.byref(nk), C.byref(ad), C.byref(st), C.byref(ast))
+    return rc, st.as_dict(), ast.as_dict()
