@@ -510,9 +510,13 @@ struct Driver {
         if (std::fabs(g[j + 1]) <= o.lin_rtol * bnorm || hn == 0.0) { conv = true; break; }
         // learned modes fall back when they stagnate, reach the ILU(0) iteration count, or
         // fall behind the ILU(0) solve's mean reduction per iteration
+        // (a non-finite estimate -- a network output with NaN or Inf -- falls back too, and
+        // its column is left out of the update)
+        const bool bad = !std::isfinite(g[j + 1]) || !std::isfinite(hn);
         if ((pc == 2 || pc == 4) &&
-            (*its >= ilu_ref_its || std::fabs(g[j + 1]) > 0.9 * std::fabs(g[j]) ||
+            (bad || *its >= ilu_ref_its || std::fabs(g[j + 1]) > 0.9 * std::fabs(g[j]) ||
              std::fabs(g[j + 1]) > beta * std::pow(ilu_ref_rate, j + 1))) {
+          if (bad) kend = j;
           fallback = true;
           break;
         }

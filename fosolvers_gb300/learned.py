@@ -193,7 +193,9 @@ def generate_pairs(n_meshes: int, seed: int = 0, sizes=(12, 20), newton_iters: i
             rc, _ = ctx.bdf_run(y, ctx.bdf_defaults(order=1, dt=dt, nsteps=1))
             if rc != 0:
                 break
-    return out
+    # keep finite samples only (a state the solver could not advance is dropped)
+    return [sm for sm in out
+            if all(bool(torch.isfinite(x).all()) for x in (sm.y, sm.b, sm.t, sm.u))]
 
 
 def train(gnn: GNN, pairs, epochs: int = 20, lr: float = 2e-3, seed: int = 0, log=None,
@@ -208,30 +210,44 @@ def train(gnn: GNN, pairs, epochs: int = 20, lr: float = 2e-3, seed: int = 0, lo
         order = rng.permutation(n)
         tot = 0.0
         lr_ep = lr * (0.5 * (1 + np.cos(np.pi * ep / max(epochs, 1))))  # cosine decay
+        used = 0
         for i in order:
             sm = pairs[i]
             gnn.zero_grad()
-            tot += gnn.loss_grad_dev(sm.ctx, sm.y, sm.u if after_ilu else sm.b, sm.t, sm.gamma)
+            loss = gnn.loss_grad_dev(sm.ctx, sm.y, sm.u if after_ilu else sm.b, sm.t, sm.gamma)
+            if not np.isfinite(loss):  # no step from a non-finite loss or gradient
+                continue
+            tot += loss
+            used += 1
             gnn.adam_step(lr=max(lr_ep, 1e-5))
-        hist.append(tot / n)
+        hist.append(tot / max(used, 1))
         if log:
             log(f"epoch {ep}: loss {hist[-1]:.4e}")
     return hist
 
 
-def krylov_iterations(pairs_ctx, precond: int, lin_rtol: float = 1e-6, maxl: int = 30):
-    """Krylov iterations (and fallbacks) of the linear solves of the given pairs."""
+def krylov_iterations(pairs_ctx, precond: int, lin_rtol: float = 1e-6, maxl: int = 30,
+                      timing: bool = False):
+    """Krylov iterations (and fallbacks) of the linear solves of the given pairs; with
+    timing, also the summed CUDA-event time of the solves in ms (the ILU(0) factorisation,
+    where the solve makes one, included)."""
     import torch
-    its, fb = [], 0
+    its, fb, ms = [], 0, 0.0
     for (c, y, b, t, gam, _u) in pairs_ctx:
         f = torch.empty_like(y)
         c.rhs_dev(0.0, y, f)
         x = torch.empty_like(b)
         opts = c.bdf_defaults(precond=precond, lin_rtol=lin_rtol, maxl=maxl, max_restarts=8)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
         rc, st = c.linear_solve(y, f, gam, b, x, opts)
+        e1.record()
+        torch.cuda.synchronize()
+        ms += e0.elapsed_time(e1)
         its.append(st["n_lin_iters"])
         fb += st["n_fallback"]
-    return its, fb
+    return (its, fb, ms) if timing else (its, fb)
 
 
 DEFAULT_WEIGHTS = Path(__file__).resolve().parent / "weights" / "gnn_sine.npy"
@@ -266,15 +282,18 @@ def _main(argv=None):
     t0 = time.time()
     hist = train(g, tr, epochs=a.epochs, lr=a.lr, log=lambda s: print(s, flush=True))
     print(f"trained in {time.time() - t0:.1f} s: loss {hist[0]:.4e} -> {hist[-1]:.4e}", flush=True)
+    Path(a.out).parent.mkdir(parents=True, exist_ok=True)
+    g.save(a.out)
+    print("saved", a.out, flush=True)
+    del tr
     for s in te:
         s.ctx.attach_gnn(g)
     for tol in (1e-3, 1e-6):
-        r = {name: sum(krylov_iterations(te, pc, lin_rtol=tol)[0])
-             for name, pc in (("none", 0), ("learned", 3), ("ILU(0)", 1))}
-        print(f"held-out Krylov iterations at {tol:g}: {r}", flush=True)
-    Path(a.out).parent.mkdir(parents=True, exist_ok=True)
-    g.save(a.out)
-    print("saved", a.out)
+        r = {}
+        for name, pc in (("none", 0), ("learned", 3), ("ILU(0)", 1), ("learned+fallback", 2)):
+            its, fb, ms = krylov_iterations(te, pc, lin_rtol=tol, timing=True)
+            r[name] = {"iterations": sum(its), "ms": round(ms, 1), "fallbacks": fb}
+        print(f"held-out ({len(te)} solves at {a.test_size}^3 x 6) at {tol:g}: {r}", flush=True)
 
 
 if __name__ == "__main__":
