@@ -21,9 +21,10 @@ rho E = rho (r T0 / (gamma - 1) + |u0|^2 / 2) (foeuler.f90:123-138).  Condition 
 are matched to elements by group id, first match wins (foeuler.f90:145-154).
 
 Time stepping: the reference hands the step size to CVODE (adaptive order and step,
-RTOL 1e-6).  Here the steps are fixed-size BDF1/BDF2 of the device driver, with dt given
-or derived from a CFL number on the initial state, and an output file at every multiple
-of the output interval.
+RTOL 1e-6, ATOL 1e-12).  Here either the device driver's variable-order, variable-step BDF
+at those tolerances runs from output time to output time (``adaptive``), or fixed-size
+BDF1/BDF2 steps with dt given or derived from a CFL number on the initial state; an output
+file is written at every multiple of the output interval.
 
 Output: ``rst_<k>.vtk`` with the grid (elements in the grid's order: cells, then facets)
 and per-element density, velocity, pressure and temperature (foeuler.f90:332-345).  The
@@ -182,8 +183,11 @@ def write_state(path, mesh, grid, y, r, gamm):
 
 
 def run_case(case_dir, out_dir=None, dt=None, cfl=5.0, order=2, flags=0, precond=1,
-             newton_rtol=1e-8, max_steps=None, write=True, log=print) -> dict:
-    """Run a foeuler case directory to its final time with fixed BDF steps on the GPU.
+             newton_rtol=1e-8, max_steps=None, write=True, log=print, adaptive=False,
+             rtol=1e-6, atol=1e-12) -> dict:
+    """Run a foeuler case directory to its final time on the GPU, with fixed BDF steps of
+    size dt, or (adaptive) with the variable-order, variable-step driver at the local error
+    tolerances foeuler gives CVODE (RTOL 1e-6, ATOL 1e-12; dt is then the first step).
     Returns the final SoA state (reference cell order) and run statistics."""
     import torch
     from .euler import FOEuler, PolyFvGrid
@@ -212,7 +216,29 @@ def run_case(case_dir, out_dir=None, dt=None, cfl=5.0, order=2, flags=0, precond
     t, k_out, n_steps, tot = 0.0, 0, 0, {}
     t_next = t_int
     resume = 0
-    while t < t_final * (1.0 - 1e-12) and (max_steps is None or n_steps < max_steps):
+    h = dt
+    while adaptive and t < t_final * (1.0 - 1e-12):
+        t_stop = min(t_next, t_final)
+        nk = ctx.bdf_defaults(precond=precond, newton_rtol=newton_rtol)
+        ad = ctx.adapt_defaults(rtol=rtol, atol=atol, h0=min(h, t_stop - t))
+        rc, st, ast = ctx.bdf_adaptive(yi, t, t_stop, nk, ad)
+        if rc != 0:
+            raise RuntimeError(f"adaptive BDF failed at t = {t:g} (rc {rc}): {ast}")
+        t = t_stop
+        h = ast["h_last"]
+        n_steps += ast["n_accepted"]
+        for key, val in list(st.items()) + list(ast.items()):
+            if isinstance(val, (int, float)) and key.startswith("n_"):
+                tot[key] = tot.get(key, 0) + val
+        log(f"[i] t = {t:.6g}, {n_steps} steps (last h = {h:.4g}, order {ast['q_last']}), "
+            f"Newton {st['n_newton']}, Krylov {st['n_lin_iters']}")
+        k_out += 1
+        if write:
+            yo = torch.empty_like(yi)
+            ctx.to_reference(yi, yo)
+            write_state(out / f"rst_{k_out}.vtk", mesh, grid, yo.cpu().numpy(), r, gamm)
+        t_next += t_int
+    while not adaptive and t < t_final * (1.0 - 1e-12) and (max_steps is None or n_steps < max_steps):
         n = max(1, int(math.ceil((min(t_next, t_final) - t) / dt - 1e-9)))
         if max_steps is not None:
             n = min(n, max_steps - n_steps)
@@ -254,10 +280,15 @@ def _main(argv=None):
     ap.add_argument("--order", type=int, default=2, choices=[1, 2])
     ap.add_argument("--fp32", action="store_true", help="FP32 flux and ILU(0) (flags 1 | 4 | 8)")
     ap.add_argument("--max-steps", type=int, default=None)
+    ap.add_argument("--adaptive", action="store_true",
+                    help="variable-order, variable-step BDF at --rtol/--atol (foeuler's CVODE "
+                         "tolerances by default); --dt or --cfl then sets the first step")
+    ap.add_argument("--rtol", type=float, default=1e-6)
+    ap.add_argument("--atol", type=float, default=1e-12)
     a = ap.parse_args(argv)
     flags = (1 | 4 | 8) if a.fp32 else 0
     res = run_case(a.case_dir, a.out, dt=a.dt, cfl=a.cfl, order=a.order, flags=flags,
-                   max_steps=a.max_steps)
+                   max_steps=a.max_steps, adaptive=a.adaptive, rtol=a.rtol, atol=a.atol)
     print(f"done: t = {res['t']:g}, {res['steps']} steps, {res['outputs']} outputs, "
           f"{res['cells']} cells")
 

@@ -52,3 +52,34 @@ def test_case_directory_matches_oracle_and_writes_results(cuda, tmp_path):
     np.testing.assert_array_equal(data["cell"]["velocity"][:nC], u)
     np.testing.assert_array_equal(data["cell"]["pressure"][:nC], p)
     np.testing.assert_array_equal(data["cell"]["temperature"][:nC], T)
+
+
+def test_adaptive_case_matches_oracle(cuda, tmp_path):
+    """The same case with the variable-order, variable-step driver at RTOL 1e-6, ATOL 1e-6
+    (SI state magnitudes ~1 to 1e5) from output time to output time: identical accepted-step
+    count to the oracle's restatement over each interval, final state within 1e-9."""
+    m = M.box_mesh(8, 5, 5, jitter=0.1, seed=7, extent=(1.0, 0.6, 0.6))
+    t1 = 4e-4
+    _write_case(tmp_path, m, [(M.GID_XMIN, 11, [1.05e5, 300.0, 1.0, 0.0, 0.0]),
+                              (M.GID_XMAX, 20, [0.95e5])],
+                ic=(1.0e5, 300.0, 0.0, 0.0, 0.0), sim=(t1, t1 / 2))
+    res = run_case(tmp_path, tmp_path / "out", dt=1e-6, adaptive=True, rtol=1e-6, atol=1e-6,
+                   newton_rtol=1e-10, log=lambda s: None)
+    assert res["outputs"] == 2 and abs(res["t"] - t1) <= 1e-15
+
+    wl = workload_from_case(tmp_path, dt=1e-6)
+    c = Case(wl)
+    c.match_ilu_order()
+    rhs, pset, psol = c.oracle.callbacks()
+    y_ref = c.y0.copy()
+    n_acc, h = 0, 1e-6
+    for (ta, tb) in ((0.0, t1 / 2), (t1 / 2, t1)):
+        rc, st, ast = O.bdf_adaptive(c.N, rhs, pset, psol, c.oracle.h, y_ref, ta, tb,
+                                     O.bdf_defaults(newton_rtol=1e-10),
+                                     O.adapt_defaults(rtol=1e-6, atol=1e-6, h0=min(h, tb - ta)))
+        assert rc == 0, ast
+        n_acc += ast["n_accepted"]
+        h = ast["h_last"]
+    print("adaptive case", res["steps"], n_acc, rel_err(res["y"], y_ref))
+    assert res["steps"] == n_acc
+    assert rel_err(res["y"], y_ref) <= 1e-9
