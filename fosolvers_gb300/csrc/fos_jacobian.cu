@@ -384,8 +384,13 @@ __global__ void __launch_bounds__(kT) k_ilu_factor(
   // update operands (inv(D_q), U_qj of earlier levels) of the first kPre operations of a row
   // are fetched into shared memory before the elimination, all loads in flight at once
   constexpr int kPre = sizeof(TF) == 4 ? 8 : 0;
-  __shared__ TF sm[kRowsPerCta][kMaxBlocksPerRow][25];
-  __shared__ TF bsm[kRowsPerCta][kPre > 0 ? kPre : 1][25];
+  // row strides padded so that the 5 lanes x 6 rows of a warp (and the 6 rows' broadcast
+  // operand reads) fall in distinct shared-memory banks: 185 = 7 x 25 + 10, 201 = 8 x 25 + 1
+  constexpr int kSmRow = 185, kBsRow = kPre > 0 ? 201 : 25;
+  __shared__ TF sm_[kRowsPerCta * kSmRow];
+  __shared__ TF bsm_[kRowsPerCta * kBsRow];
+  auto sm = [&](int r, int b) -> TF* { return sm_ + r * kSmRow + 25 * b; };
+  auto bsm = [&](int r, int o) -> TF* { return bsm_ + r * kBsRow + 25 * o; };
   const int lane = threadIdx.x & 31;
   const int sub = lane / 5, a = lane - 5 * sub;
   const int lrow = (threadIdx.x >> 5) * 6 + (sub < 6 ? sub : 0);
@@ -413,7 +418,7 @@ __global__ void __launch_bounds__(kT) k_ilu_factor(
       for (int o = 0; o < kPre; o++)
         if (o < no) {
 #pragma unroll
-          for (int k = 0; k < 5; k++) bsm[lrow][o][5 * a + k] = pre[o][k];
+          for (int k = 0; k < 5; k++) bsm(lrow, o)[5 * a + k] = pre[o][k];
         }
     }
     // P = I - (gamma / v) J in the factor's precision (FP32 arithmetic in the FP32 form)
@@ -425,7 +430,7 @@ __global__ void __launch_bounds__(kT) k_ilu_factor(
       const bool dg = (s0 + b) == sd;
 #pragma unroll
       for (int k = 0; k < 5; k++)
-        sm[lrow][b][5 * a + k] = ((dg && k == a) ? TF(1) : TF(0)) - sc * (TF)src[k];
+        sm(lrow, b)[5 * a + k] = ((dg && k == a) ? TF(1) : TF(0)) - sc * (TF)src[k];
     }
   }
   __syncwarp();  // the five lanes of a row see each other's operand rows
@@ -433,11 +438,11 @@ __global__ void __launch_bounds__(kT) k_ilu_factor(
     for (int o = 0; o < no; o++) {
       const int3 op = upd[o0 + o];
       TF A[5];
-      TF* Ar = &sm[lrow][op.x - s0][5 * a];
+      TF* Ar = sm(lrow, op.x - s0) + 5 * a;
 #pragma unroll
       for (int k = 0; k < 5; k++) A[k] = Ar[k];
-      const TF* B = (o < kPre) ? &bsm[lrow][o < kPre ? o : 0][0] : LU + 25 * (size_t)op.y;
-      TF* dst = &sm[lrow][(op.z < 0 ? op.x : op.z) - s0][5 * a];
+      const TF* B = (o < kPre) ? bsm(lrow, o) : LU + 25 * (size_t)op.y;
+      TF* dst = sm(lrow, (op.z < 0 ? op.x : op.z) - s0) + 5 * a;
 #pragma unroll
       for (int b = 0; b < 5; b++) {
         TF acc = 0;
@@ -447,7 +452,7 @@ __global__ void __launch_bounds__(kT) k_ilu_factor(
       }
     }
 #pragma unroll
-    for (int b = 0; b < 5; b++) D[b] = sm[lrow][sd - s0][5 * a + b];
+    for (int b = 0; b < 5; b++) D[b] = sm(lrow, sd - s0)[5 * a + b];
   }
   const int base = lane - a;
   bool ok = true;
@@ -471,12 +476,12 @@ __global__ void __launch_bounds__(kT) k_ilu_factor(
   if (!active) return;
   if (!ok) atomicMin(ierr, p + 1);
 #pragma unroll
-  for (int b = 0; b < 5; b++) sm[lrow][sd - s0][5 * a + b] = D[b];
+  for (int b = 0; b < 5; b++) sm(lrow, sd - s0)[5 * a + b] = D[b];
   const int nb = prow[p + 1] - s0;
   for (int b = 0; b < nb; b++) {
     TF* dst = LU + 25 * (size_t)(s0 + b) + 5 * a;
 #pragma unroll
-    for (int k = 0; k < 5; k++) dst[k] = sm[lrow][b][5 * a + k];
+    for (int k = 0; k < 5; k++) dst[k] = sm(lrow, b)[5 * a + k];
   }
 }
 
