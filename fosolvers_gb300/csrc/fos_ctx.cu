@@ -32,7 +32,8 @@ fos_ctx::~fos_ctx() {
   void* ptrs[] = {d_old2new, d_new2old, d_faceLR, d_faceNA, d_faceNA32, d_crow, d_cent, d_invV,
                   d_bcT, d_bcP, d_W, d_Whl, d_ell, d_F, d_stage, d_y, d_f, d_z, d_red, d_scal,
                   d_flag, d_prow, d_pcol, d_pdiag, d_cdiag, d_ipos, d_ord, d_fslot, d_Jraw,
-                  d_LU, d_LU32, d_lrows_f, d_lrows_b, d_upd_ptr, d_upd, d_ilu_tmp, d_Jb, d_ierr};
+                  d_LU, d_LU32, d_lrows_f, d_lrows_b, d_upd_ptr, d_upd, d_ilu_tmp, d_Jb, d_ierr,
+                  d_closure32};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h_scal) cudaFreeHost(h_scal);
@@ -284,6 +285,30 @@ extern "C" int fos_ctx_create(fos_ctx** out, int nC, int nE, int nPi, int nPb, c
     for (int e = crow[i]; e < crow[i + 1]; e++) ell[(size_t)c->ell_w * i + (e - crow[i])] = cent[e];
   std::vector<double> invV(nC);
   for (int i = 0; i < nC; i++) invV[c->old2new[i]] = 1.0 / v[i];
+  // closure vector of every cell, sum over its faces of the outward aP n.  The FP32 flux
+  // writes each face flow as the cell's own flux aP F(u_c).n plus a difference and drops the
+  // own-flux part, whose sum is F(u_c).S_c: zero for cells with planar faces, not for
+  // hexahedra with warped faces (the quad area vectors do not close), where it is restored
+  std::vector<double> S(3 * (size_t)nC, 0.0);
+  double amax = 0.0;
+  for (int f = 0; f < nP; f++) {
+    const double* an = &faceNA[2 * (size_t)f].x;  // nx, ny, nz, aP
+    const double a = an[3];
+    amax = std::max(amax, a);
+    for (int d = 0; d < 3; d++) {
+      S[3 * (size_t)faceLR[f].x + d] += a * an[d];
+      if (f < nPi) S[3 * (size_t)faceLR[f].y + d] -= a * an[d];
+    }
+  }
+  double smax = 0.0;
+  for (double x : S) smax = std::max(smax, std::fabs(x));
+  if (smax > 1e-12 * amax) {
+    std::vector<float4> S32(nC);
+    for (int i = 0; i < nC; i++)
+      S32[i] = make_float4((float)S[3 * (size_t)i], (float)S[3 * (size_t)i + 1],
+                           (float)S[3 * (size_t)i + 2], 0.0f);
+    FOS_TRY(upload(&c->d_closure32, S32.data(), nC));
+  }
 
   FOS_TRY(upload(&c->d_old2new, c->old2new.data(), nC));
   FOS_TRY(upload(&c->d_new2old, c->new2old.data(), nC));

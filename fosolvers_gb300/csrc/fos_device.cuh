@@ -2,9 +2,16 @@
 #pragma once
 #include "fos_internal.h"
 
+// x^e for x > 0 as exp(e ln x).  The isentropic ratios below have x = 1 + (g-1)/2 M^2 >= 1;
+// inline exp and log keep the ghost state free of function calls (pow is a called routine).
+__device__ __forceinline__ double pow_pos(double x, double e) { return exp(e * log(x)); }
+
 // Ghost conserved state of a boundary face (foeuler.f90:209-330); U = interior
-// conserved (rho, mx, my, mz, E), n = unit normal out of the interior cell.
-static __device__ __noinline__ void ghost_state(int type, const double* __restrict__ bp, const double U[5],
+// conserved (rho, mx, my, mz, E), n = unit normal out of the interior cell.  Inlined into
+// each boundary kernel: as a called function (with the called pow) it raised "illegal
+// instruction" faults from kernels allocated fewer registers (78-80) than the call chain
+// used, on the condition types that reach pow.
+__device__ __forceinline__ void ghost_state(int type, const double* __restrict__ bp, const double U[5],
                             double nx, double ny, double nz, double g, double r, double G[5]) {
   const double gm1 = g - 1.0;
   switch (type) {
@@ -22,7 +29,7 @@ static __device__ __noinline__ void ghost_state(int type, const double* __restri
       double q2 = u0 * u0 + u1 * u1 + u2 * u2;
       double TG = TtG - 0.5 * gm1 / g / r * q2;
       double Mach = sqrt(q2) / sqrt(g * r * TG);
-      double pG = ptG * pow(1.0 + 0.5 * gm1 * Mach * Mach, -g / gm1);
+      double pG = ptG * pow_pos(1.0 + 0.5 * gm1 * Mach * Mach, -g / gm1);
       double rG = pG / r / TG;
       if (Mach < 1.0) {
         double ui0 = U[1] / U[0], ui1 = U[2] / U[0], ui2 = U[3] / U[0];
@@ -31,7 +38,7 @@ static __device__ __noinline__ void ghost_state(int type, const double* __restri
         q2 = u0 * u0 + u1 * u1 + u2 * u2;
         TG = TtG - 0.5 * gm1 / g / r * q2;
         Mach = sqrt(q2) / sqrt(g * r * TG);
-        pG = ptG * pow(1.0 + 0.5 * gm1 * Mach * Mach, -g / gm1);
+        pG = ptG * pow_pos(1.0 + 0.5 * gm1 * Mach * Mach, -g / gm1);
         rG = pG / r / TG;
       }
       G[0] = rG; G[1] = rG * u0; G[2] = rG * u1; G[3] = rG * u2;
@@ -62,17 +69,17 @@ static __device__ __noinline__ void ghost_state(int type, const double* __restri
         double sN = nx * ui0 + ny * ui1 + nz * ui2;
         ut0 = ui0 - nx * sN; ut1 = ui1 - ny * sN; ut2 = ui2 - nz * sN;
         Mach = sqrt(uu) / sqrt(g / rm * gm1 * (Em - 0.5 * uu * rm));
-        ptG = gm1 * (Em - 0.5 * uu * rm) * pow(1.0 + 0.5 * gm1 * Mach * Mach, g / gm1);
+        ptG = gm1 * (Em - 0.5 * uu * rm) * pow_pos(1.0 + 0.5 * gm1 * Mach * Mach, g / gm1);
       } else {
         ut0 = g0 - un0; ut1 = g1 - un1; ut2 = g2 - un2;
         Mach = sqrt(g0 * g0 + g1 * g1 + g2 * g2) / sqrt(g * r * TG);
-        ptG = pG * pow(1.0 + 0.5 * gm1 * Mach * Mach, g / gm1);
+        ptG = pG * pow_pos(1.0 + 0.5 * gm1 * Mach * Mach, g / gm1);
       }
       double u0 = un0 + ut0, u1 = un1 + ut1, u2 = un2 + ut2;
       double q2 = u0 * u0 + u1 * u1 + u2 * u2;
       TG = a * a / g / r;
       Mach = sqrt(q2) / a;
-      pG = ptG * pow(1.0 + 0.5 * gm1 * Mach * Mach, -g / gm1);
+      pG = ptG * pow_pos(1.0 + 0.5 * gm1 * Mach * Mach, -g / gm1);
       double rG = pG / r / TG;
       G[0] = rG; G[1] = rG * u0; G[2] = rG * u1; G[3] = rG * u2;
       G[4] = rG * (1.0 / gm1 * r * TG + 0.5 * q2);

@@ -970,6 +970,10 @@ int fos_gnn_precond(fos_ctx* c, const double* y, const double* r, double gamma, 
 
 extern "C" int fos_ctx_attach_gnn(fos_ctx* c, fos_gnn* g) {
   if (!c) return -1;
+  if (g && c->ell_w != 4) {  // the network's message passing reads 4 neighbour slots
+    fos_set_error("learned preconditioner: tetrahedral grids only");
+    return -2;
+  }
   c->gnn = g;
   return 0;
 }

@@ -58,6 +58,8 @@ struct fos_ctx {
   int* d_ell = nullptr;       // [ell_w*nC] the same entries, fixed width, -1 = empty
   int ell_w = 4;
   double* d_invV = nullptr;   // [nC]
+  float4* d_closure32 = nullptr;  // [nC] sum of outward aP n over the cell's faces (FP32 flux);
+                                  // null when every cell is closed
   int* d_bcT = nullptr;       // [nBC]
   double* d_bcP = nullptr;    // [maxP*nBC]
 

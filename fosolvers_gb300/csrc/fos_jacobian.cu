@@ -163,6 +163,29 @@ __device__ __forceinline__ void ghost_prim(int f, int nC, int2 lr, const double*
   R.s = sqrt(G[0]);
 }
 
+// Ghost-side primitives (u, v, w, H, sqrt(rho)) of the boundary faces for k_jac_cell32, FP64,
+// written into the face slots of the flow array (6 doubles per face; the residual rewrites
+// them before it reads them), from the FP32 normals widened as the FP32 assembly uses them.
+__global__ void __launch_bounds__(kT) k_jac_ghost64(int nFi, int nF, int nC,
+                                                    const int2* __restrict__ faceLR,
+                                                    const float4* __restrict__ faceNA32,
+                                                    const double* __restrict__ y,
+                                                    const int* __restrict__ bcT,
+                                                    const double* __restrict__ bcP, int maxP,
+                                                    double g, double r, double* __restrict__ Gb) {
+  const int f = nFi + blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nF) return;
+  const int2 lr = __ldg(faceLR + f);
+  const float4 na = __ldg(faceNA32 + f);
+  Prim R;
+  ghost_prim(f, nC, lr, y, bcT, bcP, maxP, f2d_bits(na.x), f2d_bits(na.y), f2d_bits(na.z), g, r,
+             R);
+  double2* G2 = reinterpret_cast<double2*>(Gb + 6 * (size_t)f);
+  G2[0] = make_double2(R.u, R.v);
+  G2[1] = make_double2(R.w, R.H);
+  G2[2] = make_double2(R.s, 0.0);
+}
+
 // FP64 form: FP64 primitives and geometry
 template <typename TJ>
 __global__ void __launch_bounds__(kT) k_jac_face(int nFi, int nF, int nC,
@@ -216,8 +239,8 @@ __global__ void __launch_bounds__(64) k_jac_cell32(
     int nC, int nFi, const int* __restrict__ ipos, const int* __restrict__ prow,
     const int* __restrict__ cdiag, const int* __restrict__ ell, const int2* __restrict__ faceLR,
     const float4* __restrict__ faceNA32, const int* __restrict__ fslot,
-    const float* __restrict__ Whl, const double* __restrict__ y, const int* __restrict__ bcT,
-    const double* __restrict__ bcP, int maxP, double g, double r, float* __restrict__ J) {
+    const float* __restrict__ Whl, const double* __restrict__ Gb, double g,
+    float* __restrict__ J) {
   constexpr int kRow = (kW + 1) * 25;  // floats of a full block row
   __shared__ float stg[2][32][kRow];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -245,11 +268,11 @@ __global__ void __launch_bounds__(64) k_jac_cell32(
       PrimT<float> Q;
       if (f < nFi) {
         Q = load_prim_f32(Whl, isR ? lr.x : lr.y);
-      } else {
-        Prim R;
-        ghost_prim(f, nC, lr, y, bcT, bcP, maxP, f2d_bits(na.x), f2d_bits(na.y), f2d_bits(na.z),
-                   g, r, R);
-        Q = {{d2f_trunc(R.u), d2f_trunc(R.v), d2f_trunc(R.w)}, d2f_trunc(R.H), d2f_trunc(R.s)};
+      } else {  // ghost primitives of k_jac_ghost64
+        const double2* G2 = reinterpret_cast<const double2*>(Gb + 6 * (size_t)f);
+        const double2 a0 = __ldg(G2), a1 = __ldg(G2 + 1), a2 = __ldg(G2 + 2);
+        Q = {{d2f_trunc(a0.x), d2f_trunc(a0.y), d2f_trunc(a1.x)}, d2f_trunc(a1.y),
+             d2f_trunc(a2.x)};
       }
       const PrimT<float>& L = (f < nFi && isR) ? Q : P;
       const PrimT<float>& R = (f < nFi && isR) ? P : Q;
@@ -736,19 +759,21 @@ static int jac_assemble_t(fos_ctx* c, const double* y) {
   TJ* Jb = reinterpret_cast<TJ*>(c->d_Jb);
   if constexpr (sizeof(TJ) == sizeof(float)) {
     if (int rc = fos_prim_hl_launch(c, y)) return rc;
+    if (c->nFb)
+      fos_launch(c, k_jac_ghost64, nb(c->nFb), kT, c->nFi, c->nF, c->nC,
+                 (const int2*)c->d_faceLR, (const float4*)c->d_faceNA32, y,
+                 (const int*)c->d_bcT, (const double*)c->d_bcP, c->maxP, c->gamm, c->r, c->d_F);
     const int grid = (c->nC + 63) / 64;
     if (c->ell_w == 4)
       fos_launch(c, k_jac_cell32<4>, grid, 64, c->nC, c->nFi, (const int*)c->d_ipos,
                  (const int*)c->d_prow, (const int*)c->d_cdiag, (const int*)c->d_ell,
                  (const int2*)c->d_faceLR, (const float4*)c->d_faceNA32, (const int*)c->d_fslot,
-                 (const float*)c->d_Whl, y, (const int*)c->d_bcT, (const double*)c->d_bcP,
-                 c->maxP, c->gamm, c->r, J);
+                 (const float*)c->d_Whl, (const double*)c->d_F, c->gamm, J);
     else
       fos_launch(c, k_jac_cell32<6>, grid, 64, c->nC, c->nFi, (const int*)c->d_ipos,
                  (const int*)c->d_prow, (const int*)c->d_cdiag, (const int*)c->d_ell,
                  (const int2*)c->d_faceLR, (const float4*)c->d_faceNA32, (const int*)c->d_fslot,
-                 (const float*)c->d_Whl, y, (const int*)c->d_bcT, (const double*)c->d_bcP,
-                 c->maxP, c->gamm, c->r, J);
+                 (const float*)c->d_Whl, (const double*)c->d_F, c->gamm, J);
     FOS_LAUNCH_CHECK();
     return 0;
   } else {

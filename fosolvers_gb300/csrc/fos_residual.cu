@@ -14,8 +14,8 @@
 // The FP32-flux variant (FOS_FLUX_FP32) computes the same flow in FP32, in flux-difference
 // form, from per-cell FP32 (hi, lo) primitive pairs (k_prim_hl), and fuses the interior
 // faces into the cell gather (k_cell32: each interior face evaluated by both of its cells,
-// bit-identically); boundary faces go through k_face32b (ghost state in FP64).  Sums are in
-// FP64 in both variants.
+// bit-identically); boundary faces go through k_bface32 (ghost state and flow in FP64,
+// stored as the difference from the cell's own flux).  Sums are in FP64 in both variants.
 #include <cmath>
 #include <mutex>
 #include <string>
@@ -308,24 +308,20 @@ __device__ __forceinline__ void roe_split_mj(float rm, float dr, float um, float
   dw[0] = h * d0; dw[1] = h * d1; dw[2] = h * d2; dw[3] = h * d3; dw[4] = h * d4;
 }
 
-__device__ __forceinline__ void store_f32(float* __restrict__ F, int f, const float dF[5],
-                                          const float dw[5]) {
-  float4* F4 = reinterpret_cast<float4*>(F + 12 * (size_t)f);  // AoS (dF, dw) pairs, 48 B
-  F4[0] = make_float4(dF[0], dw[0], dF[1], dw[1]);
-  F4[1] = make_float4(dF[2], dw[2], dF[3], dw[3]);
-  F4[2] = make_float4(dF[4], dw[4], 0.0f, 0.0f);
-}
-
-// boundary faces [nFi, nF): ghost state and means/jumps in FP64 (1% of the faces)
-__global__ void __launch_bounds__(kThreads) k_face32b(
-    int nFi, int nF, int nC, const int2* __restrict__ faceLR, const float4* __restrict__ faceNA,
+// Boundary faces [nFi, nF) of the FP32 flux, all in FP64 (1% of the faces): the Roe flow of
+// k_face64 (interior state, ghost state, both primitives from the conserved variables)
+// minus the interior cell's own flux aP F(u_L).n, i.e. the flow in the difference form that
+// k_cell32 accumulates.  Stored as FP64 (5 of the face's 6 slots of F).
+__global__ void __launch_bounds__(kThreads) k_bface32(
+    int nFi, int nF, int nC, const int2* __restrict__ faceLR, const double2* __restrict__ faceNA,
     const double* __restrict__ y, const double* __restrict__ v, const double* __restrict__ d_s,
     const int* __restrict__ bcT, const double* __restrict__ bcP, int maxP, double g, double r,
-    float* __restrict__ F) {
+    double* __restrict__ F) {
   const int f = nFi + blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nF) return;
   const int2 lr = __ldg(faceLR + f);
-  const float4 na = __ldg(faceNA + f);
+  const double2 n01 = __ldg(faceNA + 2 * (size_t)f), n2a = __ldg(faceNA + 2 * (size_t)f + 1);
+  const double nx = n01.x, ny = n01.y, nz = n2a.x, aP = n2a.y;
   double U[5], G[5];
 #pragma unroll
   for (int q = 0; q < 5; q++) U[q] = y[(size_t)q * nC + lr.x];
@@ -336,18 +332,17 @@ __global__ void __launch_bounds__(kThreads) k_face32b(
   }
   const int row = lr.y;
   const int type = row > 0 ? bcT[row - 1] : FOS_BC_WALL;
-  ghost_state(type, row > 0 ? bcP + (size_t)maxP * (row - 1) : nullptr, U, na.x, na.y, na.z, g,
-              r, G);
+  ghost_state(type, row > 0 ? bcP + (size_t)maxP * (row - 1) : nullptr, U, nx, ny, nz, g, r, G);
   P64 L, R;
   prim_from_cons(U[0], U[1], U[2], U[3], U[4], g - 1.0, L);
   prim_from_cons(G[0], G[1], G[2], G[3], G[4], g - 1.0, R);
-  float dF[5], dw[5];
-  roe_split_mj((float)(0.5 * (L.rho + R.rho)), (float)(R.rho - L.rho), (float)(0.5 * (L.u + R.u)),
-               (float)(R.u - L.u), (float)(0.5 * (L.v + R.v)), (float)(R.v - L.v),
-               (float)(0.5 * (L.w + R.w)), (float)(R.w - L.w), (float)(0.5 * (L.H + R.H)),
-               (float)(R.H - L.H), (float)(R.p - L.p), (float)L.s, (float)R.s, na.x, na.y, na.z,
-               na.w, (float)(g - 1.0), dF, dw);
-  store_f32(F, f, dF, dw);
+  double flow[5];
+  roe_flow64(L, R, nx, ny, nz, aP, g - 1.0, flow);
+  const double m = aP * L.rho * (L.u * nx + L.v * ny + L.w * nz), pa = aP * L.p;
+  double2* F2 = reinterpret_cast<double2*>(F + 6 * (size_t)f);
+  F2[0] = make_double2(flow[0] - m, flow[1] - (m * L.u + pa * nx));
+  F2[1] = make_double2(flow[2] - (m * L.v + pa * ny), flow[3] - (m * L.w + pa * nz));
+  F2[2] = make_double2(flow[4] - m * L.H, 0.0);
 }
 
 // Fused interior flux + cell gather for the FP32 flux (one pass, no face-flow array for
@@ -356,14 +351,16 @@ __global__ void __launch_bounds__(kThreads) k_face32b(
 // jumps, FP32 instructions only, so
 // the two cells of a face compute bit-identical (dF, dw) and the scheme stays exactly
 // conservative; the cell then takes -(dF - dw) (cell is L) or -(dF + dw) (cell is R) in
-// FP64, in ascending ELL order.  Boundary faces read the flows k_face32b wrote.  Each face
-// is evaluated twice -- cheap FP32 arithmetic in exchange for the 2 x 48 B per face a
-// face-flow array costs in HBM traffic.
+// FP64, in ascending ELL order.  Boundary faces read the FP64 differences k_bface32 wrote.
+// Each face is evaluated twice -- cheap FP32 arithmetic in exchange for the 2 x 48 B per face
+// a face-flow array costs in HBM traffic.  Cells that are not closed (Sc non-null: warped
+// faces) also take the own-flux sum the difference form leaves out, -F(u_c).S_c.
 template <int kW>
 __global__ void __launch_bounds__(kThreads) k_cell32(
     int nC, int nFi, const int* __restrict__ ell, const int2* __restrict__ faceLR,
     const float4* __restrict__ faceNA, const float* __restrict__ W, float gm1,
-    const float* __restrict__ Fb, const double* __restrict__ invV, int mode,
+    const double* __restrict__ Fb, const float4* __restrict__ Sc,
+    const double* __restrict__ invV, int mode,
     const double* __restrict__ vv, const double* __restrict__ fy, const double* __restrict__ d_s,
     double a, double b, double* __restrict__ out, int* __restrict__ flag) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -380,35 +377,44 @@ __global__ void __launch_bounds__(kThreads) k_cell32(
     if (k > 0 && e[k] < 0) continue;
     const int f = e[k] >> 1;
     const bool isR = e[k] & 1;
+    if (f >= nFi) {  // boundary face (cell is L): the FP64 difference of k_bface32
+      const double2* F2 = reinterpret_cast<const double2*>(Fb + 6 * (size_t)f);
+      const double2 a0 = __ldg(F2), a1 = __ldg(F2 + 1), a2 = __ldg(F2 + 2);
+      const double d[5] = {a0.x, a0.y, a1.x, a1.y, a2.x};
+#pragma unroll
+      for (int q = 0; q < 5; q++) acc[q] = k == 0 ? -d[q] : acc[q] - d[q];
+      continue;
+    }
     const float sw = isR ? 1.0f : -1.0f;  // R: -(dF + dw), L: -(dF - dw)
     float dF[5], dw[5];
-    if (f < nFi) {
-      const int2 lr = __ldg(faceLR + f);
-      const float4 na = __ldg(faceNA + f);
-      PHL Q;
-      load_hl(W, isR ? lr.x : lr.y, Q);
-      const PHL& L = isR ? Q : P;
-      const PHL& R = isR ? P : Q;
-      float m[6], d[6];
+    const int2 lr = __ldg(faceLR + f);
+    const float4 na = __ldg(faceNA + f);
+    PHL Q;
+    load_hl(W, isR ? lr.x : lr.y, Q);
+    const PHL& L = isR ? Q : P;
+    const PHL& R = isR ? P : Q;
+    float m[6], d[6];
 #pragma unroll
-      for (int j = 0; j < 6; j++) {
-        m[j] = 0.5f * (L.h[j] + R.h[j]) + 0.5f * (L.l[j] + R.l[j]);
-        d[j] = (R.h[j] - L.h[j]) + (R.l[j] - L.l[j]);
-      }
-      roe_split_mj(m[0], d[0], m[1], d[1], m[2], d[2], m[3], d[3], m[4], d[4], d[5], L.s, R.s,
-                   na.x, na.y, na.z, na.w, gm1, dF, dw);
-    } else {
-      const float4* F4 = reinterpret_cast<const float4*>(Fb + 12 * (size_t)f);
-      const float4 a0 = __ldg(F4), a1 = __ldg(F4 + 1), a2 = __ldg(F4 + 2);
-      dF[0] = a0.x; dw[0] = a0.y; dF[1] = a0.z; dw[1] = a0.w;
-      dF[2] = a1.x; dw[2] = a1.y; dF[3] = a1.z; dw[3] = a1.w;
-      dF[4] = a2.x; dw[4] = a2.y;
+    for (int j = 0; j < 6; j++) {
+      m[j] = 0.5f * (L.h[j] + R.h[j]) + 0.5f * (L.l[j] + R.l[j]);
+      d[j] = (R.h[j] - L.h[j]) + (R.l[j] - L.l[j]);
     }
+    roe_split_mj(m[0], d[0], m[1], d[1], m[2], d[2], m[3], d[3], m[4], d[4], d[5], L.s, R.s,
+                 na.x, na.y, na.z, na.w, gm1, dF, dw);
 #pragma unroll
     for (int q = 0; q < 5; q++) {
       const float term = fmaf(sw, dw[q], dF[q]);
       acc[q] = k == 0 ? f2d_bits(-term) : acc[q] - f2d_bits(term);
     }
+  }
+  if (Sc) {  // own flux through the closure vector: rho u.S, rho u u.S + p S, rho H u.S
+    const float4 S = __ldg(Sc + c);
+    const float t = P.h[0] * (P.h[1] * S.x + P.h[2] * S.y + P.h[3] * S.z);
+    acc[0] -= f2d_bits(t);
+    acc[1] -= f2d_bits(fmaf(t, P.h[1], P.h[5] * S.x));
+    acc[2] -= f2d_bits(fmaf(t, P.h[2], P.h[5] * S.y));
+    acc[3] -= f2d_bits(fmaf(t, P.h[3], P.h[5] * S.z));
+    acc[4] -= f2d_bits(t * P.h[4]);
   }
   gather_epilogue(nC, c, acc, __ldg(invV + c), mode, vv, fy, d_s, a, b, out, flag);
 }
@@ -476,20 +482,19 @@ int fos_residual_launch(fos_ctx* c, const double* y, const double* v, const doub
   if (c->flags & FOS_FLUX_FP32) {
     fos_launch(c, k_prim_hl, nblk(c->nC), kThreads, c->nC, y, v, d_s, gm1, c->d_Whl);
     if (c->nFb)
-      fos_launch(c, k_face32b, nblk(c->nFb), kThreads, c->nFi, c->nF, c->nC,
-                 (const int2*)c->d_faceLR, (const float4*)c->d_faceNA32, y, v, d_s,
-                 (const int*)c->d_bcT, (const double*)c->d_bcP, c->maxP, c->gamm, c->r,
-                 reinterpret_cast<float*>(c->d_F));
+      fos_launch(c, k_bface32, nblk(c->nFb), kThreads, c->nFi, c->nF, c->nC,
+                 (const int2*)c->d_faceLR, (const double2*)c->d_faceNA, y, v, d_s,
+                 (const int*)c->d_bcT, (const double*)c->d_bcP, c->maxP, c->gamm, c->r, c->d_F);
     if (c->ell_w == 4)
       fos_launch(c, k_cell32<4>, nblk(c->nC), kThreads, c->nC, c->nFi, (const int*)c->d_ell,
                  (const int2*)c->d_faceLR, (const float4*)c->d_faceNA32, (const float*)c->d_Whl,
-                 (float)gm1, reinterpret_cast<const float*>(c->d_F), (const double*)c->d_invV,
-                 mode, v, fy, d_s, a, b, out, c->d_flag);
+                 (float)gm1, (const double*)c->d_F, (const float4*)c->d_closure32,
+                 (const double*)c->d_invV, mode, v, fy, d_s, a, b, out, c->d_flag);
     else
       fos_launch(c, k_cell32<6>, nblk(c->nC), kThreads, c->nC, c->nFi, (const int*)c->d_ell,
                  (const int2*)c->d_faceLR, (const float4*)c->d_faceNA32, (const float*)c->d_Whl,
-                 (float)gm1, reinterpret_cast<const float*>(c->d_F), (const double*)c->d_invV,
-                 mode, v, fy, d_s, a, b, out, c->d_flag);
+                 (float)gm1, (const double*)c->d_F, (const float4*)c->d_closure32,
+                 (const double*)c->d_invV, mode, v, fy, d_s, a, b, out, c->d_flag);
   } else {
     fos_launch(c, k_prim64, nblk(c->nC), kThreads, c->nC, y, v, d_s, gm1, c->d_W);
     fos_launch(c, k_face64, nblk(c->nF), kThreads, c->nFi, c->nF, c->nC,
@@ -610,22 +615,22 @@ extern "C" int fos_euler_rhs_dev_static(const fos_ctx* c, double t, const double
   cudaStream_t s = c->stream;
   if (c->flags & FOS_FLUX_FP32) {
     float* Whl = reinterpret_cast<float*>(bytes);
-    float* F = reinterpret_cast<float*>(bytes + kStaticCellBytes);
+    double* F = reinterpret_cast<double*>(bytes + kStaticCellBytes);
     k_prim_hl<<<nblk(c->nC), kThreads, 0, s>>>(c->nC, y, nullptr, nullptr, gm1, Whl);
     if (c->nFb)
-      k_face32b<<<nblk(c->nFb), kThreads, 0, s>>>(c->nFi, c->nF, c->nC, c->d_faceLR,
-                                                  c->d_faceNA32, y, nullptr, nullptr, c->d_bcT,
+      k_bface32<<<nblk(c->nFb), kThreads, 0, s>>>(c->nFi, c->nF, c->nC, c->d_faceLR,
+                                                  c->d_faceNA, y, nullptr, nullptr, c->d_bcT,
                                                   c->d_bcP, c->maxP, c->gamm, c->r, F);
     if (c->ell_w == 4)
       k_cell32<4><<<nblk(c->nC), kThreads, 0, s>>>(c->nC, c->nFi, c->d_ell, c->d_faceLR,
-                                                   c->d_faceNA32, Whl, (float)gm1, F, c->d_invV,
-                                                   0, nullptr, nullptr, nullptr, 0.0, 0.0, ydot,
-                                                   nullptr);
+                                                   c->d_faceNA32, Whl, (float)gm1, F,
+                                                   c->d_closure32, c->d_invV, 0, nullptr,
+                                                   nullptr, nullptr, 0.0, 0.0, ydot, nullptr);
     else
       k_cell32<6><<<nblk(c->nC), kThreads, 0, s>>>(c->nC, c->nFi, c->d_ell, c->d_faceLR,
-                                                   c->d_faceNA32, Whl, (float)gm1, F, c->d_invV,
-                                                   0, nullptr, nullptr, nullptr, 0.0, 0.0, ydot,
-                                                   nullptr);
+                                                   c->d_faceNA32, Whl, (float)gm1, F,
+                                                   c->d_closure32, c->d_invV, 0, nullptr,
+                                                   nullptr, nullptr, 0.0, 0.0, ydot, nullptr);
   } else {
     double* W = reinterpret_cast<double*>(bytes);
     double* F = reinterpret_cast<double*>(bytes + kStaticCellBytes);

@@ -242,7 +242,8 @@ class FOEuler:
         return rc, st.as_dict(), ast.as_dict()
 
     def attach_gnn(self, gnn):
-        """Learned preconditioner used by bdf_run / linear_solve when opts.precond == 2."""
+        """Learned preconditioner used by bdf_run / linear_solve when opts.precond >= 2
+        (tetrahedral grids only: raises on a grid with hexahedra)."""
         check(_lib.lib().fos_ctx_attach_gnn(self._h, gnn.handle if gnn is not None else None),
               "attach_gnn")
         self._gnn = gnn

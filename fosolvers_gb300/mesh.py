@@ -23,7 +23,7 @@ from itertools import permutations
 
 import numpy as np
 
-TET, TRI = 20, 10
+TET, TRI, HEX, QUAD = 20, 10, 21, 11
 GID_XMIN, GID_XMAX, GID_YMIN, GID_YMAX, GID_ZMIN, GID_ZMAX = 1, 2, 3, 4, 5, 6
 
 
@@ -32,7 +32,7 @@ class Mesh:
     pN: np.ndarray          # (nN, 3) float64 node positions
     sE: np.ndarray          # (nE,) int32 shape codes
     nNE: np.ndarray         # (nE,) int32 nodes per element
-    iNE: np.ndarray         # (nE, 4) int32 1-based node ids (row = element)
+    iNE: np.ndarray         # (nE, m) int32 1-based node ids (row = element; m = 4, or 8 with hexes)
     gid: np.ndarray         # (nE,) int32 group ids
     nC: int
     dims: tuple = ()
@@ -50,7 +50,7 @@ class Mesh:
     def centroids(self) -> np.ndarray:
         idx = self.iNE - 1
         cnt = self.nNE[:, None].astype(np.float64)
-        mask = (np.arange(4)[None, :] < self.nNE[:, None])
+        mask = (np.arange(idx.shape[1])[None, :] < self.nNE[:, None])
         pts = self.pN[np.where(mask, idx, 0)] * mask[..., None]
         return pts.sum(axis=1) / cnt
 
@@ -74,7 +74,12 @@ def _kuhn_tets() -> np.ndarray:
 
 
 def box_mesh(nx: int, ny: int, nz: int, extent=(1.0, 1.0, 1.0), jitter: float = 0.1,
-             seed: int = 0, bump: bool = False) -> Mesh:
+             seed: int = 0, bump: bool = False, cells: str = "tet") -> Mesh:
+    """The box of nx x ny x nz hexahedra; cells="tet" cuts each into the 6 Kuhn
+    tetrahedra with TRI facets, cells="hex" keeps the HEX cells (Gmsh node order:
+    bottom face counter-clockwise, then the top face) with QUAD facets."""
+    if cells not in ("tet", "hex"):
+        raise ValueError(f"cells must be 'tet' or 'hex', not {cells!r}")
     Lx, Ly, Lz = extent
     hx, hy, hz = Lx / nx, Ly / ny, Lz / nz
     ix, iy, iz = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), np.arange(nz + 1), indexing="ij")
@@ -99,6 +104,9 @@ def box_mesh(nx: int, ny: int, nz: int, extent=(1.0, 1.0, 1.0), jitter: float = 
     hi, hj, hk = hi.reshape(-1), hj.reshape(-1), hk.reshape(-1)
     corners = np.stack([nid(hi + (k & 1), hj + ((k >> 1) & 1), hk + ((k >> 2) & 1))
                         for k in range(8)], axis=1)  # (nH, 8)
+    if cells == "hex":
+        return _hex_box(pN, corners, nid, nx, ny, nz, extent,
+                        {"jitter": jitter, "seed": seed, "bump": bump, "cells": "hex"})
     kt = _kuhn_tets()
     tets = corners[:, kt].reshape(-1, 4)  # (6 nH, 4)
     # boundary triangles: quad (a, b, c, d) with the min->max diagonal, split as in the Kuhn tets
@@ -137,6 +145,43 @@ def box_mesh(nx: int, ny: int, nz: int, extent=(1.0, 1.0, 1.0), jitter: float = 
     gid = np.concatenate([np.zeros(nC, np.int32), gids.astype(np.int32)])
     return Mesh(pN=pN, sE=sE, nNE=nNE, iNE=iNE, gid=gid, nC=nC, dims=(nx, ny, nz),
                 extent=tuple(extent), meta={"jitter": jitter, "seed": seed, "bump": bump})
+
+
+def _hex_box(pN, corners, nid, nx, ny, nz, extent, meta) -> Mesh:
+    """HEX cells and QUAD side facets of the box; corner k of a hex is (k & 1, k >> 1 & 1,
+    k >> 2) in its i, j, k offsets, so Gmsh order is corners 0, 1, 3, 2, 4, 5, 7, 6."""
+    hexes = corners[:, [0, 1, 3, 2, 4, 5, 7, 6]]
+    quads, gids = [], []
+
+    def side(fixed_axis, fixed_val, gid):
+        axes = [a for a in range(3) if a != fixed_axis]
+        n1, n2 = [nx, ny, nz][axes[0]], [nx, ny, nz][axes[1]]
+        u, v = np.meshgrid(np.arange(n1), np.arange(n2), indexing="ij")
+        u, v = u.reshape(-1), v.reshape(-1)
+
+        def node(du, dv):
+            ijk = [None, None, None]
+            ijk[fixed_axis] = np.full_like(u, fixed_val)
+            ijk[axes[0]] = u + du
+            ijk[axes[1]] = v + dv
+            return nid(*ijk)
+
+        quads.append(np.stack([node(0, 0), node(1, 0), node(1, 1), node(0, 1)], axis=1))
+        gids.append(np.full(u.size, gid))
+
+    side(0, 0, GID_XMIN); side(0, nx, GID_XMAX)
+    side(1, 0, GID_YMIN); side(1, ny, GID_YMAX)
+    side(2, 0, GID_ZMIN); side(2, nz, GID_ZMAX)
+    quads = np.concatenate(quads)
+    nC, nF = hexes.shape[0], quads.shape[0]
+    iNE = np.zeros((nC + nF, 8), np.int32)
+    iNE[:nC] = hexes + 1
+    iNE[nC:, :4] = quads + 1
+    sE = np.concatenate([np.full(nC, HEX, np.int32), np.full(nF, QUAD, np.int32)])
+    nNE = np.concatenate([np.full(nC, 8, np.int32), np.full(nF, 4, np.int32)])
+    gid = np.concatenate([np.zeros(nC, np.int32), np.concatenate(gids).astype(np.int32)])
+    return Mesh(pN=pN, sE=sE, nNE=nNE, iNE=iNE, gid=gid, nC=nC, dims=(nx, ny, nz),
+                extent=tuple(extent), meta=meta)
 
 
 # ------------------------------------------------------------------ initial states

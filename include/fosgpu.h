@@ -167,7 +167,8 @@ int fos_gnn_loss_grad_dev(fos_gnn* g, fos_ctx* ctx, const double* y, const doubl
 int fos_gnn_get_grad(const fos_gnn* g, float* host);
 int fos_gnn_adam_step(fos_gnn* g, float lr, float beta1, float beta2, float eps,
                       float grad_scale);
-/* network used by fos_bdf_run when opts.precond == 2 (not owned by the context) */
+/* network used by fos_bdf_run when opts.precond >= 2 (not owned by the context); g = NULL
+   detaches.  Returns -2 on a grid with hexahedra (the network reads 4 neighbour slots). */
 int fos_ctx_attach_gnn(fos_ctx* ctx, fos_gnn* g);
 
 /* ------------------------------------------------------------------ driver */

@@ -52,6 +52,30 @@ class Case:
         return f
 
 
+def hex_workload(nx: int = 10, seed: int = 0) -> M.Workload:
+    """nx x (nx - 2) x (nx - 4) jittered hexahedra (HEX cells, QUAD facets), the sinusoidal
+    state, walls, BDF2 dt = 5e-4 x 6 steps: the six-face cell kernels' case."""
+    m = M.box_mesh(nx, nx - 2, nx - 4, jitter=0.1, seed=seed, cells="hex")
+    st = M.sine_state(m.centroids(), seed)
+    return M.Workload(f"hex{nx}", m, st, np.zeros(0, np.int32), np.zeros(0, np.int32),
+                      np.zeros((0, 5)), order=2, dt=5e-4, nsteps=6)
+
+
+def with_all_conditions(wl: M.Workload) -> M.Workload:
+    """Every non-UDF condition of setBC (foeuler.f90:217-325) on the six box sides: static
+    inflow (subsonic: interior momentum), total inflow, outflow (imposed p), far field,
+    zero-gradient outflow, wall."""
+    wl.bc_gid = np.array([1, 2, 3, 4, 5, 6], np.int32)
+    wl.bc_type = np.array([10, 11, 20, 30, 21, 0], np.int32)
+    wl.bc_param = np.array([[1.0, 1.0, 0.3, 0.0, 0.0],
+                            [1.2, 1.1, 0.5, 0.1, 0.0],
+                            [0.9, 0, 0, 0, 0],
+                            [1.0, 1.0, 0.2, 0.1, 0.05],
+                            [0, 0, 0, 0, 0],
+                            [0, 0, 0, 0, 0]])
+    return wl
+
+
 def perturbed(y: np.ndarray, nC: int, seed: int, amp: float = 0.05) -> np.ndarray:
     """Smooth-ish random perturbation that keeps rho and p positive."""
     rng = np.random.default_rng(seed)

@@ -9,7 +9,7 @@ import pytest
 
 from fosolvers_gb300 import mesh as M
 from fosolvers_gb300.euler import FLUX_FP32, ILU_COLOR, ILU_FP32
-from helpers import Case, field_errors, rel_err
+from helpers import Case, field_errors, hex_workload, rel_err, with_all_conditions
 from oracle import pyoracle as O
 
 pytestmark = pytest.mark.gpu
@@ -107,3 +107,40 @@ def test_fp32_form_within_1e6(cuda, extra):
     err = field_errors(y, y_ref)
     print("fp32 form sod16", err, st)
     assert max(err["rho"], err["rhou"], err["rhoE"]) <= 1e-6
+
+
+def _bdf_case(name):
+    if name == "hex10":
+        return hex_workload(10, seed=2)
+    if name == "conds6":
+        wl = with_all_conditions(M.make_workload("sod16", scale=6))
+    else:
+        wl = with_all_conditions(hex_workload(8, seed=3))
+    wl.order, wl.dt, wl.nsteps = 2, 2e-3, 6
+    return wl
+
+
+@pytest.mark.parametrize("name", ["hex10", "conds6", "conds-hex8"])
+def test_cells_and_conditions_bdf2_match_oracle(cuda, name):
+    """Hexahedral cells (six-face ELL rows, 7-block ILU rows, warped faces) and every
+    condition type: FP64 within 1e-10 of the oracle's BDF run, and the FP32 flux +
+    colour-ordered FP32 ILU(0) form within 1e-6 per conserved field."""
+    c = Case(_bdf_case(name))
+    y_ref, st_ref = oracle_run(c)
+    y, st = gpu_run(c)
+    print(name, "fp64", rel_err(y, y_ref), st, st_ref)
+    assert rel_err(y, y_ref) <= 1e-10
+    c32 = Case(_bdf_case(name), flags=FLUX_FP32 | ILU_FP32 | ILU_COLOR)
+    y32, st32 = gpu_run(c32)
+    err = field_errors(y32, y_ref)
+    print(name, "fp32 form", err, st32)
+    assert max(err["rho"], err["rhou"], err["rhoE"]) <= 1e-6
+
+
+def test_learned_preconditioner_refuses_hex_grid(cuda):
+    """The network reads four neighbour slots per cell: attaching it to a grid with
+    hexahedra is an error at attach time, not a failure inside a run."""
+    from fosolvers_gb300.learned import GNN
+    c = Case(hex_workload(6))
+    with pytest.raises(RuntimeError, match="tetrahedral grids only"):
+        c.gpu.attach_gnn(GNN(seed=0))

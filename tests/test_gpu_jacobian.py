@@ -11,13 +11,27 @@ import pytest
 
 from fosolvers_gb300 import mesh as M
 from fosolvers_gb300.euler import ILU_COLOR, ILU_FP32
-from helpers import Case, perturbed, rel_err
+from helpers import Case, hex_workload, perturbed, rel_err, with_all_conditions
 
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(scope="module", params=["sine8", "bump16", "sine8-colour"])
+def _workload(name):
+    if name == "hex8":  # six-face cells: block rows of up to 7 blocks
+        return hex_workload(8, seed=1)
+    if name == "conds6":  # every condition type on the box sides
+        return with_all_conditions(M.make_workload("sod16", scale=6))
+    if name == "conds-hex8":
+        return with_all_conditions(hex_workload(8, seed=1))
+    return M.make_workload("sine96", scale=8, seed=1)
+
+
+@pytest.fixture(scope="module",
+                params=["sine8", "bump16", "sine8-colour", "hex8", "hex8-colour", "conds6"])
 def case(request, cuda):
+    if request.param.startswith("hex") or request.param == "conds6":
+        return Case(_workload(request.param.split("-")[0]),
+                    flags=ILU_COLOR if "colour" in request.param else 0)
     if request.param == "sine8":
         return Case(M.make_workload("sine96", scale=8, seed=1))
     if request.param == "sine8-colour":
@@ -26,7 +40,17 @@ def case(request, cuda):
 
 
 def test_jacobian_blocks_match_oracle(case):
-    c = case
+    _check_blocks(case, 1e-12)
+
+
+@pytest.mark.parametrize("name", ["sine8", "hex8", "conds6", "conds-hex8"])
+def test_fp32_jacobian_blocks(cuda, name):
+    """The cell-centric FP32 assembly (FP32 (hi, lo) primitives, FP32 face arithmetic, FP64
+    ghost states) against the FP64 oracle: every block within 1e-5 of the largest entry."""
+    _check_blocks(Case(_workload(name), flags=ILU_FP32), 1e-5)
+
+
+def _check_blocks(c: Case, tol: float):
     y = perturbed(c.y0, c.nC, 3)
     mf = c.grid.maxFace
     ref = c.oracle.jac(y, mf)  # [cell, col, row]
@@ -44,7 +68,7 @@ def test_jacobian_blocks_match_oracle(case):
         for other, j in blocks:
             s = rowptr[p] + cols.index(pos[other])
             want = ref[cell, 5 * j:5 * j + 5, :].T
-            assert np.abs(val[s] - want).max() <= 1e-12 * scale
+            assert np.abs(val[s] - want).max() <= tol * scale
             nblk += 1
     assert nblk == len(col)
 
@@ -68,7 +92,7 @@ def test_ilu_apply_matches_sparskit(case):
     info = c.gpu.info()
     assert info["nlev_fwd"] >= 2 and info["nlev_bwd"] >= 2
     if c.flags & ILU_COLOR:
-        assert info["nlev_fwd"] <= 6 and info["nlev_bwd"] <= 6
+        assert info["nlev_fwd"] <= c.grid.maxFace + 2 and info["nlev_bwd"] <= c.grid.maxFace + 2
 
 
 def test_pset_jok_reuses_jacobian(case):
@@ -88,8 +112,9 @@ def test_pset_jok_reuses_jacobian(case):
     assert rel_err(z, z_ref) <= 1e-10
 
 
-def test_fp32_ilu_apply(cuda):
-    c = Case(M.make_workload("sine96", scale=8, seed=1), flags=ILU_FP32)
+@pytest.mark.parametrize("name", ["sine8", "hex8"])
+def test_fp32_ilu_apply(cuda, name):
+    c = Case(_workload(name), flags=ILU_FP32)
     y = perturbed(c.y0, c.nC, 4)
     c.match_ilu_order()
     c.oracle.pset(0.0, y, None, 0, 5e-3)

@@ -9,7 +9,7 @@ import pytest
 
 from fosolvers_gb300 import mesh as M
 from fosolvers_gb300.euler import FLUX_FP32
-from helpers import Case, perturbed, rel_err
+from helpers import Case, hex_workload, perturbed, rel_err, with_all_conditions
 
 pytestmark = pytest.mark.gpu
 
@@ -19,6 +19,7 @@ def _cases():
         "sod16": lambda: M.make_workload("sod16"),
         "sine12": lambda: M.make_workload("sine96", scale=12, seed=3),
         "bump24": lambda: M.make_workload("bump192", scale=24),
+        "hex10": lambda: hex_workload(10, seed=2),
     }
 
 
@@ -27,7 +28,7 @@ def cases(cuda):
     return {k: Case(f()) for k, f in _cases().items()}
 
 
-@pytest.mark.parametrize("name", ["sod16", "sine12", "bump24"])
+@pytest.mark.parametrize("name", ["sod16", "sine12", "bump24", "hex10"])
 @pytest.mark.parametrize("seed", [None, 11])
 def test_rhs_host_callback_matches_oracle(cases, name, seed):
     c = cases[name]
@@ -38,26 +39,24 @@ def test_rhs_host_callback_matches_oracle(cases, name, seed):
     assert rel_err(out, ref) <= 1e-11
 
 
-def test_rhs_all_condition_types(cuda):
-    """Every non-UDF condition of setBC (foeuler.f90:217-325) on one box: wall, static
-    inflow (subsonic: interior momentum), total inflow, outflow (imposed p), far field,
-    zero-gradient outflow."""
-    wl = M.make_workload("sod16", scale=6)
-    wl.bc_gid = np.array([1, 2, 3, 4, 5, 6], np.int32)
-    wl.bc_type = np.array([10, 11, 20, 30, 21, 0], np.int32)
-    wl.bc_param = np.array([[1.0, 1.0, 0.3, 0.0, 0.0],
-                            [1.2, 1.1, 0.5, 0.1, 0.0],
-                            [0.9, 0, 0, 0, 0],
-                            [1.0, 1.0, 0.2, 0.1, 0.05],
-                            [0, 0, 0, 0, 0],
-                            [0, 0, 0, 0, 0]])
-    c = Case(wl)
-    for seed in (None, 4):
-        y = c.y0 if seed is None else perturbed(c.y0, c.nC, seed, amp=0.1)
-        ref = c.oracle_rhs(y)
-        out = np.zeros_like(y)
-        assert c.gpu.rhs(0.0, y, out) == 0
-        assert rel_err(out, ref) <= 1e-11
+@pytest.mark.parametrize("name", ["tet6", "hex8"])
+def test_rhs_all_condition_types(cuda, name):
+    """Every non-UDF condition of setBC (foeuler.f90:217-325) on one box: static inflow
+    (subsonic: interior momentum), total inflow, outflow (imposed p), far field,
+    zero-gradient outflow, wall; tetrahedra and hexahedra (QUAD boundary faces), FP64 flux
+    within 1e-11 and FP32 flux within 2e-5."""
+    wl = with_all_conditions(M.make_workload("sod16", scale=6) if name == "tet6"
+                             else hex_workload(8, seed=5))
+    for flags, tol in ((0, 1e-11), (FLUX_FP32, 2e-5)):
+        c = Case(wl, flags=flags)
+        for seed in (None, 4):
+            y = c.y0 if seed is None else perturbed(c.y0, c.nC, seed, amp=0.1)
+            ref = c.oracle_rhs(y)
+            out = np.zeros_like(y)
+            assert c.gpu.rhs(0.0, y, out) == 0
+            err = rel_err(out, ref)
+            print(name, flags, seed, err)
+            assert err <= tol
 
 
 def test_rhs_bar_tet_unstructured(cuda):
@@ -78,9 +77,10 @@ def test_rhs_bar_tet_unstructured(cuda):
     assert rel_err(out, ref) <= 1e-11
 
 
-def test_rhs_device_entry_and_renumbering(cases):
+@pytest.mark.parametrize("name", ["sine12", "hex10"])
+def test_rhs_device_entry_and_renumbering(cases, name):
     import torch
-    c = cases["sine12"]
+    c = cases[name]
     y = perturbed(c.y0, c.nC, 2)
     ref = c.oracle_rhs(y)
     yr = torch.from_numpy(y).cuda()
@@ -95,10 +95,11 @@ def test_rhs_device_entry_and_renumbering(cases):
     assert c.gpu.info()["bandwidth"] < c.nC
 
 
-def test_jv_matches_oracle_difference_quotient(cases):
+@pytest.mark.parametrize("name", ["sine12", "hex10"])
+def test_jv_matches_oracle_difference_quotient(cases, name):
     """Fused FD Jv: out = a v + b (f(y + s v) - f(y))/s, s = eps (1 + ||y||)/||v||."""
     import torch
-    c = cases["sine12"]
+    c = cases[name]
     rng = np.random.default_rng(0)
     y = perturbed(c.y0, c.nC, 5)
     v = rng.normal(size=y.size)
@@ -129,7 +130,7 @@ def test_nonfinite_state_is_recoverable(cases):
     assert c.gpu.rhs(0.0, y, out) == 1  # CVODE convention: > 0 = recoverable
 
 
-@pytest.mark.parametrize("name", ["sod16", "sine12", "bump24"])
+@pytest.mark.parametrize("name", ["sod16", "sine12", "bump24", "hex10"])
 def test_fp32_flux_against_fp64_oracle(name):
     wl = _cases()[name]()
     c = Case(wl, flags=FLUX_FP32)

@@ -45,6 +45,29 @@ def test_box_grid_matches_reference(dims, seed):
     assert np.all(g.iEP[: g.nPi, 1] <= g.nC) and np.all(g.iEP[g.nPi:, 1] > g.nC)
 
 
+@pytest.mark.parametrize("dims,seed", [((1, 1, 1), 0), ((4, 3, 5), 1)])
+def test_hex_box_grid_matches_reference(dims, seed):
+    """HEX cells and QUAD facets (hexahedron face table, quad face areas, six-tetrahedron
+    volumes) against the oracle's restatement."""
+    g = _compare(M.box_mesh(*dims, jitter=0.1, seed=seed, cells="hex"))
+    nx, ny, nz = dims
+    assert g.nC == nx * ny * nz and g.maxFace == 6
+    assert g.nPb == 2 * (nx * ny + ny * nz + nx * nz)
+    assert g.nPi == 3 * nx * ny * nz - (nx * ny + ny * nz + nx * nz)
+    assert abs(g.v.sum() - 1.0) < 1e-13
+
+
+def test_unjittered_hex_cells_are_closed():
+    g = PolyFvGrid.from_mesh(M.box_mesh(4, 3, 2, jitter=0.0, cells="hex"))
+    S = np.zeros((g.nC, 3))
+    an = g.aP[:, None] * g.normP
+    np.add.at(S, g.iEP[:, 0] - 1, an)
+    inner = g.iEP[:, 1] <= g.nC
+    np.add.at(S, g.iEP[inner, 1] - 1, -an[inner])
+    assert np.abs(S).max() < 1e-15
+    np.testing.assert_allclose(g.v, 1.0 / 24, rtol=1e-13)
+
+
 def test_bump_grid_matches_reference():
     _compare(M.box_mesh(12, 4, 2, extent=(3.0, 1.0, 0.5), jitter=0.0, bump=True))
 

@@ -12,15 +12,18 @@ import pytest
 
 from fosolvers_gb300 import mesh as M
 from fosolvers_gb300.euler import FLUX_FP32
-from helpers import Case, perturbed, rel_err
+from helpers import Case, hex_workload, perturbed, rel_err, with_all_conditions
 
 pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("flags", [0, FLUX_FP32])
-def test_static_scratch_residual_matches_rhs_dev(cuda, flags):
+@pytest.mark.parametrize("name", ["sine8", "hex-conds"])
+def test_static_scratch_residual_matches_rhs_dev(cuda, flags, name):
     import torch
-    c = Case(M.make_workload("sine96", scale=8, seed=5), flags=flags)  # 3,072 cells
+    wl = (M.make_workload("sine96", scale=8, seed=5) if name == "sine8"  # 3,072 cells
+          else with_all_conditions(hex_workload(10, seed=5)))  # warped hexahedra, 480 cells
+    c = Case(wl, flags=flags)
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
     for seed in (1, 2):  # two calls in a row, different states
         y = perturbed(c.y0, c.nC, seed)
