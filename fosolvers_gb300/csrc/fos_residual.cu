@@ -308,18 +308,40 @@ __device__ __forceinline__ void roe_split_mj(float rm, float dr, float um, float
   dw[0] = h * d0; dw[1] = h * d1; dw[2] = h * d2; dw[3] = h * d3; dw[4] = h * d4;
 }
 
-// Boundary faces [nFi, nF) of the FP32 flux, all in FP64 (1% of the faces): the Roe flow of
-// k_face64 (interior state, ghost state, both primitives from the conserved variables)
-// minus the interior cell's own flux aP F(u_L).n, i.e. the flow in the difference form that
-// k_cell32 accumulates.  Stored as FP64 (5 of the face's 6 slots of F).
+// Boundary faces [nFi, nF) of the FP32 flux (1% of the faces): the face's Roe flow minus the
+// interior cell's own flux aP F(u_L).n, i.e. the flow in the difference form that k_cell32
+// accumulates, stored as FP64 (5 of the face's 6 slots of F).
+//   wall (mirrored ghost: equal rho, p, H, normal velocity reversed): the Roe average has
+//     zero normal velocity and the flow reduces to aP (0, (p + rho un (un + c)) n, 0), c^2 =
+//     (g-1)(H - |u_t|^2/2); the difference aP rho un (-1, (un + c) n - u, -H) is formed in
+//     FP32 from the FP32 primitives (k_prim_hl, same state as y + s v);
+//   other conditions: k_face64's FP64 flow (interior and ghost primitives from the conserved
+//     variables) minus the own flux, in FP64.
 __global__ void __launch_bounds__(kThreads) k_bface32(
     int nFi, int nF, int nC, const int2* __restrict__ faceLR, const double2* __restrict__ faceNA,
+    const float4* __restrict__ faceNA32, const float* __restrict__ Whl, float gm1f,
     const double* __restrict__ y, const double* __restrict__ v, const double* __restrict__ d_s,
     const int* __restrict__ bcT, const double* __restrict__ bcP, int maxP, double g, double r,
     double* __restrict__ F) {
   const int f = nFi + blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nF) return;
   const int2 lr = __ldg(faceLR + f);
+  const int row = lr.y;
+  const int type = row > 0 ? bcT[row - 1] : FOS_BC_WALL;
+  double2* F2 = reinterpret_cast<double2*>(F + 6 * (size_t)f);
+  if (type == FOS_BC_WALL) {
+    const float4 na = __ldg(faceNA32 + f);
+    const float4* w4 = reinterpret_cast<const float4*>(Whl + 16 * (size_t)lr.x);
+    const float4 a = __ldg(w4), b = __ldg(w4 + 1);  // (rho, u, v, w), (H, p, ...) hi parts
+    const float un = a.y * na.x + a.z * na.y + a.w * na.z;
+    const float q2 = a.y * a.y + a.z * a.z + a.w * a.w;
+    const float c = sqrtf(gm1f * (b.x - 0.5f * (q2 - un * un)));
+    const float m = na.w * a.x * un, k = un + c;
+    F2[0] = make_double2(f2d_bits(-m), f2d_bits(m * (k * na.x - a.y)));
+    F2[1] = make_double2(f2d_bits(m * (k * na.y - a.z)), f2d_bits(m * (k * na.z - a.w)));
+    F2[2] = make_double2(f2d_bits(-m * b.x), 0.0);
+    return;
+  }
   const double2 n01 = __ldg(faceNA + 2 * (size_t)f), n2a = __ldg(faceNA + 2 * (size_t)f + 1);
   const double nx = n01.x, ny = n01.y, nz = n2a.x, aP = n2a.y;
   double U[5], G[5];
@@ -330,8 +352,6 @@ __global__ void __launch_bounds__(kThreads) k_bface32(
 #pragma unroll
     for (int q = 0; q < 5; q++) U[q] = U[q] + s * v[(size_t)q * nC + lr.x];
   }
-  const int row = lr.y;
-  const int type = row > 0 ? bcT[row - 1] : FOS_BC_WALL;
   ghost_state(type, row > 0 ? bcP + (size_t)maxP * (row - 1) : nullptr, U, nx, ny, nz, g, r, G);
   P64 L, R;
   prim_from_cons(U[0], U[1], U[2], U[3], U[4], g - 1.0, L);
@@ -339,7 +359,6 @@ __global__ void __launch_bounds__(kThreads) k_bface32(
   double flow[5];
   roe_flow64(L, R, nx, ny, nz, aP, g - 1.0, flow);
   const double m = aP * L.rho * (L.u * nx + L.v * ny + L.w * nz), pa = aP * L.p;
-  double2* F2 = reinterpret_cast<double2*>(F + 6 * (size_t)f);
   F2[0] = make_double2(flow[0] - m, flow[1] - (m * L.u + pa * nx));
   F2[1] = make_double2(flow[2] - (m * L.v + pa * ny), flow[3] - (m * L.w + pa * nz));
   F2[2] = make_double2(flow[4] - m * L.H, 0.0);
@@ -377,35 +396,32 @@ __global__ void __launch_bounds__(kThreads) k_cell32(
     if (k > 0 && e[k] < 0) continue;
     const int f = e[k] >> 1;
     const bool isR = e[k] & 1;
-    if (f >= nFi) {  // boundary face (cell is L): the FP64 difference of k_bface32
+    double t[5];  // the face's term: -(dF - dw) (cell is L) or -(dF + dw) (cell is R)
+    if (f < nFi) {
+      const float sw = isR ? 1.0f : -1.0f;
+      const int2 lr = __ldg(faceLR + f);
+      const float4 na = __ldg(faceNA + f);
+      PHL Q;
+      load_hl(W, isR ? lr.x : lr.y, Q);
+      const PHL& L = isR ? Q : P;
+      const PHL& R = isR ? P : Q;
+      float m[6], d[6], dF[5], dw[5];
+#pragma unroll
+      for (int j = 0; j < 6; j++) {
+        m[j] = 0.5f * (L.h[j] + R.h[j]) + 0.5f * (L.l[j] + R.l[j]);
+        d[j] = (R.h[j] - L.h[j]) + (R.l[j] - L.l[j]);
+      }
+      roe_split_mj(m[0], d[0], m[1], d[1], m[2], d[2], m[3], d[3], m[4], d[4], d[5], L.s, R.s,
+                   na.x, na.y, na.z, na.w, gm1, dF, dw);
+#pragma unroll
+      for (int q = 0; q < 5; q++) t[q] = f2d_bits(fmaf(sw, dw[q], dF[q]));
+    } else {  // boundary face (cell is L): the FP64 difference of k_bface32
       const double2* F2 = reinterpret_cast<const double2*>(Fb + 6 * (size_t)f);
       const double2 a0 = __ldg(F2), a1 = __ldg(F2 + 1), a2 = __ldg(F2 + 2);
-      const double d[5] = {a0.x, a0.y, a1.x, a1.y, a2.x};
-#pragma unroll
-      for (int q = 0; q < 5; q++) acc[q] = k == 0 ? -d[q] : acc[q] - d[q];
-      continue;
+      t[0] = a0.x; t[1] = a0.y; t[2] = a1.x; t[3] = a1.y; t[4] = a2.x;
     }
-    const float sw = isR ? 1.0f : -1.0f;  // R: -(dF + dw), L: -(dF - dw)
-    float dF[5], dw[5];
-    const int2 lr = __ldg(faceLR + f);
-    const float4 na = __ldg(faceNA + f);
-    PHL Q;
-    load_hl(W, isR ? lr.x : lr.y, Q);
-    const PHL& L = isR ? Q : P;
-    const PHL& R = isR ? P : Q;
-    float m[6], d[6];
 #pragma unroll
-    for (int j = 0; j < 6; j++) {
-      m[j] = 0.5f * (L.h[j] + R.h[j]) + 0.5f * (L.l[j] + R.l[j]);
-      d[j] = (R.h[j] - L.h[j]) + (R.l[j] - L.l[j]);
-    }
-    roe_split_mj(m[0], d[0], m[1], d[1], m[2], d[2], m[3], d[3], m[4], d[4], d[5], L.s, R.s,
-                 na.x, na.y, na.z, na.w, gm1, dF, dw);
-#pragma unroll
-    for (int q = 0; q < 5; q++) {
-      const float term = fmaf(sw, dw[q], dF[q]);
-      acc[q] = k == 0 ? f2d_bits(-term) : acc[q] - f2d_bits(term);
-    }
+    for (int q = 0; q < 5; q++) acc[q] = k == 0 ? -t[q] : acc[q] - t[q];
   }
   if (Sc) {  // own flux through the closure vector: rho u.S, rho u u.S + p S, rho H u.S
     const float4 S = __ldg(Sc + c);
@@ -483,7 +499,8 @@ int fos_residual_launch(fos_ctx* c, const double* y, const double* v, const doub
     fos_launch(c, k_prim_hl, nblk(c->nC), kThreads, c->nC, y, v, d_s, gm1, c->d_Whl);
     if (c->nFb)
       fos_launch(c, k_bface32, nblk(c->nFb), kThreads, c->nFi, c->nF, c->nC,
-                 (const int2*)c->d_faceLR, (const double2*)c->d_faceNA, y, v, d_s,
+                 (const int2*)c->d_faceLR, (const double2*)c->d_faceNA,
+                 (const float4*)c->d_faceNA32, (const float*)c->d_Whl, (float)gm1, y, v, d_s,
                  (const int*)c->d_bcT, (const double*)c->d_bcP, c->maxP, c->gamm, c->r, c->d_F);
     if (c->ell_w == 4)
       fos_launch(c, k_cell32<4>, nblk(c->nC), kThreads, c->nC, c->nFi, (const int*)c->d_ell,
@@ -619,8 +636,9 @@ extern "C" int fos_euler_rhs_dev_static(const fos_ctx* c, double t, const double
     k_prim_hl<<<nblk(c->nC), kThreads, 0, s>>>(c->nC, y, nullptr, nullptr, gm1, Whl);
     if (c->nFb)
       k_bface32<<<nblk(c->nFb), kThreads, 0, s>>>(c->nFi, c->nF, c->nC, c->d_faceLR,
-                                                  c->d_faceNA, y, nullptr, nullptr, c->d_bcT,
-                                                  c->d_bcP, c->maxP, c->gamm, c->r, F);
+                                                  c->d_faceNA, c->d_faceNA32, Whl, (float)gm1, y,
+                                                  nullptr, nullptr, c->d_bcT, c->d_bcP, c->maxP,
+                                                  c->gamm, c->r, F);
     if (c->ell_w == 4)
       k_cell32<4><<<nblk(c->nC), kThreads, 0, s>>>(c->nC, c->nFi, c->d_ell, c->d_faceLR,
                                                    c->d_faceNA32, Whl, (float)gm1, F,
