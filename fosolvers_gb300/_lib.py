@@ -91,6 +91,14 @@ _SIGS = {
     "fos_gnn_get_grad": (C.c_int, [_vp, C.POINTER(C.c_float)]),
     "fos_gnn_adam_step": (C.c_int, [_vp, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float]),
     "fos_ctx_attach_gnn": (C.c_int, [_vp, _vp]),
+    "fos_ilut_create": (C.c_int, [C.POINTER(_vp), C.c_int, C.c_int]),
+    "fos_ilut_factor_dev": (C.c_int, [_vp, _vp, _vp, _vp, C.c_double, _vp]),
+    "fos_ilut_solve_dev": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "fos_ilut_status": (C.c_int, [_vp]),
+    "fos_ilut_copy": (C.c_long, [_vp, _dp, _ip, _ip, C.c_long]),
+    "fos_ilut_info": (C.c_int, [_vp, _lp]),
+    "fos_ilut_destroy": (None, [_vp]),
+    "fos_ctx_set_ilut": (C.c_int, [_vp, C.c_int, C.c_double]),
     "fos_bdf_defaults": (None, [C.POINTER(BdfOpts)]),
     "fos_bdf_run": (C.c_int, [_vp, C.c_double, _vp, C.POINTER(BdfOpts), C.POINTER(BdfStats)]),
     "fos_bdf_run_host": (C.c_int, [_vp, C.c_double, _dp, C.POINTER(BdfOpts), C.POINTER(BdfStats)]),

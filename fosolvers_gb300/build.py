@@ -20,7 +20,7 @@ BUILD = HERE / "_build"
 LIB = HERE / "libfosgpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["fos_ctx.cu", "fos_residual.cu", "fos_jacobian.cu", "fos_bdf.cu", "fos_gnn.cu",
-           "fos_grid.cpp"]
+           "fos_ilut.cu", "fos_grid.cpp"]
 
 
 def _nvcc() -> str:

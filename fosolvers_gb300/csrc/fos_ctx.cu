@@ -33,11 +33,12 @@ fos_ctx::~fos_ctx() {
                   d_bcT, d_bcP, d_W, d_Whl, d_ell, d_F, d_stage, d_y, d_f, d_z, d_red, d_scal,
                   d_flag, d_prow, d_pcol, d_pdiag, d_cdiag, d_ipos, d_ord, d_fslot, d_Jraw,
                   d_LU, d_LU32, d_lrows_f, d_lrows_b, d_upd_ptr, d_upd, d_ilu_tmp, d_Jb, d_ierr,
-                  d_closure32};
+                  d_closure32, d_pia, d_pja, d_pa, d_vol, d_ilut_x};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h_scal) cudaFreeHost(h_scal);
   fos_bdf_work_free(bdf);
+  fos_ilut_destroy(ilut);
 }
 
 namespace {
@@ -285,6 +286,8 @@ extern "C" int fos_ctx_create(fos_ctx** out, int nC, int nE, int nPi, int nPb, c
     for (int e = crow[i]; e < crow[i + 1]; e++) ell[(size_t)c->ell_w * i + (e - crow[i])] = cent[e];
   std::vector<double> invV(nC);
   for (int i = 0; i < nC; i++) invV[c->old2new[i]] = 1.0 / v[i];
+  c->h_vol.resize(nC);
+  for (int i = 0; i < nC; i++) c->h_vol[c->old2new[i]] = v[i];
   // closure vector of every cell, sum over its faces of the outward aP n.  The FP32 flux
   // writes each face flow as the cell's own flux aP F(u_c).n plus a difference and drops the
   // own-flux part, whose sum is F(u_c).S_c: zero for cells with planar faces, not for

@@ -104,6 +104,17 @@ struct fos_ctx {
   std::vector<int> h_ilu_pos;     // ILU position of every internal row
   double* d_ilu_tmp = nullptr;  // two AoS sweep vectors, 8 values per row each
   fos_bdf_work* bdf = nullptr;  // driver workspace, kept between calls
+
+  // ---- ILUT preconditioner (FOS_PREC_ILUT): scalar CSR of P in ILU position order
+  std::vector<double> h_vol;      // cell volumes, internal order
+  fos_ilut* ilut = nullptr;
+  int ilut_lfil = 50;
+  double ilut_droptol = 1e-6;
+  int* d_pia = nullptr;           // [5nC+1]
+  int* d_pja = nullptr;           // [25 nnzb]
+  double* d_pa = nullptr;         // [25 nnzb]
+  double* d_vol = nullptr;        // [nC]
+  double* d_ilut_x = nullptr;     // [5nC] position-order work vector
   long n_launch = 0;            // kernels launched through fos_launch
   fos_gnn* gnn = nullptr;       // learned preconditioner (not owned)
 
@@ -133,3 +144,6 @@ int fos_jac_setup(fos_ctx* c);
 int fos_jac_assemble(fos_ctx* c, const double* y);
 int fos_ilu_factor(fos_ctx* c, double gamma);
 int fos_ilu_apply(fos_ctx* c, const double* r, double* z);
+// fos_ilut.cu: the Euler preconditioner with ILUT (FOS_PREC_ILUT)
+int fos_ilut_ctx_factor(fos_ctx* c, double gamma);
+int fos_ilut_ctx_apply(fos_ctx* c, const double* r, double* z);

@@ -814,6 +814,7 @@ static int ilu_factor_t(fos_ctx* c, double gamma, TF* LU) {
 }
 
 int fos_ilu_factor(fos_ctx* c, double gamma) {
+  if (c->flags & FOS_PREC_ILUT) return fos_ilut_ctx_factor(c, gamma);
   const int big = 0x7fffffff;
   FOS_CUDA(cudaMemcpyAsync(c->d_ierr, &big, sizeof(int), cudaMemcpyHostToDevice, c->stream));
   int rc = (c->flags & FOS_ILU_FP32) ? ilu_factor_t<float, float>(c, gamma, c->d_LU32)
@@ -854,6 +855,7 @@ static int ilu_apply_t(fos_ctx* c, const TF* LU, const double* r, double* z) {
 }
 
 int fos_ilu_apply(fos_ctx* c, const double* r, double* z) {
+  if (c->flags & FOS_PREC_ILUT) return fos_ilut_ctx_apply(c, r, z);
   if (c->flags & FOS_ILU_FP32) return ilu_apply_t<float>(c, c->d_LU32, r, z);
   return ilu_apply_t<double>(c, c->d_LU, r, z);
 }

@@ -26,6 +26,7 @@ from ._lib import BdfOpts, BdfStats, check, dptr, iptr
 FLUX_FP64, FLUX_FP32 = 0, 1
 ORDER_RCM, ORDER_NATURAL = 0, 2
 ILU_FP32, ILU_COLOR = 4, 8
+PREC_ILUT = 16  # pset/psol with ILUT (FP64) instead of block ILU(0)
 
 
 @dataclass
@@ -240,6 +241,11 @@ class FOEuler:
                                                C.byref(ad), C.byref(st), C.byref(ast)),
                    "fos_bdf_adaptive")
         return rc, st.as_dict(), ast.as_dict()
+
+    def set_ilut(self, lfil: int = 50, droptol: float = 1e-6):
+        """ILUT parameters of a context created with PREC_ILUT (fopbc's fill 50 and drop
+        tolerance 1e-6 by default, modPbc.f90:21,658); used from the next pset on."""
+        check(_lib.lib().fos_ctx_set_ilut(self._h, int(lfil), float(droptol)), "set_ilut")
 
     def attach_gnn(self, gnn):
         """Learned preconditioner used by bdf_run / linear_solve when opts.precond >= 2

@@ -47,7 +47,9 @@ enum {
   FOS_ORDER_RCM = 0,   /* reverse Cuthill--McKee renumbering (default) */
   FOS_ORDER_NATURAL = 2,
   FOS_ILU_FP32 = 4,    /* ILU(0) factors and apply in FP32 */
-  FOS_ILU_COLOR = 8    /* ILU(0) on a multicolour ordering (few levels) */
+  FOS_ILU_COLOR = 8,   /* ILU(0) on a multicolour ordering (few levels) */
+  FOS_PREC_ILUT = 16   /* pset/psol factor P with ILUT (FP64) instead of block ILU(0);
+                          parameters from fos_ctx_set_ilut, default lfil 50, droptol 1e-6 */
 };
 
 /* ------------------------------------------------------------------ setup */
@@ -170,6 +172,36 @@ int fos_gnn_adam_step(fos_gnn* g, float lr, float beta1, float beta2, float eps,
 /* network used by fos_bdf_run when opts.precond >= 2 (not owned by the context); g = NULL
    detaches.  Returns -2 on a grid with hexahedra (the network reads 4 neighbour slots). */
 int fos_ctx_attach_gnn(fos_ctx* ctx, fos_gnn* g);
+
+/* ------------------------------------------------------------------ ILUT */
+
+/* Dual-threshold incomplete LU of a CSR matrix on the device: the reference's ILU class
+ * (numerics/sparse.f90:52-63 type, :334-348 initILU, :370-383 factILU, :386-392 solveILU),
+ * i.e. SPARSKIT ilut (ITSOL/ilut.f:38-382) and lusol (:2272-2320).  Given the same CSR
+ * matrix the factors are bit-identical to ilut's.  CSR arrays are 0-based device arrays
+ * (ia n+1, ja and a nnz); a row may list its columns in any order. */
+typedef struct fos_ilut fos_ilut;
+/* storage for n rows; lfil is clamped to n - 1 as initILU does (sparse.f90:341);
+ * lfil < 0 returns -4 (ilut's ierr) */
+int fos_ilut_create(fos_ilut** out, int n, int lfil);
+/* factor (factILU): returns 0, -5 on a zero row (ilut's ierr), -6 if a dependency wait ran
+ * out, -1 on bad arguments.  Synchronises the stream. */
+int fos_ilut_factor_dev(fos_ilut* f, const int* ia, const int* ja, const double* a,
+                        double droptol, void* stream);
+/* x = (LU)^{-1} y (solveILU / lusol), device vectors, x may equal y; asynchronous */
+int fos_ilut_solve_dev(fos_ilut* f, const double* y, double* x, void* stream);
+/* after the stream has drained: 0, or -6 when a solve's dependency wait ran out */
+int fos_ilut_status(fos_ilut* f);
+/* the factors in ilut's MSR layout on the host (1-based values): alu(1:n) the inverted
+ * diagonal, jlu(1:n+1) row pointers, ju(1:n) the start of each U row; returns the used
+ * length (all three pointers null: only the length), < 0 on error */
+long fos_ilut_copy(const fos_ilut* f, double* alu, int* jlu, int* ju, long iwk);
+/* out[0..3] = n, lfil, working-row capacity, kernels launched */
+int fos_ilut_info(const fos_ilut* f, long* out);
+void fos_ilut_destroy(fos_ilut* f);
+/* ILUT parameters of a context created with FOS_PREC_ILUT (fopbc's PBC_PREC_FILL = 50 and
+ * PBC_PREC_DROPTOL = 1e-6 by default, modPbc.f90:21,658); takes effect at the next pset */
+int fos_ctx_set_ilut(fos_ctx* ctx, int lfil, double droptol);
 
 /* ------------------------------------------------------------------ driver */
 

@@ -361,6 +361,10 @@ struct oe_ctx {
   int *pja, *pia, *jlu, *jluu, *iw;
   double *t1, *t2;
   int* perm; /* ILU cell order: old -> new (NULL = natural) */
+  /* ILUT in place of ilu0 (lfil >= 0), the reference ILU class on P */
+  int ilut_lfil, ilut_iwk;
+  double ilut_droptol, *ilut_alu, *ilut_w;
+  int *ilut_jlu, *ilut_ju, *ilut_jw;
 };
 
 static double dot3(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
@@ -375,6 +379,7 @@ oe_ctx* oe_new(int nC, int nE, int nPi, int nPb, const int* iEP, const double* a
   int nP = nPi + nPb;
   c->nC = nC; c->nE = nE; c->nP = nP; c->nPi = nPi; c->nPb = nPb; c->maxFace = maxFace;
   c->nBC = nBC; c->maxP = maxP; c->gamm = gamm; c->r = r; c->nthreads = 1;
+  c->ilut_lfil = -1;
   c->iEP = (int*)xcalloc((size_t)2 * nP, sizeof(int)); memcpy(c->iEP, iEP, sizeof(int) * 2 * (size_t)nP);
   c->aP = (double*)xcalloc(nP, sizeof(double)); memcpy(c->aP, aP, sizeof(double) * nP);
   c->normP = (double*)xcalloc((size_t)3 * nP, sizeof(double)); memcpy(c->normP, normP, sizeof(double) * 3 * (size_t)nP);
@@ -426,7 +431,29 @@ void oe_free(oe_ctx* c) {
   free(c->JacP); free(c->JacC); free(c->ju_); free(c->jH); free(c->jc);
   free(c->pa); free(c->pja); free(c->pia); free(c->alu); free(c->jlu); free(c->jluu); free(c->iw);
   free(c->t1); free(c->t2); free(c->perm);
+  free(c->ilut_alu); free(c->ilut_w); free(c->ilut_jlu); free(c->ilut_ju); free(c->ilut_jw);
   free(c);
+}
+/* ILUT for pset/psol with the ILU class's sizing (sparse.f90:334-348: lfil clamped to
+ * n - 1, alu/jlu of n*min(2*lfil+1, n)); lfil < 0 goes back to ilu0 */
+void oe_set_ilut(oe_ctx* c, int lfil, double droptol) {
+  const int n = 5 * c->nC;
+  free(c->ilut_alu); free(c->ilut_w); free(c->ilut_jlu); free(c->ilut_ju); free(c->ilut_jw);
+  c->ilut_alu = NULL; c->ilut_w = NULL; c->ilut_jlu = NULL; c->ilut_ju = NULL; c->ilut_jw = NULL;
+  c->ilut_lfil = lfil < 0 ? -1 : (lfil < n - 1 ? lfil : n - 1);
+  c->ilut_droptol = droptol;
+  if (c->ilut_lfil < 0) return;
+  const long w = 2L * c->ilut_lfil + 1;
+  c->ilut_iwk = (int)((long)n * (w < n ? w : n));
+  c->ilut_alu = (double*)xcalloc(c->ilut_iwk, sizeof(double));
+  c->ilut_jlu = (int*)xcalloc(c->ilut_iwk, sizeof(int));
+  c->ilut_ju = (int*)xcalloc(n, sizeof(int));
+  c->ilut_w = (double*)xcalloc(n + 1, sizeof(double));
+  c->ilut_jw = (int*)xcalloc(2 * (size_t)n, sizeof(int));
+}
+int oe_ilut_factors(const oe_ctx* c, const double** alu, const int** jlu, const int** ju) {
+  *alu = c->ilut_alu; *jlu = c->ilut_jlu; *ju = c->ilut_ju;
+  return c->ilut_lfil < 0 ? -1 : c->ilut_iwk;
 }
 void oe_set_threads(oe_ctx* c, int nthreads) { c->nthreads = nthreads < 1 ? 1 : nthreads; }
 void oe_set_ilu_order(oe_ctx* c, const int* old2new) {
@@ -943,6 +970,154 @@ int o_ilu0(int n, const double* a, const int* ja, const int* ia, double* alu, in
 #undef JU
 #undef IW
 }
+/* Quick-split (ITSOL/ilut.f:2376-2434): permute a[0..n) (and ind alike) so that the ncut
+ * entries of largest magnitude come first; ncut is 1-based, nothing happens outside [1, n]. */
+void o_qsplit(double* a, int* ind, int n, int ncut) {
+  int first = 0, last = n - 1;
+  const int cut = ncut - 1;
+  if (cut < first || cut > last) return;
+  for (;;) {
+    int mid = first;
+    const double key = fabs(a[mid]);
+    for (int j = first + 1; j <= last; j++)
+      if (fabs(a[j]) > key) {
+        mid++;
+        double t = a[mid]; a[mid] = a[j]; a[j] = t;
+        int it = ind[mid]; ind[mid] = ind[j]; ind[j] = it;
+      }
+    double t = a[mid]; a[mid] = a[first]; a[first] = t;
+    int it = ind[mid]; ind[mid] = ind[first]; ind[first] = it;
+    if (mid == cut) return;
+    if (mid > cut) last = mid - 1; else first = mid + 1;
+  }
+}
+
+/* Dual-threshold ILU (ITSOL/ilut.f:38-382), MSR output as ilu0's: alu(1:n) inverted
+ * diagonal, row i = its L entries then (from ju(i)) its U entries.  All index arrays hold
+ * 1-based values; w (n+1) and jw (2n) are work.  Returns ierr: 0, -1 row longer than n,
+ * -2 / -3 L / U storage (iwk) exhausted, -4 lfil < 0, -5 zero row.
+ * Per row ii: tnorm = mean |a|; L and U parts unpacked (U keeps the CSR order, fill-ins
+ * appended); the L entries are eliminated in increasing column order, each multiplier
+ * fact = w * (inverted pivot) dropped when |fact| <= droptol, else stored and its pivot row's
+ * U part subtracted (new columns appended); the lfil largest multipliers are kept
+ * (quick-split); U entries with |w| <= droptol*tnorm are dropped, the min(lenu, lfil)
+ * largest split off and min(lenu, lfil) - 1 of them stored; a zero pivot becomes
+ * (1e-4 + droptol) tnorm. */
+int o_ilut(int n, const double* a, const int* ja, const int* ia, int lfil, double droptol,
+           double* alu, int* jlu, int* ju, int iwk, double* w, int* jw) {
+#define ALU(k) alu[(k)-1]
+#define JLU(k) jlu[(k)-1]
+#define JU(k) ju[(k)-1]
+#define W(k) w[(k)-1]
+#define JW(k) jw[(k)-1]
+  if (lfil < 0) return -4;
+  int ju0 = n + 2;
+  JLU(1) = ju0;
+  for (int j = 1; j <= n; j++) JW(n + j) = 0;
+  for (int ii = 1; ii <= n; ii++) {
+    const int j1 = ia[ii - 1], j2 = ia[ii] - 1;
+    double tnorm = 0.0;
+    for (int k = j1; k <= j2; k++) tnorm += fabs(a[k - 1]);
+    if (tnorm == 0.0) return -5;
+    tnorm = tnorm / (double)(j2 - j1 + 1);
+    int lenu = 1, lenl = 0;
+    JW(ii) = ii;
+    W(ii) = 0.0;
+    JW(n + ii) = ii;
+    for (int j = j1; j <= j2; j++) {
+      const int k = ja[j - 1];
+      const double t = a[j - 1];
+      if (k < ii) {
+        lenl++;
+        JW(lenl) = k; W(lenl) = t; JW(n + k) = lenl;
+      } else if (k == ii) {
+        W(ii) = t;
+      } else {
+        lenu++;
+        const int jpos = ii + lenu - 1;
+        JW(jpos) = k; W(jpos) = t; JW(n + k) = jpos;
+      }
+    }
+    int len = 0;
+    for (int jj = 1; jj <= lenl; jj++) {
+      int jrow = JW(jj), k = jj;
+      for (int j = jj + 1; j <= lenl; j++)
+        if (JW(j) < jrow) { jrow = JW(j); k = j; }
+      if (k != jj) {
+        const int j = JW(jj);
+        JW(jj) = JW(k); JW(k) = j;
+        JW(n + jrow) = jj; JW(n + j) = k;
+        const double sw = W(jj); W(jj) = W(k); W(k) = sw;
+      }
+      JW(n + jrow) = 0;
+      const double fact = W(jj) * ALU(jrow);
+      if (fabs(fact) <= droptol) continue;
+      for (int kk = JU(jrow); kk <= JLU(jrow + 1) - 1; kk++) {
+        const double sv = fact * ALU(kk);
+        const int j = JLU(kk);
+        const int jpos = JW(n + j);
+        if (j >= ii) {
+          if (jpos == 0) {
+            lenu++;
+            if (lenu > n) return -1;
+            const int i = ii + lenu - 1;
+            JW(i) = j; JW(n + j) = i; W(i) = -sv;
+          } else {
+            W(jpos) = W(jpos) - sv;
+          }
+        } else {
+          if (jpos == 0) {
+            lenl++;
+            if (lenl > n) return -1;
+            JW(lenl) = j; JW(n + j) = lenl; W(lenl) = -sv;
+          } else {
+            W(jpos) = W(jpos) - sv;
+          }
+        }
+      }
+      len++;
+      W(len) = fact;
+      JW(len) = jrow;
+    }
+    for (int k = 1; k <= lenu; k++) JW(n + JW(ii + k - 1)) = 0;
+    lenl = len;
+    len = lenl < lfil ? lenl : lfil;
+    o_qsplit(&W(1), &JW(1), lenl, len);
+    for (int k = 1; k <= len; k++) {
+      if (ju0 > iwk) return -2;
+      ALU(ju0) = W(k);
+      JLU(ju0) = JW(k);
+      ju0++;
+    }
+    JU(ii) = ju0;
+    len = 0;
+    for (int k = 1; k <= lenu - 1; k++)
+      if (fabs(W(ii + k)) > droptol * tnorm) {
+        len++;
+        W(ii + len) = W(ii + k);
+        JW(ii + len) = JW(ii + k);
+      }
+    lenu = len + 1;
+    len = lenu < lfil ? lenu : lfil;
+    o_qsplit(&W(ii + 1), &JW(ii + 1), lenu - 1, len);
+    if (len + ju0 > iwk) return -3;
+    for (int k = ii + 1; k <= ii + len - 1; k++) {
+      JLU(ju0) = JW(k);
+      ALU(ju0) = W(k);
+      ju0++;
+    }
+    if (W(ii) == 0.0) W(ii) = (0.0001 + droptol) * tnorm;
+    ALU(ii) = 1.0 / W(ii);
+    JLU(ii + 1) = ju0;
+  }
+  return 0;
+#undef ALU
+#undef JLU
+#undef JU
+#undef W
+#undef JW
+}
+
 void o_lusol(int n, const double* y, double* x, const double* alu, const int* jlu, const int* ju) {
   for (int i = 1; i <= n; i++) { /* ITSOL/ilut.f:2272-2320 */
     double s = y[i - 1];
@@ -1026,6 +1201,11 @@ int oe_pset(double t, const double* y, const double* fy, int jok, int* jcur, dou
     *jcur = 0;
   }
   oe_build_P(c, gamma);
+  if (c->ilut_lfil >= 0) {
+    c->ierr = o_ilut(5 * c->nC, c->pa, c->pja, c->pia, c->ilut_lfil, c->ilut_droptol,
+                     c->ilut_alu, c->ilut_jlu, c->ilut_ju, c->ilut_iwk, c->ilut_w, c->ilut_jw);
+    return c->ierr == 0 ? 0 : (c->ierr == -5 ? 1 : -1);
+  }
   c->ierr = o_ilu0(5 * c->nC, c->pa, c->pja, c->pia, c->alu, c->jlu, c->jluu, c->iw);
   return c->ierr ? 1 : 0; /* zero pivot: recoverable */
 }
@@ -1037,7 +1217,10 @@ int oe_psol(double t, const double* y, const double* fy, const double* r, double
   const int nC = c->nC;
   for (int i = 0; i < nC; i++)
     for (int a = 0; a < 5; a++) c->t1[5 * pnew(c, i) + a] = r[a * nC + i];
-  o_lusol(5 * nC, c->t1, c->t2, c->alu, c->jlu, c->jluu);
+  if (c->ilut_lfil >= 0)
+    o_lusol(5 * nC, c->t1, c->t2, c->ilut_alu, c->ilut_jlu, c->ilut_ju);
+  else
+    o_lusol(5 * nC, c->t1, c->t2, c->alu, c->jlu, c->jluu);
   for (int i = 0; i < nC; i++)
     for (int a = 0; a < 5; a++) z[a * nC + i] = c->t2[5 * pnew(c, i) + a];
   return 0;

@@ -71,6 +71,10 @@ void oe_set_threads(oe_ctx* c, int nthreads);
  * cell c (0-based); NULL = the reference's natural order.  ILU(0) depends on the order, so
  * parity with a renumbered GPU factorisation uses the GPU's order here. */
 void oe_set_ilu_order(oe_ctx* c, const int* old2new);
+/* pset/psol with ILUT (lfil, droptol; sized as the ILU class) instead of ilu0; lfil < 0
+ * goes back to ilu0.  oe_ilut_factors: the last ILUT factors (MSR), returns iwk or -1 */
+void oe_set_ilut(oe_ctx* c, int lfil, double droptol);
+int oe_ilut_factors(const oe_ctx* c, const double** alu, const int** jlu, const int** ju);
 /* the three CVODE callbacks (foeuler.f90:349-437) with N_Vector data as raw arrays;
  * ud is the oe_ctx*.  pset assembles findEulerJac, P = I - gamma*diag(1/v)*JacC in
  * interleaved (cell-major) scalar COO, coocsr, sorted rows, ilu0; psol = lusol. */
@@ -100,6 +104,11 @@ void o_amux(int n, const double* x, double* y, const double* a, const int* ja, c
 int o_ilu0(int n, const double* a, const int* ja, const int* ia, double* alu, int* jlu, int* ju,
            int* iw);
 void o_lusol(int n, const double* y, double* x, const double* alu, const int* jlu, const int* ju);
+void o_qsplit(double* a, int* ind, int n, int ncut);
+/* ILUT: alu, jlu sized iwk (>= n*(2*lfil+1) suffices), ju n, w n+1, jw 2n (work).
+ * returns ierr (0 ok, -1..-5 as SPARSKIT) */
+int o_ilut(int n, const double* a, const int* ja, const int* ia, int lfil, double droptol,
+           double* alu, int* jlu, int* ju, int iwk, double* w, int* jw);
 
 /* ---------------------------------------------------------------- Newton-Krylov / BDF */
 typedef int (*o_rhs_fn)(double t, const double* y, double* ydot, void* ud);

@@ -69,6 +69,8 @@ _SIGS = {
     "oe_free": (None, [_vp]),
     "oe_set_threads": (None, [_vp, C.c_int]),
     "oe_set_ilu_order": (None, [_vp, _ip]),
+    "oe_set_ilut": (None, [_vp, C.c_int, C.c_double]),
+    "oe_ilut_factors": (C.c_int, [_vp, C.POINTER(_dp), C.POINTER(_ip), C.POINTER(_ip)]),
     "oe_rhs": (C.c_int, [C.c_double, _dp, _dp, _vp]),
     "oe_pset": (C.c_int, [C.c_double, _dp, _dp, C.c_int, _ip, C.c_double, _vp]),
     "oe_psol": (C.c_int, [C.c_double, _dp, _dp, _dp, _dp, C.c_double, C.c_double, C.c_int, _vp]),
@@ -83,6 +85,9 @@ _SIGS = {
     "o_amux": (None, [C.c_int, _dp, _dp, _dp, _ip, _ip]),
     "o_ilu0": (C.c_int, [C.c_int, _dp, _ip, _ip, _dp, _ip, _ip, _ip]),
     "o_lusol": (None, [C.c_int, _dp, _dp, _dp, _ip, _ip]),
+    "o_qsplit": (None, [_dp, _ip, C.c_int, C.c_int]),
+    "o_ilut": (C.c_int, [C.c_int, _dp, _ip, _ip, C.c_int, C.c_double, _dp, _ip, _ip, C.c_int,
+                         _dp, _ip]),
     "o_bdf_defaults": (None, [C.POINTER(BdfOpts)]),
     "o_bdf_run": (C.c_int, [C.c_int, _vp, _vp, _vp, _vp, C.c_double, _dp, C.POINTER(BdfOpts),
                             C.POINTER(BdfStats)]),
@@ -118,6 +123,26 @@ def dp(a):
 def ip(a):
     assert a.dtype == np.int32 and a.flags.c_contiguous
     return a.ctypes.data_as(_ip)
+
+
+def ilut(n, a, ja, ia, lfil, droptol):
+    """The reference's ILU class on a CSR matrix with 1-based ja/ia (numerics/sparse.f90:
+    initILU :334-348 clamps lfil to n - 1 and sizes alu/jlu to n*min(2*lfil+1, n); factILU
+    :370-383 calls ilut).  Returns (ierr, alu, jlu, ju) in MSR form."""
+    lfil = min(lfil, n - 1)
+    iwk = n * min(2 * lfil + 1, n)
+    alu, jlu = np.zeros(iwk), np.zeros(iwk, np.int32)
+    ju, w, jw = np.zeros(n, np.int32), np.zeros(n + 1), np.zeros(2 * n, np.int32)
+    ierr = lib().o_ilut(n, dp(np.ascontiguousarray(a, np.float64)),
+                        ip(np.ascontiguousarray(ja, np.int32)), ip(np.ascontiguousarray(ia, np.int32)),
+                        lfil, droptol, dp(alu), ip(jlu), ip(ju), iwk, dp(w), ip(jw))
+    return ierr, alu, jlu, ju
+
+
+def lusol(n, y, alu, jlu, ju):
+    x = np.zeros(n)
+    lib().o_lusol(n, dp(np.ascontiguousarray(y, np.float64)), dp(x), dp(alu), ip(jlu), ip(ju))
+    return x
 
 
 def grid_build(mesh) -> dict:
@@ -179,6 +204,23 @@ class Euler:
         else:
             self._perm = np.ascontiguousarray(old2new, np.int32)
             lib().oe_set_ilu_order(self.h, ip(self._perm))
+
+    def set_ilut(self, lfil=50, droptol=1e-6):
+        """pset/psol with ILUT (the ILU class of numerics/sparse.f90) instead of ilu0;
+        lfil=None goes back to ilu0."""
+        lib().oe_set_ilut(self.h, -1 if lfil is None else int(lfil), float(droptol))
+
+    def ilut_factors(self):
+        """(alu, jlu, ju) of the last ILUT factorisation, MSR arrays trimmed to their use."""
+        alu, jlu, ju = _dp(), _ip(), _ip()
+        iwk = lib().oe_ilut_factors(self.h, C.byref(alu), C.byref(jlu), C.byref(ju))
+        if iwk < 0:
+            raise RuntimeError("no ILUT set")
+        n = 5 * self.nC
+        jl = np.ctypeslib.as_array(jlu, shape=(iwk,))
+        used = int(jl[n]) - 1
+        return (np.ctypeslib.as_array(alu, shape=(iwk,))[:used].copy(), jl[:used].copy(),
+                np.ctypeslib.as_array(ju, shape=(n,)).copy())
 
     def close(self):
         if self.h:

@@ -43,6 +43,105 @@ def test_ilu1_kat(oracle_lib):
     assert np.linalg.norm(x - [1.0, 1.5, 2.8, 2.75]) <= 1e-9
 
 
+def test_ilu1_kat_ilut():
+    """src/test/ILU1.f90:11-22 as the reference runs it: ILU%init(4, 7, 4) (lfil clamped to
+    3), setCOO without clean-up (rows keep the COO order: row 2 is [2, 1], row 4 is [4, 2]),
+    fact(0) = ilut with droptol 0, solve = lusol: x = [1, 3/2, 14/5, 11/4] within 1e-9."""
+    ao, jao, iao = _csr()
+    assert list(jao[iao[1] - 1:iao[2] - 1]) == [2, 1]
+    ierr, alu, jlu, ju = O.ilut(4, ao, jao, iao, 4, 0.0)
+    assert ierr == 0
+    x = O.lusol(4, [1.0, 2.0, 3.0, 4.0], alu, jlu, ju)
+    assert np.linalg.norm(x - [1.0, 1.5, 2.8, 2.75]) <= 1e-9
+
+
+def _dense_lu_of_msr(n, alu, jlu, ju):
+    """L (unit lower) and U (upper, diagonal un-inverted) as dense matrices."""
+    L, U = np.eye(n), np.zeros((n, n))
+    for i in range(n):
+        U[i, i] = 1.0 / alu[i]
+        for k in range(jlu[i] - 1, ju[i] - 1):
+            L[i, jlu[k] - 1] = alu[k]
+        for k in range(ju[i] - 1, jlu[i + 1] - 1):
+            U[i, jlu[k] - 1] = alu[k]
+    return L, U
+
+
+def _random_csr(n, density, seed, dominance=4.0):
+    rng = np.random.default_rng(seed)
+    A = (rng.random((n, n)) < density) * rng.normal(size=(n, n))
+    A += np.diag(dominance + np.abs(A).sum(1) * 0.1 + rng.random(n))
+    ia = np.zeros(n + 1, np.int32)
+    ja, a = [], []
+    for i in range(n):
+        cols = np.flatnonzero(A[i])
+        rng.shuffle(cols)  # ilut takes rows in any column order
+        ja += list(cols + 1)
+        a += list(A[i, cols])
+        ia[i + 1] = ia[i] + len(cols)
+    return A, np.array(a), np.array(ja, np.int32), ia + 1
+
+
+def test_ilut_without_dropping_is_exact_lu():
+    """lfil = n - 1 and droptol = 0 keep every entry: L U = A (no pivoting)."""
+    n = 40
+    A, a, ja, ia = _random_csr(n, 0.15, 1)
+    ierr, alu, jlu, ju = O.ilut(n, a, ja, ia, n, 0.0)
+    assert ierr == 0
+    L, U = _dense_lu_of_msr(n, alu, jlu, ju)
+    np.testing.assert_allclose(L @ U, A, atol=1e-12 * np.abs(A).max())
+
+
+def test_ilut_dual_threshold_limits():
+    """Every L row keeps at most lfil entries and every U row at most lfil - 1 off-diagonal
+    entries (the quick-split keeps min(lenu, lfil) including the diagonal slot); stored U
+    entries exceed droptol * mean |a| of their row; quick-split keeps the largest."""
+    n, lfil, tol = 60, 5, 1e-3
+    A, a, ja, ia = _random_csr(n, 0.3, 2)
+    ierr, alu, jlu, ju = O.ilut(n, a, ja, ia, lfil, tol)
+    assert ierr == 0
+    for i in range(n):
+        nl = ju[i] - jlu[i]
+        nu = jlu[i + 1] - ju[i]
+        assert nl <= lfil and nu <= lfil - 1
+        tnorm = np.abs(A[i]).sum() / np.count_nonzero(A[i])
+        u = alu[ju[i] - 1:jlu[i + 1] - 1]
+        assert np.all(np.abs(u) > tol * tnorm)
+        assert np.all(jlu[ju[i] - 1:jlu[i + 1] - 1] > i + 1)
+        assert np.all(jlu[jlu[i] - 1:ju[i] - 1] < i + 1)
+
+
+def test_qsplit_partitions_by_magnitude():
+    rng = np.random.default_rng(4)
+    for n, cut in ((1, 1), (7, 3), (50, 10), (50, 50), (30, 1)):
+        a = rng.normal(size=n)
+        ind = np.arange(n, dtype=np.int32)
+        a0 = a.copy()
+        O.lib().o_qsplit(O.dp(a), O.ip(ind), n, cut)
+        np.testing.assert_array_equal(a, a0[ind])
+        assert np.abs(a[:cut]).min() >= np.abs(a[cut - 1:]).max() - 0.0
+
+
+def test_ilut_error_codes():
+    """-5 zero row, -4 negative lfil, -3 U storage exhausted: the ILU class sizes alu to
+    n*min(2*lfil+1, n), which for n = 2 is 4 < n + 2, so even a diagonal matrix fails."""
+    L = O.lib()
+
+    def run(a, ja, ia, lfil, iwk):
+        n = len(ia) - 1
+        w, jw = np.zeros(n + 1), np.zeros(2 * n, np.int32)
+        alu, jlu, ju = np.zeros(iwk), np.zeros(iwk, np.int32), np.zeros(n, np.int32)
+        return L.o_ilut(n, O.dp(np.array(a)), O.ip(np.array(ja, np.int32)),
+                        O.ip(np.array(ia, np.int32)), lfil, 0.0, O.dp(alu), O.ip(jlu), O.ip(ju),
+                        iwk, O.dp(w), O.ip(jw))
+
+    assert run([1.0, 0.0], [1, 2], [1, 2, 3], 1, 16) == -5
+    assert run([1.0, 1.0], [1, 2], [1, 2, 3], -1, 16) == -4
+    assert run([1.0, 1.0], [1, 2], [1, 2, 3], 1, 16) == 0
+    assert O.ilut(2, np.array([1.0, 1.0]), np.array([1, 2], np.int32),
+                  np.array([1, 2, 3], np.int32), 1, 0.0)[0] == -3
+
+
 def test_ilu0_zero_pivot_reports_row(oracle_lib):
     """ilu0 returns ierr = k on a zero pivot at step k (ilut.f:1896,1911)."""
     A = np.array([1.0, 0.0, 1.0])
