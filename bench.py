@@ -76,6 +76,12 @@ def parse():
     ap.add_argument("--no-ops", action="store_true", help="skip the per-operation timing")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--op-reps", type=int, default=5)
+    ap.add_argument("--ilut", action="store_true",
+                    help="the ILUT preconditioner arm (FP64 flux, ILUT(lfil, droptol) on P in the "
+                         "RCM order) against block ILU(0) on the same mesh, with the oracle's "
+                         "SPARSKIT ilut on the same P as the CPU baseline; its own JSON line")
+    ap.add_argument("--lfil", type=int, default=50, help="ILUT fill (fopbc: 50)")
+    ap.add_argument("--droptol", type=float, default=1e-6, help="ILUT drop tolerance (fopbc: 1e-6)")
     ap.add_argument("--profile-ops", action="store_true",
                     help="profiling target: one warm-up round, then one residual, Jv, pset, "
                          "ILU(0) apply and network apply on the workload; no JSON line")
@@ -115,6 +121,96 @@ def profile_ops(args):
     print(json.dumps({"profile_ops": args.workload, "cells": grid.nC, "faces": grid.nP,
                       "mode": args.mode, "finite": bool(torch.isfinite(out).all())}))
     ctx.close()
+
+
+def run_ilut(args):
+    """ILUT arm: BDF steps/s of the FP64 flux with GMRES(30) + ILUT(lfil, droptol) and with
+    block ILU(0), both in the RCM order; the ILUT factorisation (P formed and factored,
+    Jacobian reused) and one psol timed with CUDA events; the oracle's ilut + lusol on the
+    same state as the CPU baseline (one core, SPARSKIT is serial)."""
+    import torch
+    from __graft_entry__ import build
+    build()
+    from fosolvers_gb300 import mesh as M
+    from fosolvers_gb300.euler import FOEuler, PolyFvGrid, PREC_ILUT
+    from oracle import pyoracle as O
+    scale = args.scale or 24
+    wl = M.make_workload(args.workload, scale=scale)
+    grid = PolyFvGrid.from_mesh(wl.mesh)
+    ibc = M.ibc_for(wl.mesh, wl.bc_gid)
+    nC = grid.nC
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    y0_ref = torch.from_numpy(M.soa(wl.elem_state, nC)).to(dev)
+    gamma = wl.dt * (2.0 / 3.0 if wl.order == 2 else 1.0)
+    out = {}
+    for name, flags in (("ilut", PREC_ILUT), ("ilu0", 0)):
+        ctx = FOEuler(grid, ibc, wl.bc_type, wl.bc_param, wl.gamm, wl.r, flags=flags,
+                      stream=stream)
+        if flags:
+            ctx.set_ilut(args.lfil, args.droptol)
+        y0 = torch.empty_like(y0_ref)
+        ctx.to_internal(y0_ref, y0)
+        mk = lambda n: ctx.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=n, precond=1)
+        ms, st, launches, _, _ = timed_bdf(ctx, y0, mk, args, dev, stream, None)
+        rec = {"steps_per_s": args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
+               "n_newton": st["n_newton"], "n_lin_iters": st["n_lin_iters"],
+               "gpu_launches": launches}
+        ctx.pset_dev(0.0, y0, 0, gamma)
+        r = torch.randn(y0.shape, dtype=y0.dtype, device=dev,
+                        generator=torch.Generator(device=dev).manual_seed(0))
+        z = torch.empty_like(r)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        torch.cuda.synchronize(dev)
+        ev[0].record(stream)
+        for _ in range(3):
+            ctx.pset_dev(0.0, y0, 1, gamma)
+        ev[1].record(stream)
+        for _ in range(10):
+            ctx.psol_dev(r, z)
+        ev[2].record(stream)
+        torch.cuda.synchronize(dev)
+        rec["factor_ms"] = ev[0].elapsed_time(ev[1]) / 3
+        rec["psol_ms"] = ev[1].elapsed_time(ev[2]) / 10
+        if flags:
+            order = ctx.ilu_order()
+        out[name] = rec
+        ctx.close()
+    # CPU baseline: the oracle's ilut + lusol on P of the same state, the GPU's cell order
+    e = O.Euler(grid.__dict__, ibc, wl.bc_type, wl.bc_param, wl.gamm, wl.r, wl.elem_state)
+    e.set_ilu_order(order)
+    e.set_ilut(args.lfil, args.droptol)
+    y = M.soa(wl.elem_state, nC)
+    e.pset(0.0, y, None, 0, gamma)
+    t0 = time.perf_counter()
+    rc, _ = e.pset(0.0, y, None, 1, gamma)
+    t_fact = time.perf_counter() - t0
+    r = np.random.default_rng(0).normal(size=5 * nC)
+    z = np.zeros_like(r)
+    t0 = time.perf_counter()
+    e.psol(0.0, None, None, r, z, gamma)
+    t_sol = time.perf_counter() - t0
+    alu, jlu, ju = e.ilut_factors()
+    stored = int(jlu[5 * nC]) - 1 - (5 * nC + 1)
+    e.close()
+    g = out["ilut"]
+    line = {
+        "metric": f"ILUT({args.lfil}, {args.droptol:g}) factorisation of P = I - gamma J/v, "
+                  "1 GB300 vs SPARSKIT ilut restated (1 core)",
+        "value": g["factor_ms"], "unit": "ms", "higher_is_better": False, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": f"{args.workload} at {scale}^3 x 6 = {nC} tets, "
+                               f"{5 * nC} unknowns", "lfil": args.lfil, "droptol": args.droptol,
+                   "order": "RCM (internal)", "stored_lu_entries": stored,
+                   "stored_per_row": round(stored / (5 * nC), 2)},
+        "ilut": g, "ilu0": out["ilu0"],
+        "cpu_baseline": {"factor_ms": 1e3 * t_fact, "psol_ms": 1e3 * t_sol, "cores": 1,
+                         "kind": "port", "rc": rc,
+                         "sample": "the oracle's o_ilut (ITSOL/ilut.f:38-382 restated) on the "
+                                   "same P, and o_lusol, one call each"},
+        "speedup_factor": 1e3 * t_fact / g["factor_ms"], "speedup_psol": 1e3 * t_sol / g["psol_ms"],
+    }
+    print(json.dumps(line), flush=True)
 
 
 # ------------------------------------------------------------------ clocks
@@ -318,6 +414,9 @@ def main():
     args = parse()
     if args.profile_ops:
         profile_ops(args)
+        return
+    if args.ilut:
+        run_ilut(args)
         return
     world, rank, local, pg = dist_setup(args)
     if args.impl == "reference":

@@ -14,9 +14,9 @@
 //           written out (__dmul_rn / __dsub_rn): given the same CSR the factors are
 //           bit-identical to SPARSKIT's.  Fill-in positions follow ilut's append order
 //           (ballot prefix counts), and the quick-split runs on one lane.
-//   solve   the forward and backward sweeps of lusol, rows claimed in order (ascending,
-//           then descending), each lane waiting on the rows its entries read; the row sum
-//           is a fixed-order warp reduction.
+//   solve   the forward and backward sweeps of lusol, rows claimed level by level of the L
+//           and U dependency graphs, each unknown published by its own store and polled by
+//           the rows that read it; the row sum is a fixed-order warp reduction.
 //
 // Storage: every row owns lfil slots for L and lfil for U (ilut keeps at most lfil L and
 // lfil - 1 off-diagonal U entries per row), so the factor storage never runs out (the
@@ -40,11 +40,13 @@ struct fos_ilut {
   int* d_Ucnt = nullptr;
   double* d_dinv = nullptr;
   int* d_done = nullptr;   // factor: epoch of the factorisation that published the row
-  int* d_fdone = nullptr;  // solve: epoch of the forward / backward sweep that finished the row
-  int* d_bdone = nullptr;
+  double* d_z = nullptr;   // forward-sweep result (kPending before each solve)
+  int* d_permF = nullptr;  // rows by forward / backward level: the solves' claim order
+  int* d_permB = nullptr;
+  int nlevF = 0, nlevB = 0;
   int* d_ctr = nullptr;    // [0] factor ticket [1] forward [2] backward [3] error [4] error row
   int* h_ctr = nullptr;    // pinned copy
-  int fepoch = 0, sepoch = 0;
+  int fepoch = 0;
   int cap = 256;           // working-row capacity (entries of L and of U)
   bool factored = false;
   long launches = 0;
@@ -52,8 +54,8 @@ struct fos_ilut {
 };
 
 fos_ilut::~fos_ilut() {
-  void* p[] = {d_Lcol, d_Lval, d_Lcnt, d_Ucol, d_Uval, d_Ucnt, d_dinv, d_done, d_fdone, d_bdone,
-               d_ctr};
+  void* p[] = {d_Lcol, d_Lval, d_Lcnt, d_Ucol, d_Uval, d_Ucnt, d_dinv, d_done, d_z,
+               d_permF, d_permB, d_ctr};
   for (void* q : p)
     if (q) cudaFree(q);
   if (h_ctr) cudaFreeHost(h_ctr);
@@ -80,7 +82,7 @@ __device__ __forceinline__ bool wait_row(const int* flag, int j, int epoch, int*
   for (long it = 0; it < kSpinLimit; it++) {
     if (ld_acquire(flag + j) >= epoch) return true;
     if (*(volatile int*)(ctr + 3) == kErrTimeout) return false;
-    __nanosleep(64);
+    if (it > 8) __nanosleep(32);
   }
   atomicCAS(ctr + 3, 0, kErrTimeout);
   return false;
@@ -288,15 +290,8 @@ __global__ void __launch_bounds__(32 * kWarps) k_ilut_factor(
       __syncwarp();
       continue;
     }
-    // L part: the lfil largest multipliers (ilut.f:236-254)
-    const int keepl = min(len, lfil);
-    if (lane == 0) qsplit(lval, lcol, len, keepl);
-    __syncwarp();
-    for (int k = lane; k < keepl; k += 32) {
-      Lcol[(size_t)ii * slot + k] = lcol[k];
-      Lval[(size_t)ii * slot + k] = lval[k];
-    }
-    // U part: drop |w| <= droptol * tnorm keeping the order, then the largest (:258-287)
+    // U part first (the rows below wait for it): drop |w| <= droptol * tnorm keeping the
+    // order, keep the largest (ilut.f:258-287), publish U and the inverted pivot
     const double thr = __dmul_rn(droptol, tnorm);
     int cnt = 0;
     for (int c = 1; c < lenu; c += 32) {
@@ -328,51 +323,127 @@ __global__ void __launch_bounds__(32 * kWarps) k_ilut_factor(
       double w0 = uval[0];
       if (w0 == 0.0) w0 = __dmul_rn(__dadd_rn(0.0001, droptol), tnorm);
       dinv[ii] = 1.0 / w0;
-      Lcnt[ii] = keepl;
       Ucnt[ii] = nu;
     }
     __threadfence();
     __syncwarp();
     if (lane == 0) st_release(done + ii, epoch);
+    // L part afterwards, off the rows-below path: the lfil largest multipliers (:236-254);
+    // only the sweeps read it, after this kernel
+    const int keepl = min(len, lfil);
+    if (lane == 0) qsplit(lval, lcol, len, keepl);
+    __syncwarp();
+    for (int k = lane; k < keepl; k += 32) {
+      Lcol[(size_t)ii * slot + k] = lcol[k];
+      Lval[(size_t)ii * slot + k] = lval[k];
+    }
+    if (lane == 0) Lcnt[ii] = keepl;
+    __syncwarp();
   }
 }
 
-// lusol forward sweep (ilut.f:2300-2305): x_i = y_i - sum_k L_ik x_k, rows ascending
+// The sweeps publish each solved unknown by its own 64-bit store: the output vectors start
+// filled with kPending, a signalling-NaN pattern that no arithmetic produces (results that
+// would carry it are stored as the canonical NaN), and a row polls the unknowns it reads
+// until they stop being kPending.  One L2 round trip per dependency, no flags, no fences.
+constexpr unsigned long long kPending = 0x7ff4deadbeefcafeull;
+// warps of a sweep: about kLookahead levels' worth of rows in flight.  More only add warps
+// that spin on unknowns many levels ahead and load L2 with their polls.
+#ifndef FOS_ILUT_LOOKAHEAD
+#define FOS_ILUT_LOOKAHEAD 2
+#endif
+constexpr int kLookahead = FOS_ILUT_LOOKAHEAD;
+#ifndef FOS_ILUT_MIN_WARPS
+#define FOS_ILUT_MIN_WARPS 304
+#endif
+
+__device__ __forceinline__ double ld_poll(const double* p) {
+  double v;
+  asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_publish(double* p, double v) {
+  if (__double_as_longlong(v) == (long long)kPending) v = __longlong_as_double(0x7ff8000000000000ll);
+  asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
+}
+__device__ __forceinline__ bool pending(double v) {
+  return __double_as_longlong(v) == (long long)kPending;
+}
+// wait for an unknown: bounded spin, false (and the error word set) when the limit ran out
+__device__ __forceinline__ double wait_value(const double* x, int j, double v, int* ctr, bool& ok) {
+  for (long it = 0; pending(v); it++) {
+    if (it >= kSpinLimit) { atomicCAS(ctr + 3, 0, kErrTimeout); ok = false; return 0.0; }
+    if (*(volatile int*)(ctr + 3) == kErrTimeout) { ok = false; return 0.0; }
+    if (it > 8) __nanosleep(32);
+    v = ld_poll(x + j);
+  }
+  return v;
+}
+
+__global__ void k_fill_pending(long n, double* __restrict__ x) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) x[i] = __longlong_as_double((long long)kPending);
+}
+
+// sum_k A_ik x_k over a row's cnt stored entries, lanes over entries two at a time (both
+// loads in flight before either is waited for); fixed-order warp reduction
+__device__ __forceinline__ double row_dot(const int* __restrict__ col, const double* __restrict__ val,
+                                         int cnt, const double* x, int* ctr, int lane) {
+  double s = 0.0;
+  bool ok = true;
+  for (int k = lane; k < cnt; k += 64) {
+    const int j0 = col[k];
+    const bool two = k + 32 < cnt;
+    const int j1 = two ? col[k + 32] : j0;
+    double v0 = ld_poll(x + j0), v1 = ld_poll(x + j1);
+    v0 = wait_value(x, j0, v0, ctr, ok);
+    s += val[k] * v0;
+    if (two) {
+      v1 = wait_value(x, j1, v1, ctr, ok);
+      s += val[k + 32] * v1;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(~0u, s, o);
+  return s;
+}
+
+// lusol forward sweep (ilut.f:2300-2305): z_i = y_i - sum_k L_ik z_k into z (kPending on
+// entry), and x_i set to kPending for the backward sweep (x may be y: row i reads y_i only).
+// Rows are claimed in order of their level in the L dependency graph (perm): the rows in
+// flight are mostly independent, and a row's dependencies have lower levels, hence earlier
+// claims.
 __global__ void __launch_bounds__(256) k_ilut_fwd(int n, int lfil, const int* __restrict__ Lcol,
                                                   const double* __restrict__ Lval,
                                                   const int* __restrict__ Lcnt,
-                                                  const double* y, double* x,
-                                                  int* __restrict__ flag, int epoch,
+                                                  const int* __restrict__ perm,
+                                                  const double* y, double* z, double* x,
                                                   int* __restrict__ ctr) {
   const int lane = threadIdx.x & 31;
   const size_t slot = (size_t)(lfil > 0 ? lfil : 1);
   for (;;) {
-    int i = 0;
-    if (lane == 0) i = atomicAdd(ctr + 1, 1);
-    i = __shfl_sync(~0u, i, 0);
-    if (i >= n) return;
-    const int cnt = Lcnt[i];
-    double s = 0.0;
-    for (int k = lane; k < cnt; k += 32) {
-      const int j = Lcol[(size_t)i * slot + k];
-      if (wait_row(flag, j, epoch, ctr)) s += Lval[(size_t)i * slot + k] * x[j];
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(~0u, s, o);
+    int t = 0;
+    if (lane == 0) t = atomicAdd(ctr + 1, 1);
+    t = __shfl_sync(~0u, t, 0);
+    if (t >= n) return;
+    const int i = perm[t];
+    const double yi = y[i];  // own operand first, so its load overlaps the dependency polls
+    const double s = row_dot(Lcol + (size_t)i * slot, Lval + (size_t)i * slot, Lcnt[i], z, ctr, lane);
     if (lane == 0) {
-      x[i] = y[i] - s;
-      __threadfence();
-      st_release(flag + i, epoch);
+      x[i] = __longlong_as_double((long long)kPending);
+      st_publish(z + i, yi - s);
     }
   }
 }
 
-// lusol backward sweep (:2309-2315): x_i = dinv_i (x_i - sum_k U_ik x_k), rows descending
+// lusol backward sweep (:2309-2315): x_i = dinv_i (z_i - sum_k U_ik x_k) into x (kPending on
+// entry), rows claimed by level in the U dependency graph
 __global__ void __launch_bounds__(256) k_ilut_bwd(int n, int lfil, const int* __restrict__ Ucol,
                                                   const double* __restrict__ Uval,
                                                   const int* __restrict__ Ucnt,
-                                                  const double* __restrict__ dinv, double* x,
-                                                  int* __restrict__ flag, int epoch,
+                                                  const double* __restrict__ dinv,
+                                                  const int* __restrict__ perm,
+                                                  const double* __restrict__ z, double* x,
                                                   int* __restrict__ ctr) {
   const int lane = threadIdx.x & 31;
   const size_t slot = (size_t)(lfil > 0 ? lfil : 1);
@@ -381,20 +452,10 @@ __global__ void __launch_bounds__(256) k_ilut_bwd(int n, int lfil, const int* __
     if (lane == 0) t = atomicAdd(ctr + 2, 1);
     t = __shfl_sync(~0u, t, 0);
     if (t >= n) return;
-    const int i = n - 1 - t;
-    const int cnt = Ucnt[i];
-    double s = 0.0;
-    for (int k = lane; k < cnt; k += 32) {
-      const int j = Ucol[(size_t)i * slot + k];
-      if (wait_row(flag, j, epoch, ctr)) s += Uval[(size_t)i * slot + k] * x[j];
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(~0u, s, o);
-    if (lane == 0) {
-      x[i] = dinv[i] * (x[i] - s);
-      __threadfence();
-      st_release(flag + i, epoch);
-    }
+    const int i = perm[t];
+    const double zi = z[i], di = dinv[i];
+    const double s = row_dot(Ucol + (size_t)i * slot, Uval + (size_t)i * slot, Ucnt[i], x, ctr, lane);
+    if (lane == 0) st_publish(x + i, di * (zi - s));
   }
 }
 
@@ -457,17 +518,16 @@ extern "C" int fos_ilut_create(fos_ilut** out, int n, int lfil) {
   rc = rc ? rc : alloc(&f->d_Ucnt, n);
   rc = rc ? rc : alloc(&f->d_dinv, n);
   rc = rc ? rc : alloc(&f->d_done, n);
-  rc = rc ? rc : alloc(&f->d_fdone, n);
-  rc = rc ? rc : alloc(&f->d_bdone, n);
+  rc = rc ? rc : alloc(&f->d_z, n);
+  rc = rc ? rc : alloc(&f->d_permF, n);
+  rc = rc ? rc : alloc(&f->d_permB, n);
   rc = rc ? rc : alloc(&f->d_ctr, 8);
   if (!rc && cudaMallocHost((void**)&f->h_ctr, 8 * sizeof(int)) != cudaSuccess) {
     fos_set_error("fos_ilut_create: cudaMallocHost failed");
     rc = -100;
   }
   if (!rc) {
-    if (cudaMemset(f->d_done, 0, sizeof(int) * n) != cudaSuccess ||
-        cudaMemset(f->d_fdone, 0, sizeof(int) * n) != cudaSuccess ||
-        cudaMemset(f->d_bdone, 0, sizeof(int) * n) != cudaSuccess) {
+    if (cudaMemset(f->d_done, 0, sizeof(int) * n) != cudaSuccess) {
       fos_set_error("fos_ilut_create: cudaMemset failed");
       rc = -100;
     }
@@ -481,6 +541,51 @@ extern "C" int fos_ilut_create(fos_ilut** out, int n, int lfil) {
 }
 
 extern "C" void fos_ilut_destroy(fos_ilut* f) { delete f; }
+
+// Claim orders of the two sweeps: rows sorted (stably) by their level in the L graph (1 +
+// the largest level among the rows its stored L entries read, rows ascending) and in the U
+// graph (the same over U entries, rows descending), computed here on the host from the
+// stored columns.
+static int solve_orders(fos_ilut* f, cudaStream_t s) {
+  const int n = f->n;
+  const size_t slot = (size_t)std::max(f->lfil, 1);
+  std::vector<int> lcnt(n), ucnt(n), lcol(slot * n), ucol(slot * n);
+  FOS_CUDA(cudaMemcpyAsync(lcnt.data(), f->d_Lcnt, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  FOS_CUDA(cudaMemcpyAsync(ucnt.data(), f->d_Ucnt, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  FOS_CUDA(cudaMemcpyAsync(lcol.data(), f->d_Lcol, sizeof(int) * slot * n, cudaMemcpyDeviceToHost, s));
+  FOS_CUDA(cudaMemcpyAsync(ucol.data(), f->d_Ucol, sizeof(int) * slot * n, cudaMemcpyDeviceToHost, s));
+  FOS_CUDA(cudaStreamSynchronize(s));
+  auto by_level = [n](const std::vector<int>& lv, int nlev, std::vector<int>& perm) {
+    std::vector<int> start(nlev + 2, 0);
+    for (int i = 0; i < n; i++) start[lv[i] + 1]++;
+    for (int l = 0; l <= nlev; l++) start[l + 1] += start[l];
+    perm.resize(n);
+    for (int i = 0; i < n; i++) perm[start[lv[i]]++] = i;
+  };
+  std::vector<int> lev(n, 0), permF, permB;
+  int nl = 0;
+  for (int i = 0; i < n; i++) {
+    int m = 0;
+    for (int k = 0; k < lcnt[i]; k++) m = std::max(m, lev[lcol[(size_t)i * slot + k]]);
+    lev[i] = m + 1;
+    nl = std::max(nl, m + 1);
+  }
+  by_level(lev, nl, permF);
+  int nu = 0;
+  for (int i = n - 1; i >= 0; i--) {
+    int m = 0;
+    for (int k = 0; k < ucnt[i]; k++) m = std::max(m, lev[ucol[(size_t)i * slot + k]]);
+    lev[i] = m + 1;  // lev now holds U levels (rows above i are final)
+    nu = std::max(nu, m + 1);
+  }
+  by_level(lev, nu, permB);
+  f->nlevF = nl;
+  f->nlevB = nu;
+  FOS_CUDA(cudaMemcpyAsync(f->d_permF, permF.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  FOS_CUDA(cudaMemcpyAsync(f->d_permB, permB.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  FOS_CUDA(cudaStreamSynchronize(s));
+  return 0;
+}
 
 int fos_ilut_factor_on(fos_ilut* f, const int* ia, const int* ja, const double* a,
                        double droptol, cudaStream_t s) {
@@ -530,6 +635,8 @@ int fos_ilut_factor_on(fos_ilut* f, const int* ia, const int* ja, const double* 
       continue;
     }
     f->factored = err == 0;
+    if (f->factored)
+      if (int rc = solve_orders(f, s)) return rc;
     if (err == kErrZeroRow) {
       fos_set_error("fos_ilut_factor_dev: zero row " + std::to_string(row + 1));
       return -5;
@@ -548,13 +655,18 @@ int fos_ilut_solve_on(fos_ilut* f, const double* y, double* x, cudaStream_t s) {
     return -1;
   }
   FOS_CUDA(cudaMemsetAsync(f->d_ctr, 0, 4 * sizeof(int), s));
-  f->sepoch++;
-  const int grid = grid_for((const void*)k_ilut_fwd, 256, 0, 8, f->n);
-  k_ilut_fwd<<<grid, 256, 0, s>>>(f->n, f->lfil, f->d_Lcol, f->d_Lval, f->d_Lcnt, y, x,
-                                  f->d_fdone, f->sepoch, f->d_ctr);
-  k_ilut_bwd<<<grid, 256, 0, s>>>(f->n, f->lfil, f->d_Ucol, f->d_Uval, f->d_Ucnt, f->d_dinv, x,
-                                  f->d_bdone, f->sepoch, f->d_ctr);
-  f->launches += 2;
+  k_fill_pending<<<(f->n + 255) / 256, 256, 0, s>>>(f->n, f->d_z);
+  // rows in flight: kLookahead levels of the average width, at least one CTA per SM
+  auto sweep_grid = [&](int nlev) {
+    const long width = (f->n + std::max(nlev, 1) - 1) / std::max(nlev, 1);
+    const long warps = std::max((long)FOS_ILUT_MIN_WARPS, kLookahead * width);
+    return std::min(grid_for((const void*)k_ilut_fwd, 256, 0, 8, f->n), (int)((warps + 7) / 8));
+  };
+  k_ilut_fwd<<<sweep_grid(f->nlevF), 256, 0, s>>>(f->n, f->lfil, f->d_Lcol, f->d_Lval, f->d_Lcnt,
+                                                  f->d_permF, y, f->d_z, x, f->d_ctr);
+  k_ilut_bwd<<<sweep_grid(f->nlevB), 256, 0, s>>>(f->n, f->lfil, f->d_Ucol, f->d_Uval, f->d_Ucnt,
+                                                  f->d_dinv, f->d_permB, f->d_z, x, f->d_ctr);
+  f->launches += 3;
   FOS_CUDA(cudaGetLastError());
   return 0;
 }
@@ -646,6 +758,8 @@ extern "C" int fos_ilut_info(const fos_ilut* f, long* out) {
   out[1] = f->lfil;
   out[2] = f->cap;
   out[3] = f->launches;
+  out[4] = f->nlevF;
+  out[5] = f->nlevB;
   return 0;
 }
 

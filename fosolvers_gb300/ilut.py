@@ -50,7 +50,7 @@ class ILU:
 
     @property
     def lfil(self) -> int:
-        out = (C.c_long * 4)()
+        out = (C.c_long * 6)()
         _lib.lib().fos_ilut_info(self.handle, out)
         return int(out[1])
 

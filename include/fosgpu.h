@@ -196,7 +196,8 @@ int fos_ilut_status(fos_ilut* f);
  * diagonal, jlu(1:n+1) row pointers, ju(1:n) the start of each U row; returns the used
  * length (all three pointers null: only the length), < 0 on error */
 long fos_ilut_copy(const fos_ilut* f, double* alu, int* jlu, int* ju, long iwk);
-/* out[0..3] = n, lfil, working-row capacity, kernels launched */
+/* out[0..5] = n, lfil, working-row capacity, kernels launched, levels of the L and U
+ * dependency graphs (the sweeps claim rows level by level) */
 int fos_ilut_info(const fos_ilut* f, long* out);
 void fos_ilut_destroy(fos_ilut* f);
 /* ILUT parameters of a context created with FOS_PREC_ILUT (fopbc's PBC_PREC_FILL = 50 and

@@ -95,7 +95,7 @@ def test_long_rows_grow_the_working_capacity(cuda):
     p = gpu_ilu(n, a, ja, ia, n, 0.0)
     from fosolvers_gb300 import _lib
     import ctypes as C
-    info = (C.c_long * 4)()
+    info = (C.c_long * 6)()
     _lib.lib().fos_ilut_info(p.handle, info)
     assert info[2] > 256
     assert_same_factors(p, ref)
