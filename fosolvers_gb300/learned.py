@@ -127,7 +127,8 @@ def smooth_field(x: np.ndarray, rng, nwaves: int = 3) -> np.ndarray:
 
 def generate_pairs(n_meshes: int, seed: int = 0, sizes=(12, 20), newton_iters: int = 2,
                    bdf_steps: int = 2, cfl=(0.03, 0.3), lin_rtol: float = 1e-6, flags: int = 0,
-                   states=("random", "sine"), n_random: int = 3):
+                   states=("random", "sine"), n_random: int = 3, lean: bool = False,
+                   keep_u: bool = True):
     """(y, v, t, gamma) training samples on the device, from the plain solver.
 
     At each sampled state of a BDF1 run (seeded meshes, random piecewise or sinusoidal
@@ -137,6 +138,11 @@ def generate_pairs(n_meshes: int, seed: int = 0, sizes=(12, 20), newton_iters: i
       * operator samples: t = w for random w (white noise mixed with a smooth field) and
         v = J_G w from the fused finite-difference Jv kernel -- exact pairs that cover the
         directions FGMRES feeds the preconditioner besides the first residual.
+    lean: once a mesh's samples are made, they move to a fresh context on the same grid
+    (same internal order) that has never factored anything, and the generating context
+    with its Jacobian and ILU(0) storage (~2 KB per cell) is freed -- what lets hundreds
+    of meshes' samples stay on the device.  keep_u=False drops u (only the
+    ILU-then-correction form trains on it).
     Returns a list of Sample."""
     import torch
     from . import mesh as M
@@ -146,6 +152,7 @@ def generate_pairs(n_meshes: int, seed: int = 0, sizes=(12, 20), newton_iters: i
     gen.manual_seed(seed)
     out = []
     for k in range(n_meshes):
+        first = len(out)
         n = int(rng.integers(sizes[0], sizes[1] + 1))
         m = M.box_mesh(n, n, n, jitter=0.1, seed=seed * 1000 + k)
         xc = m.centroids()
@@ -171,8 +178,10 @@ def generate_pairs(n_meshes: int, seed: int = 0, sizes=(12, 20), newton_iters: i
                 x = torch.empty_like(b)
                 opts = ctx.bdf_defaults(precond=1, lin_rtol=lin_rtol, max_restarts=8)
                 ctx.linear_solve(yk, f, dt, b, x, opts)  # leaves ILU(0) factored at (yk, dt)
-                u = torch.empty_like(b)
-                ctx.psol_dev(b, u)
+                u = None
+                if keep_u:
+                    u = torch.empty_like(b)
+                    ctx.psol_dev(b, u)
                 out.append(Sample(ctx, yk.clone(), b, x, dt, u))
                 if it + 1 < newton_iters:
                     yk = yk + x
@@ -187,15 +196,23 @@ def generate_pairs(n_meshes: int, seed: int = 0, sizes=(12, 20), newton_iters: i
                 w = w.reshape(-1).contiguous()
                 v = torch.empty_like(w)
                 ctx.jv_dev(0.0, yn, f, w, v, 1.0, -dt, ynorm)
-                u = torch.empty_like(v)
-                ctx.psol_dev(v, u)
+                u = None
+                if keep_u:
+                    u = torch.empty_like(v)
+                    ctx.psol_dev(v, u)
                 out.append(Sample(ctx, yn.clone(), v, w, dt, u))
             rc, _ = ctx.bdf_run(y, ctx.bdf_defaults(order=1, dt=dt, nsteps=1))
             if rc != 0:
                 break
+        if lean:
+            light = FOEuler(grid, flags=flags)
+            out[first:] = [sm._replace(ctx=light) for sm in out[first:]]
+            ctx.close()
+            del ctx
+            torch.cuda.empty_cache()
     # keep finite samples only (a state the solver could not advance is dropped)
     return [sm for sm in out
-            if all(bool(torch.isfinite(x).all()) for x in (sm.y, sm.b, sm.t, sm.u))]
+            if all(bool(torch.isfinite(x).all()) for x in (sm.y, sm.b, sm.t, sm.u) if x is not None)]
 
 
 def train(gnn: GNN, pairs, epochs: int = 20, lr: float = 2e-3, seed: int = 0, log=None,
@@ -272,9 +289,19 @@ def _main(argv=None):
     ap.add_argument("--cfl", type=float, nargs=2, default=(0.03, 0.3))
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--flags", type=int, default=0)
+    ap.add_argument("--newton-iters", type=int, default=2)
+    ap.add_argument("--bdf-steps", type=int, default=2)
+    ap.add_argument("--n-random", type=int, default=3)
+    ap.add_argument("--lean", action="store_true",
+                    help="free each generating context's preconditioner storage (many meshes)")
+    ap.add_argument("--tols", type=float, nargs="+", default=(1e-3, 1e-6))
+    ap.add_argument("--compare", default=None,
+                    help="also evaluate these weights on the same held-out solves")
     a = ap.parse_args(argv)
     t0 = time.time()
-    tr = generate_pairs(a.meshes, seed=a.seed, sizes=tuple(a.sizes), cfl=tuple(a.cfl), flags=a.flags)
+    tr = generate_pairs(a.meshes, seed=a.seed, sizes=tuple(a.sizes), cfl=tuple(a.cfl), flags=a.flags,
+                        newton_iters=a.newton_iters, bdf_steps=a.bdf_steps, n_random=a.n_random,
+                        lean=a.lean, keep_u=not a.lean)
     te = generate_pairs(a.test_meshes, seed=a.seed + 1000, sizes=(a.test_size, a.test_size),
                         cfl=tuple(a.cfl), flags=a.flags)
     print(f"samples: {len(tr)} training, {len(te)} held out ({time.time() - t0:.1f} s)", flush=True)
@@ -286,13 +313,22 @@ def _main(argv=None):
     g.save(a.out)
     print("saved", a.out, flush=True)
     del tr
-    for s in te:
-        s.ctx.attach_gnn(g)
-    for tol in (1e-3, 1e-6):
+    nets = [("learned", g)]
+    if a.compare:
+        g0 = GNN(seed=0)
+        g0.load(a.compare)
+        nets.append(("compared", g0))
+    for tol in a.tols:
         r = {}
-        for name, pc in (("none", 0), ("learned", 3), ("ILU(0)", 1), ("learned+fallback", 2)):
+        for name, pc in (("none", 0), ("ILU(0)", 1)):
             its, fb, ms = krylov_iterations(te, pc, lin_rtol=tol, timing=True)
             r[name] = {"iterations": sum(its), "ms": round(ms, 1), "fallbacks": fb}
+        for label, net in nets:
+            for s in te:
+                s.ctx.attach_gnn(net)
+            for name, pc in ((label, 3), (label + "+fallback", 2)):
+                its, fb, ms = krylov_iterations(te, pc, lin_rtol=tol, timing=True)
+                r[name] = {"iterations": sum(its), "ms": round(ms, 1), "fallbacks": fb}
         print(f"held-out ({len(te)} solves at {a.test_size}^3 x 6) at {tol:g}: {r}", flush=True)
 
 
