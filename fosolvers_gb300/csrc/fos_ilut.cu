@@ -41,6 +41,7 @@ struct fos_ilut {
   double* d_dinv = nullptr;
   int* d_done = nullptr;   // factor: epoch of the factorisation that published the row
   double* d_z = nullptr;   // forward-sweep result (kPending before each solve)
+  int* d_levL = nullptr;   // level of every row in the L graph, published by the factor
   int* d_permF = nullptr;  // rows by forward / backward level: the solves' claim order
   int* d_permB = nullptr;
   int nlevF = 0, nlevB = 0;
@@ -55,7 +56,7 @@ struct fos_ilut {
 
 fos_ilut::~fos_ilut() {
   void* p[] = {d_Lcol, d_Lval, d_Lcnt, d_Ucol, d_Uval, d_Ucnt, d_dinv, d_done, d_z,
-               d_permF, d_permB, d_ctr};
+               d_levL, d_permF, d_permB, d_ctr};
   for (void* q : p)
     if (q) cudaFree(q);
   if (h_ctr) cudaFreeHost(h_ctr);
@@ -146,7 +147,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_ilut_factor(
     int lfil, double droptol, int cap, int epoch, int* __restrict__ Lcol,
     double* __restrict__ Lval, int* __restrict__ Lcnt, int* __restrict__ Ucol,
     double* __restrict__ Uval, int* __restrict__ Ucnt, double* __restrict__ dinv,
-    int* __restrict__ done, int* __restrict__ ctr) {
+    int* __restrict__ levL, int* __restrict__ done, int* __restrict__ ctr) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned hmask = 4u * cap - 1u;
@@ -206,8 +207,10 @@ __global__ void __launch_bounds__(32 * kWarps) k_ilut_factor(
       }
       if (lenl > cap || lenu > cap) ok = false;
     }
-    // elimination of the L entries in increasing column order (ilut.f:150-226)
-    int jj = 0;
+    // elimination of the L entries in increasing column order (ilut.f:150-226); lev = the
+    // largest L-graph level among the rows of stored multipliers (a superset of the kept
+    // ones, so 1 + lev is a valid level for the sweeps' claim order)
+    int jj = 0, lev = 0;
     while (ok && jj < lenl) {
       int best = INT_MAX, bidx = -1;
       for (int k = jj + lane; k < lenl; k += 32)
@@ -238,6 +241,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_ilut_factor(
       (void)ld_acquire(done + jrow);
       const double fact = __dmul_rn(lval[jj], dinv[jrow]);
       if (fabs(fact) <= droptol) { jj++; __syncwarp(); continue; }
+      lev = max(lev, levL[jrow]);
       const int ulen = Ucnt[jrow];
       const int* uc = Ucol + (size_t)jrow * slot;
       const double* uv = Uval + (size_t)jrow * slot;
@@ -284,6 +288,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_ilut_factor(
         Lcnt[ii] = 0;
         Ucnt[ii] = 0;
         dinv[ii] = 0.0;
+        levL[ii] = 1;
         __threadfence();
         st_release(done + ii, epoch);
       }
@@ -324,6 +329,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_ilut_factor(
       if (w0 == 0.0) w0 = __dmul_rn(__dadd_rn(0.0001, droptol), tnorm);
       dinv[ii] = 1.0 / w0;
       Ucnt[ii] = nu;
+      levL[ii] = lev + 1;
     }
     __threadfence();
     __syncwarp();
@@ -386,7 +392,9 @@ __global__ void k_fill_pending(long n, double* __restrict__ x) {
 }
 
 // sum_k A_ik x_k over a row's cnt stored entries, lanes over entries two at a time (both
-// loads in flight before either is waited for); fixed-order warp reduction
+// loads in flight before either is waited for); fixed-order warp reduction.  A wait that
+// ran out makes the sum NaN, so the failure reaches callers that only look at the result
+// (the Krylov driver's non-finite checks) as well as fos_ilut_status.
 __device__ __forceinline__ double row_dot(const int* __restrict__ col, const double* __restrict__ val,
                                          int cnt, const double* x, int* ctr, int lane) {
   double s = 0.0;
@@ -403,6 +411,7 @@ __device__ __forceinline__ double row_dot(const int* __restrict__ col, const dou
       s += val[k + 32] * v1;
     }
   }
+  if (!ok) s = __longlong_as_double(0x7ff8000000000000ll);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(~0u, s, o);
   return s;
@@ -519,6 +528,7 @@ extern "C" int fos_ilut_create(fos_ilut** out, int n, int lfil) {
   rc = rc ? rc : alloc(&f->d_dinv, n);
   rc = rc ? rc : alloc(&f->d_done, n);
   rc = rc ? rc : alloc(&f->d_z, n);
+  rc = rc ? rc : alloc(&f->d_levL, n);
   rc = rc ? rc : alloc(&f->d_permF, n);
   rc = rc ? rc : alloc(&f->d_permB, n);
   rc = rc ? rc : alloc(&f->d_ctr, 8);
@@ -542,19 +552,13 @@ extern "C" int fos_ilut_create(fos_ilut** out, int n, int lfil) {
 
 extern "C" void fos_ilut_destroy(fos_ilut* f) { delete f; }
 
-// Claim orders of the two sweeps: rows sorted (stably) by their level in the L graph (1 +
-// the largest level among the rows its stored L entries read, rows ascending) and in the U
-// graph (the same over U entries, rows descending), computed here on the host from the
-// stored columns.
+// Claim orders of the two sweeps: rows sorted (stably) by their level in the L graph
+// (published by the factor kernel) and in the U graph (1 + the largest U level among the
+// rows its U entries read), computed here on the host from the stored U columns, fetched
+// in chunks of rows from the bottom up so host memory stays small at any size.
 static int solve_orders(fos_ilut* f, cudaStream_t s) {
   const int n = f->n;
   const size_t slot = (size_t)std::max(f->lfil, 1);
-  std::vector<int> lcnt(n), ucnt(n), lcol(slot * n), ucol(slot * n);
-  FOS_CUDA(cudaMemcpyAsync(lcnt.data(), f->d_Lcnt, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
-  FOS_CUDA(cudaMemcpyAsync(ucnt.data(), f->d_Ucnt, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
-  FOS_CUDA(cudaMemcpyAsync(lcol.data(), f->d_Lcol, sizeof(int) * slot * n, cudaMemcpyDeviceToHost, s));
-  FOS_CUDA(cudaMemcpyAsync(ucol.data(), f->d_Ucol, sizeof(int) * slot * n, cudaMemcpyDeviceToHost, s));
-  FOS_CUDA(cudaStreamSynchronize(s));
   auto by_level = [n](const std::vector<int>& lv, int nlev, std::vector<int>& perm) {
     std::vector<int> start(nlev + 2, 0);
     for (int i = 0; i < n; i++) start[lv[i] + 1]++;
@@ -562,27 +566,35 @@ static int solve_orders(fos_ilut* f, cudaStream_t s) {
     perm.resize(n);
     for (int i = 0; i < n; i++) perm[start[lv[i]]++] = i;
   };
-  std::vector<int> lev(n, 0), permF, permB;
+  std::vector<int> lev(n), perm;
+  FOS_CUDA(cudaMemcpyAsync(lev.data(), f->d_levL, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  FOS_CUDA(cudaStreamSynchronize(s));
   int nl = 0;
-  for (int i = 0; i < n; i++) {
-    int m = 0;
-    for (int k = 0; k < lcnt[i]; k++) m = std::max(m, lev[lcol[(size_t)i * slot + k]]);
-    lev[i] = m + 1;
-    nl = std::max(nl, m + 1);
-  }
-  by_level(lev, nl, permF);
-  int nu = 0;
-  for (int i = n - 1; i >= 0; i--) {
-    int m = 0;
-    for (int k = 0; k < ucnt[i]; k++) m = std::max(m, lev[ucol[(size_t)i * slot + k]]);
-    lev[i] = m + 1;  // lev now holds U levels (rows above i are final)
-    nu = std::max(nu, m + 1);
-  }
-  by_level(lev, nu, permB);
+  for (int i = 0; i < n; i++) nl = std::max(nl, lev[i]);
+  by_level(lev, nl, perm);
   f->nlevF = nl;
+  FOS_CUDA(cudaMemcpyAsync(f->d_permF, perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  FOS_CUDA(cudaStreamSynchronize(s));
+  const int chunk = (int)std::max<size_t>(1, (size_t)(16u << 20) / (slot * sizeof(int)));
+  std::vector<int> cnt(chunk), col(slot * chunk);
+  int nu = 0;
+  for (int hi = n; hi > 0; hi -= chunk) {
+    const int lo = std::max(0, hi - chunk), m = hi - lo;
+    FOS_CUDA(cudaMemcpyAsync(cnt.data(), f->d_Ucnt + lo, sizeof(int) * m, cudaMemcpyDeviceToHost, s));
+    FOS_CUDA(cudaMemcpyAsync(col.data(), f->d_Ucol + slot * lo, sizeof(int) * slot * m,
+                             cudaMemcpyDeviceToHost, s));
+    FOS_CUDA(cudaStreamSynchronize(s));
+    for (int i = hi - 1; i >= lo; i--) {  // rows above i are final: U columns are > i
+      int mx = 0;
+      const int* c = col.data() + slot * (i - lo);
+      for (int k = 0; k < cnt[i - lo]; k++) mx = std::max(mx, lev[c[k]]);
+      lev[i] = mx + 1;
+      nu = std::max(nu, mx + 1);
+    }
+  }
+  by_level(lev, nu, perm);
   f->nlevB = nu;
-  FOS_CUDA(cudaMemcpyAsync(f->d_permF, permF.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
-  FOS_CUDA(cudaMemcpyAsync(f->d_permB, permB.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  FOS_CUDA(cudaMemcpyAsync(f->d_permB, perm.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
   FOS_CUDA(cudaStreamSynchronize(s));
   return 0;
 }
@@ -624,7 +636,7 @@ int fos_ilut_factor_on(fos_ilut* f, const int* ia, const int* ja, const double* 
     k_ilut_factor<<<grid, 32 * kWarps, smem, s>>>(f->n, ia, ja, a, f->lfil, droptol, f->cap,
                                                   f->fepoch, f->d_Lcol, f->d_Lval, f->d_Lcnt,
                                                   f->d_Ucol, f->d_Uval, f->d_Ucnt, f->d_dinv,
-                                                  f->d_done, f->d_ctr);
+                                                  f->d_levL, f->d_done, f->d_ctr);
     f->launches++;
     FOS_CUDA(cudaGetLastError());
     FOS_CUDA(cudaMemcpyAsync(f->h_ctr, f->d_ctr, 8 * sizeof(int), cudaMemcpyDeviceToHost, s));
