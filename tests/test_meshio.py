@@ -110,6 +110,18 @@ def test_reads_the_duct_example_mesh():
     assert np.abs(acc).max() <= 1e-12 * np.abs(an).max() * 10
 
 
+MESH_SIMPLE = Path("/root/reference/src/test/data/mesh_simple.vtk")
+
+
+@pytest.mark.skipif(not MESH_SIMPLE.exists(), reason="reference test data not present")
+def test_reads_the_reference_simple_vtk_mesh():
+    """src/test/readVTK1.f90:10-22: the four triangles of data/mesh_simple.vtk come out with
+    1-based nodes (1,3,2), (1,4,3), (1,2,4), (2,3,4), all TRI with 3 nodes."""
+    m, _ = IO.read_vtk(MESH_SIMPLE)
+    np.testing.assert_array_equal(m.iNE[:, :3], [[1, 3, 2], [1, 4, 3], [1, 2, 4], [2, 3, 4]])
+    assert np.all(m.sE == IO.TRI) and np.all(m.nNE == 3)
+
+
 def test_vtk_round_trip_with_cell_and_point_data(tmp_path):
     m = M.box_mesh(3, 2, 2, jitter=0.05, seed=1)
     rng = np.random.default_rng(0)
