@@ -329,8 +329,13 @@ struct Driver {
     return 0;
   }
   double gamma_cur = 0.0;  // gamma of the current linear solve (input of the learned preconditioner)
-  int psolve(const double* y, const double* r, double* z) {
+  // z = M^-1 r; with d_zsq (plain ILU(0) only, else ignored) also ||z||^2 into d_zsq from
+  // the apply's own pass over z -- the norm the next Jv of z needs.  Returns in *have_sq
+  // whether it did.
+  int psolve(const double* y, const double* r, double* z, double* d_zsq = nullptr,
+             bool* have_sq = nullptr) {
     st.n_psol++;
+    if (have_sq) *have_sq = false;
     if (pc == 0) {
       FOS_CUDA(cudaMemcpyAsync(z, r, sizeof(double) * wk.N, cudaMemcpyDeviceToDevice, c->stream));
       return 0;
@@ -341,7 +346,8 @@ struct Driver {
       if (int rc = fos_ilu_apply(c, r, wk.u)) return rc;
       return fos_gnn_precond(c, y, wk.u, gamma_cur, z);
     }
-    return fos_ilu_apply(c, r, z);
+    if (have_sq) *have_sq = d_zsq != nullptr;
+    return fos_ilu_apply(c, r, z, d_zsq);
   }
   int ensure_pset() {
     if (pset_done) return 0;
@@ -354,11 +360,12 @@ struct Driver {
     return c->ilu_ierr ? 3 : 0;
   }
   // w = J_G v at state y with f(y) = fy
+  // w = J_G v by the finite difference; have_sq: ||v||^2 is already in c->d_scal[0]
   int jv(const double* y, const double* fy, const double* v, double* w, double gamma,
-         double ynorm) {
+         double ynorm, bool have_sq = false) {
     st.n_jv++;
     st.n_rhs++;
-    int rc = fos_norm2_dev(c, v, wk.N, c->d_scal);
+    int rc = have_sq ? 0 : fos_norm2_dev(c, v, wk.N, c->d_scal);
     if (rc) return rc;
     rc = fos_jv_sigma(c, c->d_scal, ynorm, eps);
     if (rc) return rc;
@@ -399,12 +406,9 @@ struct Driver {
         gamma_step = gamma;
         y_step = y;
       }
-      // ||G|| for the linear tolerance: ||b||^2 via the norm kernel
-      if ((rc = fos_norm2_dev(c, wk.b, N, c->d_scal + 16))) return rc;
-      double bn2 = 0.0;
-      if ((rc = fetch(c->d_scal + 16, &bn2, 1))) return rc;
+      // ||b|| = ||G|| (b = -G) for the linear tolerance and GMRES's first basis vector
       int its = 0;
-      rc = gmres(y, wk.f, gamma, std::sqrt(hb[1]), std::sqrt(bn2), &its);
+      rc = gmres(y, wk.f, gamma, std::sqrt(hb[1]), gn, &its);
       st.n_lin_iters += its;
       st.n_newton++;
       if (rc < 0) return rc;
@@ -451,9 +455,10 @@ struct Driver {
       for (int j = 0; j < m; j++) {
         double* vj = wk.V + (size_t)j * N;
         double* zj = wk.Z + (size_t)j * N;
-        int rc = psolve(y, vj, zj);
+        bool have_sq = false;
+        int rc = psolve(y, vj, zj, c->d_scal, &have_sq);
         if (rc) return rc;
-        rc = jv(y, fy, zj, wk.w, gamma, ynorm);
+        rc = jv(y, fy, zj, wk.w, gamma, ynorm, have_sq);
         if (rc) return rc;
         (*its)++;
         const int nv = j + 1;

@@ -134,6 +134,7 @@ inline void fos_launch(fos_ctx* c, void (*k)(KArgs...), dim3 g, dim3 b, Args... 
 int fos_residual_launch(fos_ctx* c, const double* y, const double* v, const double* d_s,
                         const double* fy, double* out, double a, double b, int mode);
 int fos_norm2_dev(fos_ctx* c, const double* x, long n, double* d_out_sq);
+int fos_sum_partials(fos_ctx* c, int np, double* d_out);  // sum of c->d_red[0..np) in order
 int fos_permute(fos_ctx* c, const double* in, double* out, int dir);
 int fos_jv_sigma(fos_ctx* c, double* d_scal, double ynorm, double eps);
 int fos_prim_hl_launch(fos_ctx* c, const double* y);  // FP32 (hi, lo) primitives
@@ -143,7 +144,8 @@ int fos_gnn_precond(fos_ctx* c, const double* y, const double* r, double gamma, 
 int fos_jac_setup(fos_ctx* c);
 int fos_jac_assemble(fos_ctx* c, const double* y);
 int fos_ilu_factor(fos_ctx* c, double gamma);
-int fos_ilu_apply(fos_ctx* c, const double* r, double* z);
+// z = P^-1 r; with d_zsq also ||z||^2 into d_zsq (device), from the same pass over z
+int fos_ilu_apply(fos_ctx* c, const double* r, double* z, double* d_zsq = nullptr);
 // fos_ilut.cu: the Euler preconditioner with ILUT (FOS_PREC_ILUT)
 int fos_ilut_ctx_factor(fos_ctx* c, double gamma);
 int fos_ilut_ctx_apply(fos_ctx* c, const double* r, double* z);

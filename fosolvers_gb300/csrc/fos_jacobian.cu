@@ -529,6 +529,36 @@ __global__ void k_ilu_out(int nC, const int* __restrict__ ipos, const TF* __rest
   for (int a = 0; a < 5; a++) z[(size_t)a * nC + i] = to64<TF>(src[a]);
 }
 
+// k_ilu_out plus the partial sums of z^2 (the norm the finite-difference Jv of z needs):
+// fixed grid (kRedBlocks x kRedThreads), cells by grid stride, one partial per block in a
+// fixed order, so the sum is deterministic
+template <typename TF>
+__global__ void __launch_bounds__(kRedThreads) k_ilu_out_sq(int nC, const int* __restrict__ ipos,
+                                                            const TF* __restrict__ zv,
+                                                            double* __restrict__ z,
+                                                            double* __restrict__ part) {
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nC; i += gridDim.x * blockDim.x) {
+    const TF* src = zv + 8 * (size_t)ipos[i];
+#pragma unroll
+    for (int a = 0; a < 5; a++) {
+      const double v = to64<TF>(src[a]);
+      z[(size_t)a * nC + i] = v;
+      acc = fma(v, v, acc);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  __shared__ double sh[kRedThreads / 32];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kRedThreads / 32; w++) t += sh[w];
+    part[blockIdx.x] = t;
+  }
+}
+
 // Triangular sweeps in position space, five lanes per block row (lane a owns component
 // a and reads row a of every 5x5 block).  The forward sweep overwrites rv with y in place
 // (a row reads only its own rv and earlier rows' y).
@@ -830,7 +860,8 @@ int fos_ilu_factor(fos_ctx* c, double gamma) {
 }
 
 template <typename TF>
-static int ilu_apply_t(fos_ctx* c, const TF* LU, const double* r, double* z) {
+static int ilu_apply_t(fos_ctx* c, const TF* LU, const double* r, double* z,
+                       double* d_zsq = nullptr) {
   TF* yv = reinterpret_cast<TF*>(c->d_ilu_tmp);
   TF* zv = yv + 8 * (size_t)c->nC;
   fos_launch(c, k_ilu_in<TF>, nb(c->nC, 256), 256, c->nC, (const int*)c->d_ipos, r, yv);
@@ -848,16 +879,25 @@ static int ilu_apply_t(fos_ctx* c, const TF* LU, const double* r, double* z) {
     fos_launch(c, k_ilu_bwd<TF>, nb_rows5(n), kT, n, rows, c->lev_b[lc], (const int*)c->d_prow,
                (const int*)c->d_pcol, (const int*)c->d_pdiag, LU, (const TF*)yv, zv);
   }
+  if (d_zsq) {
+    fos_launch(c, k_ilu_out_sq<TF>, kRedBlocks, kRedThreads, c->nC, (const int*)c->d_ipos,
+               (const TF*)zv, z, c->d_red);
+    FOS_LAUNCH_CHECK();
+    return fos_sum_partials(c, kRedBlocks, d_zsq);
+  }
   fos_launch(c, k_ilu_out<TF>, nb(c->nC, 256), 256, c->nC, (const int*)c->d_ipos,
              (const TF*)zv, z);
   FOS_LAUNCH_CHECK();
   return 0;
 }
 
-int fos_ilu_apply(fos_ctx* c, const double* r, double* z) {
-  if (c->flags & FOS_PREC_ILUT) return fos_ilut_ctx_apply(c, r, z);
-  if (c->flags & FOS_ILU_FP32) return ilu_apply_t<float>(c, c->d_LU32, r, z);
-  return ilu_apply_t<double>(c, c->d_LU, r, z);
+int fos_ilu_apply(fos_ctx* c, const double* r, double* z, double* d_zsq) {
+  if (c->flags & FOS_PREC_ILUT) {
+    if (int rc = fos_ilut_ctx_apply(c, r, z)) return rc;
+    return d_zsq ? fos_norm2_dev(c, z, 5L * c->nC, d_zsq) : 0;
+  }
+  if (c->flags & FOS_ILU_FP32) return ilu_apply_t<float>(c, c->d_LU32, r, z, d_zsq);
+  return ilu_apply_t<double>(c, c->d_LU, r, z, d_zsq);
 }
 
 // Block Jacobian in position space: rowptr (nC+1) / col (positions) / 25-value blocks.

@@ -552,6 +552,12 @@ int fos_norm2_dev(fos_ctx* c, const double* x, long n, double* d_out_sq) {
   return 0;
 }
 
+int fos_sum_partials(fos_ctx* c, int np, double* d_out) {
+  fos_launch(c, k_sum_final, 1, 1024, (const double*)c->d_red, np, d_out);
+  FOS_LAUNCH_CHECK();
+  return 0;
+}
+
 int fos_jv_sigma(fos_ctx* c, double* d_scal, double ynorm, double eps) {
   fos_launch(c, k_sigma, 1, 1, d_scal, ynorm, eps);
   FOS_LAUNCH_CHECK();
