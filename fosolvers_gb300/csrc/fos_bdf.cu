@@ -71,16 +71,19 @@ __global__ void __launch_bounds__(kT) k_mdot(long n, const double* __restrict__ 
   block_reduce_store<NA>(acc, NA, part);
 }
 
-// w -= sum_l h[l] V_l ; then part <- V_l . w (MODE 0, CGS2 second pass), ||w||^2 (MODE 1),
-// or both (MODE 2: the DGKS test and, when it fails, the second pass's coefficients come
-// out of the same sweep over V)
+// w -= sum_l h[l] s2[l] V_l ; then part <- V_l . w (MODE 0, CGS2 second pass), ||w||^2
+// (MODE 1), or both (MODE 2: the DGKS test and, when it fails, the second pass's
+// coefficients come out of the same sweep over V).  s2 (null: all 1) are the squared
+// scales of unnormalised basis vectors (v_l = s_l V_l), so h = V^T w gives the coefficients
+// of the projection onto the v_l.
 template <int NV, int MODE>
 __global__ void __launch_bounds__(kT) k_update(long n, const double* __restrict__ V, long ldv,
                                                const double* __restrict__ h,
+                                               const double* __restrict__ s2,
                                                double* __restrict__ w,
                                                double* __restrict__ part) {
   __shared__ double hs[NV];
-  if (threadIdx.x < NV) hs[threadIdx.x] = h[threadIdx.x];
+  if (threadIdx.x < NV) hs[threadIdx.x] = s2 ? h[threadIdx.x] * s2[threadIdx.x] : h[threadIdx.x];
   __syncthreads();
   constexpr int NA = MODE == 0 ? NV : MODE == 1 ? 1 : NV + 1;
   double acc[NA];
@@ -308,10 +311,11 @@ struct Driver {
     return 0;
   }
   template <int MODE>
-  int update(int nv, const double* V, long ldv, const double* h, double* w) {
+  int update(int nv, const double* V, long ldv, const double* h, double* w,
+             const double* s2 = nullptr) {
     switch (nv) {
 #define FOS_UPD(K) \
-  case K: fos_launch(c, k_update<K, MODE>, kRedBlocks, kT, wk.N, V, ldv, h, w, wk.part); break;
+  case K: fos_launch(c, k_update<K, MODE>, kRedBlocks, kT, wk.N, V, ldv, h, s2, w, wk.part); break;
       FOS_UPD(1) FOS_UPD(2) FOS_UPD(3) FOS_UPD(4) FOS_UPD(5) FOS_UPD(6) FOS_UPD(7) FOS_UPD(8)
       FOS_UPD(9) FOS_UPD(10) FOS_UPD(11) FOS_UPD(12) FOS_UPD(13) FOS_UPD(14) FOS_UPD(15)
       FOS_UPD(16) FOS_UPD(17) FOS_UPD(18) FOS_UPD(19) FOS_UPD(20) FOS_UPD(21) FOS_UPD(22)
@@ -440,6 +444,17 @@ struct Driver {
     }
     int extra_cycles = 0;
     std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), yv(m), hbuf(4 * kMaxVec);
+    // The Arnoldi vectors are kept unnormalised: V_l holds W_l and v_l = sig[l] W_l with
+    // sig[l] = 1 / ||W_l|| (v_0 is normalised when it is formed).  The new vector of step j
+    // is J_G z'_j written straight into slot j+1, where z'_j = M(W_j) is the preconditioner
+    // applied to the stored W_j; the Arnoldi relation uses z_j = sig[j] z'_j (the FD Jv and
+    // ILU(0) are homogeneous, and flexible GMRES takes any z_j), so J_G z_j = sig[j] W_{j+1}
+    // before orthogonalisation.  Orthogonalising W_{j+1} against the W_l with coefficients
+    // sig[l]^2 (W_{j+1}, W_l) is the same projection; the Hessenberg column gets the factors
+    // sig[j] sig[l], and the solution is sum_l y_l sig[l] z'_l.  No pass over the basis
+    // normalises it.
+    std::vector<double> sig(m + 1, 1.0), sig2(m + 1, 1.0);
+    double* d_sig2 = wk.sc + 5 * kMaxVec;
     FOS_CUDA(cudaMemsetAsync(wk.d, 0, sizeof(double) * N, c->stream));
     *its = 0;
     if (bnorm == 0.0) return 0;
@@ -447,6 +462,9 @@ struct Driver {
     double beta = bnorm;
     for (int cyc = 0; cyc <= o.max_restarts + extra_cycles; cyc++) {
       fos_launch(c, k_scale, nb(N), kT, N, rvec, 1.0 / beta, wk.V);
+      sig[0] = sig2[0] = 1.0;
+      FOS_CUDA(cudaMemcpyAsync(d_sig2, sig2.data(), sizeof(double), cudaMemcpyHostToDevice,
+                               c->stream));
       bool fallback = false;
       std::fill(g.begin(), g.end(), 0.0);
       g[0] = beta;
@@ -455,10 +473,11 @@ struct Driver {
       for (int j = 0; j < m; j++) {
         double* vj = wk.V + (size_t)j * N;
         double* zj = wk.Z + (size_t)j * N;
+        double* wj = wk.V + (size_t)(j + 1) * N;  // the new vector, orthogonalised in place
         bool have_sq = false;
         int rc = psolve(y, vj, zj, c->d_scal, &have_sq);
         if (rc) return rc;
-        rc = jv(y, fy, zj, wk.w, gamma, ynorm, have_sq);
+        rc = jv(y, fy, zj, wj, gamma, ynorm, have_sq);
         if (rc) return rc;
         (*its)++;
         const int nv = j + 1;
@@ -468,37 +487,43 @@ struct Driver {
         // V^T w' (MODE 2) so the second pass needs no separate sweep over V for its
         // coefficients; otherwise it returns ||w'||^2 only (MODE 1).
         const bool fused = last_reorth;
-        if ((rc = mdot<true>(nv, wk.V, N, wk.w))) return rc;           // h, ||w||^2
+        if ((rc = mdot<true>(nv, wk.V, N, wj))) return rc;              // V^T w, ||w||^2
         if ((rc = reduce(nv + 1, wk.sc))) return rc;
         if (fused) {
-          if ((rc = update<2>(nv, wk.V, N, wk.sc, wk.w))) return rc;   // w -= V h; V^T w, ||w||^2
+          if ((rc = update<2>(nv, wk.V, N, wk.sc, wj, d_sig2))) return rc;  // w -= V s2 h; V^T w, ||w||^2
           if ((rc = reduce(nv + 1, wk.sc + kMaxVec))) return rc;
           if ((rc = fetch(wk.sc, hbuf.data(), 2 * kMaxVec))) return rc;
         } else {
-          if ((rc = update<1>(nv, wk.V, N, wk.sc, wk.w))) return rc;   // w -= V h, ||w||^2
+          if ((rc = update<1>(nv, wk.V, N, wk.sc, wj, d_sig2))) return rc;  // w -= V s2 h, ||w||^2
           if ((rc = reduce(1, wk.sc + kMaxVec + nv))) return rc;
           if ((rc = fetch(wk.sc, hbuf.data(), kMaxVec + nv + 1))) return rc;
         }
         double* col = &H[(size_t)(m + 1) * j];
-        for (int l = 0; l < nv; l++) col[l] = hbuf[l];
+        for (int l = 0; l < nv; l++) col[l] = sig[j] * sig[l] * hbuf[l];
         double hn2 = hbuf[kMaxVec + nv];
         last_reorth = hn2 < 0.5 * hbuf[nv];
         if (last_reorth) {
           const double* h2 = wk.sc + kMaxVec;  // V^T w' (device), from MODE 2 or a sweep
           if (!fused) {
-            if ((rc = mdot<false>(nv, wk.V, N, wk.w))) return rc;
+            if ((rc = mdot<false>(nv, wk.V, N, wj))) return rc;
             if ((rc = reduce(nv, wk.sc + kMaxVec))) return rc;
           }
-          if ((rc = update<1>(nv, wk.V, N, h2, wk.w))) return rc;
+          if ((rc = update<1>(nv, wk.V, N, h2, wj, d_sig2))) return rc;
           if ((rc = reduce(1, wk.sc + 3 * kMaxVec))) return rc;
           if ((rc = fetch(wk.sc + kMaxVec, hbuf.data() + kMaxVec, 2 * kMaxVec + 1))) return rc;
-          for (int l = 0; l < nv; l++) col[l] += hbuf[kMaxVec + l];
+          for (int l = 0; l < nv; l++) col[l] += sig[j] * sig[l] * hbuf[kMaxVec + l];
           hn2 = hbuf[3 * kMaxVec];
           reorth++;
         }
-        const double hn = std::sqrt(hn2);
+        const double wn = std::sqrt(hn2);  // ||W_{j+1}||
+        const double hn = sig[j] * wn;
         col[j + 1] = hn;
-        if (hn > 0.0) fos_launch(c, k_scale, nb(N), kT, N, wk.w, 1.0 / hn, wk.V + (size_t)(j + 1) * N);
+        if (wn > 0.0) {
+          sig[j + 1] = 1.0 / wn;
+          sig2[j + 1] = sig[j + 1] * sig[j + 1];
+          FOS_CUDA(cudaMemcpyAsync(d_sig2 + j + 1, sig2.data() + j + 1, sizeof(double),
+                                   cudaMemcpyHostToDevice, c->stream));
+        }
         for (int l = 0; l < j; l++) {
           const double t0 = cs[l] * col[l] + sn[l] * col[l + 1];
           col[l + 1] = -sn[l] * col[l] + cs[l] * col[l + 1];
@@ -531,6 +556,7 @@ struct Driver {
         for (int q = l + 1; q < kend; q++) s -= H[l + (size_t)(m + 1) * q] * yv[q];
         yv[l] = s / H[l + (size_t)(m + 1) * l];
       }
+      for (int l = 0; l < kend; l++) yv[l] *= sig[l];  // z_l = sig[l] z'_l
       FOS_CUDA(cudaMemcpyAsync(wk.sc + 4 * kMaxVec, yv.data(), sizeof(double) * kend,
                                cudaMemcpyHostToDevice, c->stream));
       fos_launch(c, k_comb, nb(N), kT, N, kend, (const double*)wk.Z, N,
