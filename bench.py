@@ -76,6 +76,10 @@ def parse():
     ap.add_argument("--no-ops", action="store_true", help="skip the per-operation timing")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--op-reps", type=int, default=5)
+    ap.add_argument("--msbp", type=int, default=1,
+                    help="preconditioner set-up policy of every arm: 1 = pset each BDF step; "
+                         "m > 1 = CVODE's (at most m steps between set-ups, or on a 30%% gamma "
+                         "change or a Newton failure)")
     ap.add_argument("--ilut", action="store_true",
                     help="the ILUT preconditioner arm (FP64 flux, ILUT(lfil, droptol) on P in the "
                          "RCM order) against block ILU(0) on the same mesh, with the oracle's "
@@ -151,7 +155,8 @@ def run_ilut(args):
             ctx.set_ilut(args.lfil, args.droptol)
         y0 = torch.empty_like(y0_ref)
         ctx.to_internal(y0_ref, y0)
-        mk = lambda n: ctx.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=n, precond=1)
+        mk = lambda n: ctx.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=n, precond=1,
+                                        msbp=args.msbp)
         ms, st, launches, _, _ = timed_bdf(ctx, y0, mk, args, dev, stream, None)
         rec = {"steps_per_s": args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
                "n_newton": st["n_newton"], "n_lin_iters": st["n_lin_iters"],
@@ -454,7 +459,8 @@ def main():
         ctx.attach_gnn(gnn)
 
     def mk_for(pc):
-        return lambda n, **kw: ctx.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=n, precond=pc, **kw)
+        return lambda n, **kw: ctx.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=n, precond=pc,
+                                                msbp=args.msbp, **kw)
 
     mk = mk_for(precond)
     setup_s = time.perf_counter() - t_setup
@@ -471,6 +477,16 @@ def main():
         alt[f"{args.mode}_ilu"] = {"value": world * args.steps / (allmax(pg, ms_i, dev) / 1e3),
                                    "ms_per_step": ms_i / args.steps,
                                    "n_lin_iters": st_i["n_lin_iters"]}
+    # the headline arm under CVODE's preconditioner set-up policy (MSBP = 20): psets at the
+    # first step, on the BDF1 -> BDF2 gamma change and every 20 steps, instead of every step
+    cvode = None
+    if args.msbp == 1 and not args.no_compare:
+        mk_c = lambda n, **kw: ctx.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=n,
+                                                precond=precond, msbp=20, **kw)
+        ms_c, st_c, _, _, _ = timed_bdf(ctx, y0, mk_c, args, dev, stream, pg)
+        cvode = {"msbp": 20, "value": world * args.steps / (allmax(pg, ms_c, dev) / 1e3),
+                 "ms_per_step": ms_c / args.steps, "n_pset": st_c["n_pset"],
+                 "n_lin_iters": st_c["n_lin_iters"]}
 
     # end to end: host buffer in the caller's cell order, copied in and out every step
     e2e = None
@@ -550,7 +566,8 @@ def main():
         ctx64 = make_ctx(grid, ibc, wl, "fp64", args.ilu_order, stream)
         y064 = torch.empty_like(y0_ref)
         ctx64.to_internal(y0_ref, y064)
-        mk64 = lambda n, **kw: ctx64.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=n, precond=1, **kw)
+        mk64 = lambda n, **kw: ctx64.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=n, precond=1,
+                                                  msbp=args.msbp, **kw)
         ms64, st64, _, _, y64 = timed_bdf(ctx64, y064, mk64, args, dev, stream, pg)
         v64 = world * args.steps / (allmax(pg, ms64, dev) / 1000.0)
         yb = torch.empty_like(y)
@@ -561,6 +578,13 @@ def main():
                 # error reflects that tolerance at 26.5M unknowns, the l2 error the precision
                 "state_rel_err_vs_fp64": field_rel_err(y_out, yb, nC),
                 "state_rel_l2_vs_fp64": float((y_out - yb).norm() / yb.norm())}
+        if cvode is not None:
+            mk64c = lambda n, **kw: ctx64.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=n,
+                                                       precond=1, msbp=20, **kw)
+            ms64c, st64c, _, _, _ = timed_bdf(ctx64, y064, mk64c, args, dev, stream, pg)
+            cvode["fp64_value"] = world * args.steps / (allmax(pg, ms64c, dev) / 1e3)
+            cvode["fp64_n_pset"] = st64c["n_pset"]
+            cvode["ratio"] = cvode["value"] / cvode["fp64_value"]
         ctx64.close()
 
     peaks = {}
@@ -616,6 +640,7 @@ def main():
             "config": {"workload": workload_desc(args.workload) if args.scale is None else
                        f"{args.workload} at scale {args.scale}",
                        "cells": nC, "faces": nF, "mode": args.mode, "precond": args.precond,
+                       "pset": "every BDF step" if args.msbp == 1 else f"CVODE policy, MSBP {args.msbp}",
                        "ilu_order": args.ilu_order, "ilu_levels": [info["nlev_fwd"], info["nlev_bwd"]],
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
                        "l2": "inputs larger than L2 (state 0.2 GB, ILU factors ~3-5 GB); no flush",
@@ -623,6 +648,7 @@ def main():
             "clocks": clk, "e2e": e2e, "gpu_launches": launches,
             "roofline": roof, "throughput": thr, "cpu_baseline": cpu,
             "vs_fp64_ilu": vs64, "same_precision_ilu": alt or None,
+            "cvode_setup_policy": cvode,
             "stats": {k: st[k] for k in ("n_rhs", "n_jv", "n_psol", "n_pset", "n_newton",
                                           "n_lin_iters", "n_steps", "n_fallback", "n_learned")},
         }

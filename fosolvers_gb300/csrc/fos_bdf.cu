@@ -263,6 +263,7 @@ extern "C" void fos_bdf_defaults(fos_bdf_opts* o) {
   o->jv_eps = 0.0;  // 0 = sqrt(machine epsilon of the flux precision)
   o->precond = 1;
   o->jac_reuse = 0;
+  o->msbp = 1;
   o->resume = 0;
 }
 
@@ -279,6 +280,8 @@ struct Driver {
   int pc = 0;
   // learned mode: ILU(0) factorisation is made on demand (fallback) once per BDF step
   bool pset_done = false;
+  bool keep_setup = false;  // the step reuses the last factorisation (msbp > 1)
+  bool setup_made = false;  // a pset ran during the current step
   double t_step = 0.0, gamma_step = 0.0;
   const double* y_step = nullptr;
   int ilu_ref_its = -1;  // Krylov iterations of the last ILU(0)-preconditioned solve
@@ -361,6 +364,7 @@ struct Driver {
     if (rc) return rc;
     st.n_pset++;
     pset_done = true;
+    setup_made = true;
     return c->ilu_ierr ? 3 : 0;
   }
   // w = J_G v at state y with f(y) = fy
@@ -405,7 +409,7 @@ struct Driver {
       if (gn <= gtol) return 0;
       if (k == o.max_newton) break;
       if (k == 0) {
-        pset_done = false;
+        pset_done = keep_setup;
         t_step = tn;
         gamma_step = gamma;
         y_step = y;
@@ -626,13 +630,30 @@ extern "C" int fos_bdf_run(fos_ctx* c, double t0, double* y, const fos_bdf_opts*
   FOS_CUDA(cudaMemcpyAsync(wk.yn, y, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
   if (!resume) wk.has_hist = false;
   int status = 0;
+  // preconditioner set-up policy (opts->msbp > 1: CVODE's cvLsSetup conditions)
+  int last_setup = -1;
+  double gamma_setup = 0.0;
   for (int s = 0; s < opts->nsteps && !status; s++) {
     const int q = (opts->order == 2 && (s >= 1 || resume)) ? 2 : 1;
     const double gamma = q == 1 ? opts->dt : 2.0 * opts->dt / 3.0;
     const double tn = t + opts->dt;
     fos_launch(c, k_hist, nb(N), kT, N, q, wk.yn, wk.ym, wk.hist);
     FOS_CUDA(cudaMemcpyAsync(y, wk.yn, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
-    const int nrc = dr.newton(y, gamma, wk.hist, tn);  // from y_0 = y_n
+    const bool reuse = opts->msbp > 1 && last_setup >= 0 && c->has_factor &&
+                       s - last_setup < opts->msbp &&
+                       std::fabs(gamma / gamma_setup - 1.0) <= 0.3;
+    dr.keep_setup = reuse;
+    dr.setup_made = false;
+    int nrc = dr.newton(y, gamma, wk.hist, tn);  // from y_0 = y_n
+    if (nrc == 1 && reuse) {  // failed on a reused set-up: retry the step with a fresh one
+      FOS_CUDA(cudaMemcpyAsync(y, wk.yn, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+      dr.keep_setup = false;
+      nrc = dr.newton(y, gamma, wk.hist, tn);
+    }
+    if (dr.setup_made) {
+      last_setup = s;
+      gamma_setup = gamma;
+    }
     if (nrc < 0) return nrc;
     const bool conv = nrc == 0;
     if (nrc >= 2) status = nrc;

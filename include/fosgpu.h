@@ -228,6 +228,12 @@ typedef struct {
                          of 2; 5 = the same without fallback */
   int jac_reuse;      /* 0 = assemble J every BDF step (jok = 0), 1 = keep J from the first step */
   int resume;         /* 1 = continue the BDF history of the previous call (y must be its result) */
+  int msbp;           /* preconditioner set-up policy: 1 = pset at every BDF step (default);
+                         m > 1 = CVODE's (cvLsSetup: MSBP = 20, DGMAX = 0.3): pset at the
+                         first step of the call, when m steps have passed since the last one
+                         or gamma changed by more than 30% since it, and when a step's Newton
+                         iteration fails on a reused set-up (the step is retried with a fresh
+                         one); otherwise psol uses the last factorisation */
 } fos_bdf_opts;
 
 typedef struct {

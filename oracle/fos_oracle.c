@@ -1371,7 +1371,7 @@ void o_bdf_defaults(o_bdf_opts* o) {
   o->order = 1; o->dt = 1e-3; o->nsteps = 1;
   o->newton_rtol = 1e-8; o->newton_atol = 1e-12; o->max_newton = 10;
   o->maxl = 30; o->max_restarts = 4; o->lin_rtol = 1e-3;
-  o->jv_eps = 1.4901161193847656e-08; o->use_prec = 1;
+  o->jv_eps = 1.4901161193847656e-08; o->use_prec = 1; o->msbp = 1;
 }
 
 
@@ -1381,8 +1381,10 @@ void o_bdf_defaults(o_bdf_opts* o) {
  * converged, 2 non-finite residual or rhs failure, 3 pset failure, 4 GMRES failure. */
 static int o_newton(int n, o_rhs_fn rhs, o_pset_fn pset, o_psol_fn psol, void* ud, double tn,
                     double* y, double gamma, const double* hist, const o_bdf_opts* opts,
-                    o_bdf_stats* st, double* f, double* G, double* d, double* ytmp, double* ftmp) {
+                    o_bdf_stats* st, double* f, double* G, double* d, double* ytmp, double* ftmp,
+                    int reuse, int* setup_made) {
   double gtol = 0.0;
+  if (setup_made) *setup_made = 0;
   for (int k = 0; k <= opts->max_newton; k++) {
     int rc = rhs(tn, y, f, ud);
     st->n_rhs++;
@@ -1394,10 +1396,11 @@ static int o_newton(int n, o_rhs_fn rhs, o_pset_fn pset, o_psol_fn psol, void* u
     st->last_gnorm = gn / gtol;
     if (gn <= gtol) return 0;
     if (k == opts->max_newton) break;
-    if (k == 0 && opts->use_prec) {
+    if (k == 0 && opts->use_prec && !reuse) {
       int jcur = 0;
       rc = pset(tn, y, f, 0, &jcur, gamma, ud);
       st->n_pset++;
+      if (setup_made) *setup_made = 1;
       if (rc) return 3;
     }
     nk_op op = {n, rhs, psol, ud, tn, gamma, 1.0, -gamma, sqrt(vdot(n, y, y)), opts->jv_eps,
@@ -1424,6 +1427,8 @@ int o_bdf_run(int n, o_rhs_fn rhs, o_pset_fn pset, o_psol_fn psol, void* ud, dou
   double *ytmp = (double*)xcalloc(n, sizeof(double)), *ftmp = (double*)xcalloc(n, sizeof(double));
   double t = t0;
   int status = 0;
+  int last_setup = -1; /* set-up policy (msbp > 1) */
+  double gamma_setup = 0.0;
   memcpy(yn, y, sizeof(double) * n);
   for (int s = 0; s < opts->nsteps; s++) {
     int q = (opts->order == 2 && s >= 1) ? 2 : 1;
@@ -1437,7 +1442,20 @@ int o_bdf_run(int n, o_rhs_fn rhs, o_pset_fn pset, o_psol_fn psol, void* ud, dou
     }
     double tn = t + opts->dt;
     memcpy(y, yn, sizeof(double) * n); /* predictor: previous state */
-    int nrc = o_newton(n, rhs, pset, psol, ud, tn, y, gamma, hist, opts, st, f, G, d, ytmp, ftmp);
+    const int reuse = opts->msbp > 1 && last_setup >= 0 && s - last_setup < opts->msbp &&
+                      fabs(gamma / gamma_setup - 1.0) <= 0.3;
+    int made = 0;
+    int nrc = o_newton(n, rhs, pset, psol, ud, tn, y, gamma, hist, opts, st, f, G, d, ytmp, ftmp,
+                       reuse, &made);
+    if (nrc == 1 && reuse) { /* failed on a reused set-up: retry the step with a fresh one */
+      memcpy(y, yn, sizeof(double) * n);
+      nrc = o_newton(n, rhs, pset, psol, ud, tn, y, gamma, hist, opts, st, f, G, d, ytmp, ftmp,
+                     0, &made);
+    }
+    if (made) {
+      last_setup = s;
+      gamma_setup = gamma;
+    }
     if (nrc) {
       st->fails++;
       status = nrc == 1 ? 1 : nrc;
@@ -1556,7 +1574,8 @@ int o_bdf_adaptive(int n, o_rhs_fn rhs, o_pset_fn pset, o_psol_fn psol, void* ud
     const double gamma = 1.0 / dl[0];
     for (int j = 1; j <= q; j++) cf[j - 1] = -gamma * dl[j];
     o_comb(n, hist, q, Y, cf);
-    int nrc = o_newton(n, rhs, pset, psol, ud, tn, y, gamma, hist, nk, st, f, G, d, ytmp, ftmp);
+    int nrc = o_newton(n, rhs, pset, psol, ud, tn, y, gamma, hist, nk, st, f, G, d, ytmp, ftmp,
+                       0, NULL);
     if (nrc) {
       as->n_newton_fails++;
       if (++ncf > 10 || 0.25 * h < ad->hmin) { status = 4; break; }

@@ -128,6 +128,9 @@ typedef struct {
   double lin_rtol;    /* GMRES: ||r|| <= lin_rtol*||b|| */
   double jv_eps;      /* sqrt(eps) for the finite-difference Jv increment */
   int use_prec;       /* 0 = identity psol */
+  int msbp;           /* 1 = pset every step; m > 1 = CVODE's set-up policy (cvLsSetup:
+                         at most m steps between set-ups, or a > 30% gamma change, or a
+                         Newton failure on a reused set-up, after which the step is retried) */
 } o_bdf_opts;
 typedef struct {
   long n_rhs, n_jv, n_psol, n_pset, n_newton, n_lin_iters, n_steps, fails;

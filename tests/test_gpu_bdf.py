@@ -144,3 +144,20 @@ def test_learned_preconditioner_refuses_hex_grid(cuda):
     c = Case(hex_workload(6))
     with pytest.raises(RuntimeError, match="tetrahedral grids only"):
         c.gpu.attach_gnn(GNN(seed=0))
+
+
+@pytest.mark.parametrize("msbp", [5, 20])
+def test_cvode_setup_policy_matches_oracle(cuda, msbp):
+    """CVODE's preconditioner set-up policy (msbp > 1: at most msbp steps between psets, a
+    fresh one on a > 30% gamma change or a Newton failure on a reused one) in both drivers:
+    BDF2 on the sine workload at 8^3 x 6 for 12 steps, the same pset, Newton and Krylov
+    counts, state within 1e-10."""
+    wl = M.make_workload("sine96", scale=8, seed=1)
+    c = Case(wl)
+    y_ref, st_ref = oracle_run(c, nsteps=12, msbp=msbp)
+    y, st = gpu_run(c, nsteps=12, msbp=msbp)
+    print("msbp", msbp, st, st_ref)
+    for k in ("n_pset", "n_newton", "n_lin_iters", "n_steps"):
+        assert st[k] == st_ref[k], k
+    assert st["n_pset"] < 12
+    assert rel_err(y, y_ref) <= 1e-10
