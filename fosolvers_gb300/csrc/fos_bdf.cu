@@ -824,6 +824,9 @@ extern "C" int fos_bdf_adaptive(fos_ctx* c, double t0, double tout, double* y,
   bool have_eprev = false;
   long attempts = 0;
   int status = 0;
+  // preconditioner set-up policy (nk->msbp > 1: CVODE's; steps counted as accepted steps)
+  long last_setup = -1;
+  double gamma_setup = 0.0;
   while (t < tout) {
     if (++attempts > max_steps) { status = 5; break; }
     if (t + h >= tout) h = tout - t;
@@ -853,7 +856,22 @@ extern "C" int fos_bdf_adaptive(fos_ctx* c, double t0, double tout, double* y,
       for (int j = 1; j <= q; j++) cf[j - 1] = -gamma * dl[j];
       if (int rc = A.comb(wk.hist, q, Y, cf)) return rc;
     }
-    const int nrc = dr.newton(y, gamma, wk.hist, tn);
+    const bool reuse = nk->msbp > 1 && last_setup >= 0 && c->has_factor &&
+                       as.n_accepted - last_setup < nk->msbp &&
+                       std::fabs(gamma / gamma_setup - 1.0) <= 0.3;
+    dr.keep_setup = reuse;
+    dr.setup_made = false;
+    int nrc = dr.newton(y, gamma, wk.hist, tn);
+    if (nrc > 0 && reuse) {  // failed on a reused set-up: the same step with a fresh one
+      FOS_CUDA(cudaMemcpyAsync(y, wk.ypred, sizeof(double) * N, cudaMemcpyDeviceToDevice,
+                               c->stream));
+      dr.keep_setup = false;
+      nrc = dr.newton(y, gamma, wk.hist, tn);
+    }
+    if (dr.setup_made) {
+      last_setup = as.n_accepted;
+      gamma_setup = gamma;
+    }
     if (nrc < 0) return nrc;
     if (nrc != 0) {  // Newton failure (no convergence, non-finite residual, zero pivot)
       as.n_newton_fails++;

@@ -1552,6 +1552,8 @@ int o_bdf_adaptive(int n, o_rhs_fn rhs, o_pset_fn pset, o_psol_fn psol, void* ud
   if (ad->hmax > 0.0 && h > ad->hmax) h = ad->hmax;
   int q = 1, nq = 0, nef = 0, ncf = 0, have_eprev = 0;
   long attempts = 0;
+  long last_setup = -1; /* set-up policy (nk->msbp > 1), steps counted as accepted steps */
+  double gamma_setup = 0.0;
   while (!status && t < tout) {
     if (++attempts > max_steps) { status = 5; break; }
     if (t + h >= tout) h = tout - t;
@@ -1574,8 +1576,20 @@ int o_bdf_adaptive(int n, o_rhs_fn rhs, o_pset_fn pset, o_psol_fn psol, void* ud
     const double gamma = 1.0 / dl[0];
     for (int j = 1; j <= q; j++) cf[j - 1] = -gamma * dl[j];
     o_comb(n, hist, q, Y, cf);
+    const int reuse = nk->msbp > 1 && last_setup >= 0 && as->n_accepted - last_setup < nk->msbp &&
+                      fabs(gamma / gamma_setup - 1.0) <= 0.3;
+    int made = 0;
     int nrc = o_newton(n, rhs, pset, psol, ud, tn, y, gamma, hist, nk, st, f, G, d, ytmp, ftmp,
-                       0, NULL);
+                       reuse, &made);
+    if (nrc && reuse) { /* failed on a reused set-up: the same step with a fresh one */
+      memcpy(y, ypred, sizeof(double) * n);
+      nrc = o_newton(n, rhs, pset, psol, ud, tn, y, gamma, hist, nk, st, f, G, d, ytmp, ftmp, 0,
+                     &made);
+    }
+    if (made) {
+      last_setup = as->n_accepted;
+      gamma_setup = gamma;
+    }
     if (nrc) {
       as->n_newton_fails++;
       if (++ncf > 10 || 0.25 * h < ad->hmin) { status = 4; break; }

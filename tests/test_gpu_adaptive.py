@@ -56,3 +56,31 @@ def test_adaptive_fp32_form(cuda):
     assert a32["t"] == T1
     assert abs(a32["n_accepted"] - a64["n_accepted"]) <= 0.2 * a64["n_accepted"]
     assert rel_err(y32, y64) <= 1e-5
+
+
+def test_adaptive_cvode_setup_policy_matches_oracle(cuda):
+    """The adaptive drivers with CVODE's preconditioner set-up policy (MSBP 20, DGMAX 0.3):
+    the same accepted / rejected history and pset count as the oracle's, fewer psets than
+    accepted steps, state within 1e-9."""
+    import torch
+    c = Case(M.make_workload("sod16", scale=8))
+    c.match_ilu_order()
+    rhs, pset, psol = c.oracle.callbacks()
+    y_ref = c.y0.copy()
+    rc, st_ref, ast_ref = O.bdf_adaptive(c.N, rhs, pset, psol, c.oracle.h, y_ref, 0.0, T1,
+                                         O.bdf_defaults(newton_rtol=1e-10, msbp=20),
+                                         O.adapt_defaults(rtol=1e-6, atol=1e-10, h0=1e-4))
+    assert rc == 0
+    yr = torch.from_numpy(c.y0).cuda()
+    y = torch.empty_like(yr)
+    c.gpu.to_internal(yr, y)
+    rc, st, ast = c.gpu.bdf_adaptive(y, 0.0, T1, c.gpu.bdf_defaults(newton_rtol=1e-10, msbp=20),
+                                     c.gpu.adapt_defaults(rtol=1e-6, atol=1e-10, h0=1e-4))
+    assert rc == 0, (st, ast)
+    c.gpu.to_reference(y, yr)
+    torch.cuda.synchronize()
+    print("gpu", st, ast, "\noracle", st_ref, ast_ref)
+    for k in ("n_accepted", "n_err_fails", "n_newton_fails", "q_last", "steps_at_order"):
+        assert ast[k] == ast_ref[k], k
+    assert st["n_pset"] == st_ref["n_pset"] < ast["n_accepted"]
+    assert rel_err(yr.cpu().numpy(), y_ref) <= 1e-9
