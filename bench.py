@@ -80,6 +80,8 @@ def parse():
                     help="preconditioner set-up policy of every arm: 1 = pset each BDF step; "
                          "m > 1 = CVODE's (at most m steps between set-ups, or on a 30%% gamma "
                          "change or a Newton failure)")
+    ap.add_argument("--no-cvode", action="store_true",
+                    help="skip the arms under CVODE's set-up policy (cvode_setup_policy)")
     ap.add_argument("--ilut", action="store_true",
                     help="the ILUT preconditioner arm (FP64 flux, ILUT(lfil, droptol) on P in the "
                          "RCM order) against block ILU(0) on the same mesh, with the oracle's "
@@ -480,7 +482,7 @@ def main():
     # the headline arm under CVODE's preconditioner set-up policy (MSBP = 20): psets at the
     # first step, on the BDF1 -> BDF2 gamma change and every 20 steps, instead of every step
     cvode = None
-    if args.msbp == 1 and not args.no_compare:
+    if args.msbp == 1 and not args.no_compare and not args.no_cvode:
         mk_c = lambda n, **kw: ctx.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=n,
                                                 precond=precond, msbp=20, **kw)
         ms_c, st_c, _, _, _ = timed_bdf(ctx, y0, mk_c, args, dev, stream, pg)
