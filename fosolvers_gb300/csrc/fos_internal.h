@@ -94,6 +94,9 @@ struct fos_ctx {
   float* d_LU32 = nullptr;    // [25*nnzb] factors (FP32)
   int ilu_nlev_f = 0, ilu_nlev_b = 0;
   std::vector<int> lev_f, lev_b;    // level pointers (colour starts when colouring)
+  std::vector<char> lev_f_hasL;     // forward level l has L blocks (else y = r there: no launch)
+  bool ilu_fuse_top = false;        // the last forward level is the first backward one and
+                                    // has no U blocks: one launch forms z = inv(D) y there
   int* d_lrows_f = nullptr;         // level-ordered positions (null when levels are ranges)
   int* d_lrows_b = nullptr;
   int* d_upd_ptr = nullptr;   // [nC+1] per position

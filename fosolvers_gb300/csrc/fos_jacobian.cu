@@ -508,15 +508,28 @@ __global__ void __launch_bounds__(kT) k_ilu_factor(
   }
 }
 
-// r (FP64 SoA, internal order) -> rv (AoS, 8 per row, position order)
+// r (FP64 SoA, internal order) -> rv (AoS, 8 per row, position order).  The whole row is
+// stored, padding included, in 16-byte stores: full 32-byte sectors, which the L2 writes
+// back without first reading the rest of a partly written sector from DRAM.
 template <typename TF>
 __global__ void k_ilu_in(int nC, const int* __restrict__ ipos, const double* __restrict__ r,
                          TF* __restrict__ rv) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nC) return;
-  TF* dst = rv + 8 * (size_t)ipos[i];
+  TF v[8];
 #pragma unroll
-  for (int a = 0; a < 5; a++) dst[a] = from64<TF>(r[(size_t)a * nC + i]);
+  for (int a = 0; a < 5; a++) v[a] = from64<TF>(r[(size_t)a * nC + i]);
+  v[5] = v[6] = v[7] = TF(0);
+  TF* dst = rv + 8 * (size_t)ipos[i];
+  if constexpr (sizeof(TF) == 4) {
+    float4* d = reinterpret_cast<float4*>(dst);
+    d[0] = make_float4(v[0], v[1], v[2], v[3]);
+    d[1] = make_float4(v[4], v[5], v[6], v[7]);
+  } else {
+    double2* d = reinterpret_cast<double2*>(dst);
+#pragma unroll
+    for (int k = 0; k < 4; k++) d[k] = make_double2(v[2 * k], v[2 * k + 1]);
+  }
 }
 // zv (AoS, position order) -> z (FP64 SoA, internal order)
 template <typename TF>
@@ -564,25 +577,52 @@ __global__ void __launch_bounds__(kRedThreads) k_ilu_out_sq(int nC, const int* _
 // (a row reads only its own rv and earlier rows' y).
 //   forward:  y_p = r_p - sum_{q in lower(p)} L_pq y_q           (unit block diagonal)
 //   backward: z_p = inv(D_p) (y_p - sum_{q in upper(p)} U_pq z_q)
+// z_p = inv(D_p) comp, comp = the row's five components gathered from its lanes; stored with
+// the row's padding so that the 32-byte sectors are written whole
 template <typename TF>
+__device__ __forceinline__ void ilu_diag_store(int lane, int a, bool active, int p, TF acc,
+                                               const TF* __restrict__ Dr, TF* __restrict__ zv) {
+  TF comp[5];
+  const int base = lane - a;
+#pragma unroll
+  for (int b = 0; b < 5; b++) comp[b] = __shfl_sync(0xffffffffu, acc, base + b < 32 ? base + b : 0);
+  if (!active) return;
+  TF zz = 0;
+#pragma unroll
+  for (int b = 0; b < 5; b++) zz += __ldg(Dr + b) * comp[b];
+  zv[8 * (size_t)p + a] = zz;
+  if (a < 3) zv[8 * (size_t)p + 5 + a] = TF(0);
+}
+
+// kDiag: the level has no U blocks and is also the backward sweep's first level, so the
+// launch finishes those rows (z_p = inv(D_p) y_p) instead of storing y_p
+template <typename TF, bool kDiag>
 __global__ void __launch_bounds__(kT) k_ilu_fwd(int n, const int* __restrict__ rows, int p0,
                                                 const int* __restrict__ prow,
                                                 const int* __restrict__ pcol,
                                                 const int* __restrict__ pdiag,
-                                                const TF* __restrict__ LU, TF* __restrict__ yv) {
+                                                const TF* __restrict__ LU, TF* __restrict__ yv,
+                                                TF* __restrict__ zv) {
   const int lane = threadIdx.x & 31;
   const int sub = lane / 5, a = lane - 5 * sub;
   const int t = (blockIdx.x * blockDim.x + threadIdx.x) / 32 * 6 + sub;
-  if (sub >= 6 || t >= n) return;
-  const int p = rows ? rows[t] : p0 + t;
-  TF acc = yv[8 * (size_t)p + a];
-  for (int s = prow[p]; s < pdiag[p]; s++) {
-    const TF* yq = yv + 8 * (size_t)pcol[s];
-    const TF* B = LU + 25 * (size_t)s + 5 * a;
+  const bool active = sub < 6 && t < n;
+  if (!kDiag && !active) return;
+  const int p = active ? (rows ? rows[t] : p0 + t) : 0;
+  TF acc = TF(0);
+  if (active) {
+    acc = yv[8 * (size_t)p + a];
+    for (int s = prow[p]; s < pdiag[p]; s++) {
+      const TF* yq = yv + 8 * (size_t)pcol[s];
+      const TF* B = LU + 25 * (size_t)s + 5 * a;
 #pragma unroll
-    for (int b = 0; b < 5; b++) acc -= __ldg(B + b) * yq[b];
+      for (int b = 0; b < 5; b++) acc -= __ldg(B + b) * yq[b];
+    }
   }
-  yv[8 * (size_t)p + a] = acc;
+  if constexpr (kDiag)
+    ilu_diag_store(lane, a, active, p, acc, LU + 25 * (size_t)(active ? pdiag[p] : 0) + 5 * a, zv);
+  else
+    yv[8 * (size_t)p + a] = acc;
 }
 
 template <typename TF>
@@ -607,16 +647,7 @@ __global__ void __launch_bounds__(kT) k_ilu_bwd(int n, const int* __restrict__ r
       for (int b = 0; b < 5; b++) acc -= __ldg(B + b) * zq[b];
     }
   }
-  TF comp[5];
-  const int base = lane - a;
-#pragma unroll
-  for (int b = 0; b < 5; b++) comp[b] = __shfl_sync(0xffffffffu, acc, base + b < 32 ? base + b : 0);
-  if (!active) return;
-  const TF* Dr = LU + 25 * (size_t)pdiag[p] + 5 * a;
-  TF zz = 0;
-#pragma unroll
-  for (int b = 0; b < 5; b++) zz += __ldg(Dr + b) * comp[b];
-  zv[8 * (size_t)p + a] = zz;
+  ilu_diag_store(lane, a, active, p, acc, LU + 25 * (size_t)(active ? pdiag[p] : 0) + 5 * a, zv);
 }
 
 }  // namespace
@@ -747,6 +778,21 @@ int fos_jac_setup(fos_ctx* c) {
     c->ilu_nlev_f = nlf;
     c->ilu_nlev_b = nlb;
   }
+  c->lev_f_hasL.assign(c->ilu_nlev_f, 0);
+  for (int l = 0; l < c->ilu_nlev_f; l++)
+    for (int k = c->lev_f[l]; k < c->lev_f[l + 1] && !c->lev_f_hasL[l]; k++) {
+      const int p = rows_f.empty() ? k : rows_f[k];
+      c->lev_f_hasL[l] = pdiag[p] > prow[p];
+    }
+  // colours: the forward sweep ends with the top colour and the backward one starts there;
+  // a proper colouring leaves its rows without U blocks (checked)
+  c->ilu_fuse_top = false;
+  if (c->ilu_colors) {
+    const int top = c->ilu_colors - 1;
+    bool noU = true;
+    for (int p = c->lev_f[top]; p < c->lev_f[top + 1] && noU; p++) noU = prow[p + 1] == pdiag[p] + 1;
+    c->ilu_fuse_top = noU;
+  }
   // factor update lists (IKJ): for q in lower(p) by position: scale L_pq, then
   // P_pj -= L_pq U_qj for every j in upper(q) that is also in row p
   std::vector<int> upd_ptr(nC + 1, 0);
@@ -865,13 +911,18 @@ static int ilu_apply_t(fos_ctx* c, const TF* LU, const double* r, double* z,
   TF* yv = reinterpret_cast<TF*>(c->d_ilu_tmp);
   TF* zv = yv + 8 * (size_t)c->nC;
   fos_launch(c, k_ilu_in<TF>, nb(c->nC, 256), 256, c->nC, (const int*)c->d_ipos, r, yv);
-  for (int l = 0; l < c->ilu_nlev_f; l++) {
+  const int nf = c->ilu_nlev_f;
+  for (int l = 0; l < nf; l++) {
     const int n = c->lev_f[l + 1] - c->lev_f[l];
     const int* rows = c->d_lrows_f ? c->d_lrows_f + c->lev_f[l] : nullptr;
-    fos_launch(c, k_ilu_fwd<TF>, nb_rows5(n), kT, n, rows, c->lev_f[l], (const int*)c->d_prow,
-               (const int*)c->d_pcol, (const int*)c->d_pdiag, LU, yv);
+    if (c->ilu_fuse_top && l == nf - 1)
+      fos_launch(c, k_ilu_fwd<TF, true>, nb_rows5(n), kT, n, rows, c->lev_f[l],
+                 (const int*)c->d_prow, (const int*)c->d_pcol, (const int*)c->d_pdiag, LU, yv, zv);
+    else if (c->lev_f_hasL[l])  // a level without L blocks keeps y = r
+      fos_launch(c, k_ilu_fwd<TF, false>, nb_rows5(n), kT, n, rows, c->lev_f[l],
+                 (const int*)c->d_prow, (const int*)c->d_pcol, (const int*)c->d_pdiag, LU, yv, zv);
   }
-  for (int l = 0; l < c->ilu_nlev_b; l++) {
+  for (int l = c->ilu_fuse_top ? 1 : 0; l < c->ilu_nlev_b; l++) {
     // colours run backwards for the upper sweep
     const int lc = c->ilu_colors ? c->ilu_nlev_b - 1 - l : l;
     const int n = c->lev_b[lc + 1] - c->lev_b[lc];

@@ -112,9 +112,12 @@ def test_pset_jok_reuses_jacobian(case):
     assert rel_err(z, z_ref) <= 1e-10
 
 
-@pytest.mark.parametrize("name", ["sine8", "hex8"])
-def test_fp32_ilu_apply(cuda, name):
-    c = Case(_workload(name), flags=ILU_FP32)
+@pytest.mark.parametrize("name,extra", [("sine8", 0), ("hex8", 0), ("sine8", ILU_COLOR),
+                                        ("hex8", ILU_COLOR)])
+def test_fp32_ilu_apply(cuda, name, extra):
+    """FP32 factors and sweeps in the level-scheduled and the colour order (where the last
+    forward colour also applies inv(D) and the colour without L blocks takes no launch)."""
+    c = Case(_workload(name), flags=ILU_FP32 | extra)
     y = perturbed(c.y0, c.nC, 4)
     c.match_ilu_order()
     c.oracle.pset(0.0, y, None, 0, 5e-3)
