@@ -90,8 +90,14 @@ struct fos_ctx {
   void* d_Jb = nullptr;       // [25*nFb] boundary-face diagonal terms (same type)
   int* d_ierr = nullptr;
   bool has_jac = false;
-  double* d_LU = nullptr;     // [25*nnzb] factors (FP64), diag blocks hold the inverse
+  // factors in two regions, so that each sweep streams one: the L blocks of every row (by
+  // position), then the diagonal block and the U blocks of every row; diag blocks hold the
+  // inverse.  Block storage of slot s in row p: plst[p] + (s - prow[p]) below the diagonal,
+  // pdu[p] + (s - pdiag[p]) from it on.
+  double* d_LU = nullptr;     // [25*nnzb] factors (FP64)
   float* d_LU32 = nullptr;    // [25*nnzb] factors (FP32)
+  int* d_plst = nullptr;      // [nC] storage block of the first L block of every position
+  int* d_pdu = nullptr;       // [nC] storage block of the diagonal block of every position
   int ilu_nlev_f = 0, ilu_nlev_b = 0;
   std::vector<int> lev_f, lev_b;    // level pointers (colour starts when colouring)
   std::vector<char> lev_f_hasL;     // forward level l has L blocks (else y = r there: no launch)
@@ -100,7 +106,7 @@ struct fos_ctx {
   int* d_lrows_f = nullptr;         // level-ordered positions (null when levels are ranges)
   int* d_lrows_b = nullptr;
   int* d_upd_ptr = nullptr;   // [nC+1] per position
-  int3* d_upd = nullptr;      // (slot_pq, slot_qj or diag(q), slot_pj or -1)
+  int3* d_upd = nullptr;      // (slot_pq, storage block of inv(D_q) or U_qj, slot_pj or -1)
   int ilu_ierr = 0;
   int ilu_colors = 0;            // > 0: ILU order is colour-major (FOS_ILU_COLOR)
   bool has_factor = false;

@@ -15,11 +15,14 @@
 //
 // Preconditioner: P = I - gamma diag(1/v) J, factored by block ILU(0) (the block
 // form of SPARSKIT ilu0, ITSOL/ilut.f:1793-1917: equal to scalar ILU(0) of the
-// interleaved matrix), with the inverse of each diagonal block stored in its slot
-// like ilu0 stores the inverted diagonal.  The ILU works in "position" space: block row
+// interleaved matrix), with the inverse of each diagonal block stored in place of the
+// block like ilu0 stores the inverted diagonal.  The ILU works in "position" space: block row
 // p is the p-th row of the elimination order (internal order, or colour-major for
 // FOS_ILU_COLOR); each row's blocks are contiguous and sorted by position, so lower(p) =
-// [prow[p], pdiag[p]) and upper(p) = (pdiag[p], prow[p+1]).  Rows are processed level by
+// [prow[p], pdiag[p]) and upper(p) = (pdiag[p], prow[p+1]).  The factors are stored in two
+// regions, every row's L blocks first and then every row's inverted diagonal and U blocks
+// (plst / pdu), so that the forward and the backward sweep each stream one region without
+// reading around the blocks they skip.  Rows are processed level by
 // level: colours (contiguous ranges of p) for FOS_ILU_COLOR, otherwise the level sets of
 // the lower / upper triangles (one more than the highest level among the row's lower /
 // upper neighbours, cf. SPARSKIT levels, FORMATS/unary.f:1078).  Apply = lusol
@@ -403,7 +406,8 @@ __global__ void __launch_bounds__(kT) k_ilu_factor(
     int n, const int* __restrict__ rows, int p0, const int* __restrict__ prow,
     const int* __restrict__ pdiag, const int* __restrict__ ord, const double* __restrict__ invV,
     double gamma, const TJ* __restrict__ J, const int* __restrict__ upd_ptr,
-    const int3* __restrict__ upd, TF* __restrict__ LU, int* __restrict__ ierr) {
+    const int3* __restrict__ upd, const int* __restrict__ plst, const int* __restrict__ pdu,
+    TF* __restrict__ LU, int* __restrict__ ierr) {
   // update operands (inv(D_q), U_qj of earlier levels) of the first kPre operations of a row
   // are fetched into shared memory before the elimination, all loads in flight at once
   constexpr int kPre = sizeof(TF) == 4 ? 8 : 0;
@@ -500,9 +504,10 @@ __global__ void __launch_bounds__(kT) k_ilu_factor(
   if (!ok) atomicMin(ierr, p + 1);
 #pragma unroll
   for (int b = 0; b < 5; b++) sm(lrow, sd - s0)[5 * a + b] = D[b];
-  const int nb = prow[p + 1] - s0;
+  // block b of the row: L blocks into the L region, the diagonal and U blocks into the D/U one
+  const int nb = prow[p + 1] - s0, nl = sd - s0, bl = plst[p], bdu = pdu[p];
   for (int b = 0; b < nb; b++) {
-    TF* dst = LU + 25 * (size_t)(s0 + b) + 5 * a;
+    TF* dst = LU + 25 * (size_t)(b < nl ? bl + b : bdu + (b - nl)) + 5 * a;
 #pragma unroll
     for (int k = 0; k < 5; k++) dst[k] = sm(lrow, b)[5 * a + k];
   }
@@ -601,6 +606,8 @@ __global__ void __launch_bounds__(kT) k_ilu_fwd(int n, const int* __restrict__ r
                                                 const int* __restrict__ prow,
                                                 const int* __restrict__ pcol,
                                                 const int* __restrict__ pdiag,
+                                                const int* __restrict__ plst,
+                                                const int* __restrict__ pdu,
                                                 const TF* __restrict__ LU, TF* __restrict__ yv,
                                                 TF* __restrict__ zv) {
   const int lane = threadIdx.x & 31;
@@ -612,15 +619,17 @@ __global__ void __launch_bounds__(kT) k_ilu_fwd(int n, const int* __restrict__ r
   TF acc = TF(0);
   if (active) {
     acc = yv[8 * (size_t)p + a];
-    for (int s = prow[p]; s < pdiag[p]; s++) {
+    const int s0 = prow[p], s1 = pdiag[p];
+    const TF* Lp = LU + 25 * (size_t)plst[p] + 5 * a;  // the row's L blocks, in order
+    for (int s = s0; s < s1; s++) {
       const TF* yq = yv + 8 * (size_t)pcol[s];
-      const TF* B = LU + 25 * (size_t)s + 5 * a;
+      const TF* B = Lp + 25 * (s - s0);
 #pragma unroll
       for (int b = 0; b < 5; b++) acc -= __ldg(B + b) * yq[b];
     }
   }
   if constexpr (kDiag)
-    ilu_diag_store(lane, a, active, p, acc, LU + 25 * (size_t)(active ? pdiag[p] : 0) + 5 * a, zv);
+    ilu_diag_store(lane, a, active, p, acc, LU + 25 * (size_t)(active ? pdu[p] : 0) + 5 * a, zv);
   else
     yv[8 * (size_t)p + a] = acc;
 }
@@ -630,6 +639,7 @@ __global__ void __launch_bounds__(kT) k_ilu_bwd(int n, const int* __restrict__ r
                                                 const int* __restrict__ prow,
                                                 const int* __restrict__ pcol,
                                                 const int* __restrict__ pdiag,
+                                                const int* __restrict__ pdu,
                                                 const TF* __restrict__ LU,
                                                 const TF* __restrict__ yv, TF* __restrict__ zv) {
   const int lane = threadIdx.x & 31;
@@ -638,16 +648,19 @@ __global__ void __launch_bounds__(kT) k_ilu_bwd(int n, const int* __restrict__ r
   const bool active = sub < 6 && t < n;
   const int p = active ? (rows ? rows[t] : p0 + t) : 0;
   TF acc = TF(0);
+  const TF* Dp = LU + 5 * a;  // inv(D_p), followed by the row's U blocks in order
   if (active) {
     acc = yv[8 * (size_t)p + a];
-    for (int s = pdiag[p] + 1; s < prow[p + 1]; s++) {
+    const int sd = pdiag[p], s1 = prow[p + 1];
+    Dp += 25 * (size_t)pdu[p];
+    for (int s = sd + 1; s < s1; s++) {
       const TF* zq = zv + 8 * (size_t)pcol[s];
-      const TF* B = LU + 25 * (size_t)s + 5 * a;
+      const TF* B = Dp + 25 * (s - sd);
 #pragma unroll
       for (int b = 0; b < 5; b++) acc -= __ldg(B + b) * zq[b];
     }
   }
-  ilu_diag_store(lane, a, active, p, acc, LU + 25 * (size_t)(active ? pdiag[p] : 0) + 5 * a, zv);
+  ilu_diag_store(lane, a, active, p, acc, Dp, zv);
 }
 
 }  // namespace
@@ -793,6 +806,16 @@ int fos_jac_setup(fos_ctx* c) {
     for (int p = c->lev_f[top]; p < c->lev_f[top + 1] && noU; p++) noU = prow[p + 1] == pdiag[p] + 1;
     c->ilu_fuse_top = noU;
   }
+  // factor storage: the L region (every row's L blocks by position), then the D/U region
+  std::vector<int> plst(nC), pdu(nC);
+  {
+    int nl = 0;
+    for (int p = 0; p < nC; p++) {
+      plst[p] = nl;
+      nl += pdiag[p] - prow[p];
+    }
+    for (int p = 0; p < nC; p++) pdu[p] = nl + (prow[p] - plst[p]);
+  }
   // factor update lists (IKJ): for q in lower(p) by position: scale L_pq, then
   // P_pj -= L_pq U_qj for every j in upper(q) that is also in row p
   std::vector<int> upd_ptr(nC + 1, 0);
@@ -801,10 +824,10 @@ int fos_jac_setup(fos_ctx* c) {
   for (int p = 0; p < nC; p++) {
     for (int s = prow[p]; s < pdiag[p]; s++) {
       const int q = pcol[s];
-      upd.push_back(make_int3(s, pdiag[q], -1));
+      upd.push_back(make_int3(s, pdu[q], -1));
       for (int t = pdiag[q] + 1; t < prow[q + 1]; t++) {
         const int sij = slot_of(p, pcol[t]);
-        if (sij >= 0) upd.push_back(make_int3(s, t, sij));
+        if (sij >= 0) upd.push_back(make_int3(s, pdu[q] + (t - pdiag[q]), sij));
       }
     }
     upd_ptr[p + 1] = (int)upd.size();
@@ -813,7 +836,8 @@ int fos_jac_setup(fos_ctx* c) {
   c->h_pcol = pcol;
   if (up(&c->d_prow, prow) || up(&c->d_pcol, pcol) || up(&c->d_pdiag, pdiag) ||
       up(&c->d_cdiag, cdiag) || up(&c->d_ipos, ipos) || up(&c->d_ord, ord) ||
-      up(&c->d_fslot, fslot) || up(&c->d_upd_ptr, upd_ptr) || up(&c->d_upd, upd))
+      up(&c->d_fslot, fslot) || up(&c->d_upd_ptr, upd_ptr) || up(&c->d_upd, upd) ||
+      up(&c->d_plst, plst) || up(&c->d_pdu, pdu))
     return -100;
   if (!rows_f.empty() && (up(&c->d_lrows_f, rows_f) || up(&c->d_lrows_b, rows_b))) return -100;
   const bool f32 = (c->flags & FOS_ILU_FP32) != 0;
@@ -883,7 +907,7 @@ static int ilu_factor_t(fos_ctx* c, double gamma, TF* LU) {
     fos_launch(c, k_ilu_factor<TF, TJ>, nb_rows5(n), kT, n, rows, c->lev_f[l],
                (const int*)c->d_prow, (const int*)c->d_pdiag, (const int*)c->d_ord,
                (const double*)c->d_invV, gamma, (const TJ*)c->d_Jraw, (const int*)c->d_upd_ptr,
-               (const int3*)c->d_upd, LU, c->d_ierr);
+               (const int3*)c->d_upd, (const int*)c->d_plst, (const int*)c->d_pdu, LU, c->d_ierr);
   }
   FOS_LAUNCH_CHECK();
   return 0;
@@ -917,10 +941,12 @@ static int ilu_apply_t(fos_ctx* c, const TF* LU, const double* r, double* z,
     const int* rows = c->d_lrows_f ? c->d_lrows_f + c->lev_f[l] : nullptr;
     if (c->ilu_fuse_top && l == nf - 1)
       fos_launch(c, k_ilu_fwd<TF, true>, nb_rows5(n), kT, n, rows, c->lev_f[l],
-                 (const int*)c->d_prow, (const int*)c->d_pcol, (const int*)c->d_pdiag, LU, yv, zv);
+                 (const int*)c->d_prow, (const int*)c->d_pcol, (const int*)c->d_pdiag,
+                 (const int*)c->d_plst, (const int*)c->d_pdu, LU, yv, zv);
     else if (c->lev_f_hasL[l])  // a level without L blocks keeps y = r
       fos_launch(c, k_ilu_fwd<TF, false>, nb_rows5(n), kT, n, rows, c->lev_f[l],
-                 (const int*)c->d_prow, (const int*)c->d_pcol, (const int*)c->d_pdiag, LU, yv, zv);
+                 (const int*)c->d_prow, (const int*)c->d_pcol, (const int*)c->d_pdiag,
+                 (const int*)c->d_plst, (const int*)c->d_pdu, LU, yv, zv);
   }
   for (int l = c->ilu_fuse_top ? 1 : 0; l < c->ilu_nlev_b; l++) {
     // colours run backwards for the upper sweep
@@ -928,7 +954,8 @@ static int ilu_apply_t(fos_ctx* c, const TF* LU, const double* r, double* z,
     const int n = c->lev_b[lc + 1] - c->lev_b[lc];
     const int* rows = c->d_lrows_b ? c->d_lrows_b + c->lev_b[lc] : nullptr;
     fos_launch(c, k_ilu_bwd<TF>, nb_rows5(n), kT, n, rows, c->lev_b[lc], (const int*)c->d_prow,
-               (const int*)c->d_pcol, (const int*)c->d_pdiag, LU, (const TF*)yv, zv);
+               (const int*)c->d_pcol, (const int*)c->d_pdiag, (const int*)c->d_pdu, LU,
+               (const TF*)yv, zv);
   }
   if (d_zsq) {
     fos_launch(c, k_ilu_out_sq<TF>, kRedBlocks, kRedThreads, c->nC, (const int*)c->d_ipos,
