@@ -226,13 +226,18 @@ __device__ __forceinline__ PrimT<float> load_prim_f32(const float* __restrict__ 
 
 // Cell-centric FP32 assembly: one thread per cell, cells in the internal (bandwidth-
 // reduced) order, so neighbouring cells' primitives and face data are L2 hits.  A thread
-// evaluates each face of its cell in the face's orientation (Roe average, |A~|, both
-// normal flux Jacobians -- the same expressions for both cells of the face) and keeps
-//   off-diagonal block:  cell L: block (L, R) = -aP/2 (A(u_R) - |A~|)
-//                        cell R: block (R, L) =  aP/2 (A(u_L) + |A~|)
-//   diagonal:            minus the column's off-diagonal blocks, plus the boundary pairs'
-//                        terms -aP/2 (A(u_m) + |A~|), in ELL order, in registers,
-// staging its block row (contiguous in position space) in shared memory; the warp then
+// evaluates each face of its cell in the face's orientation (Roe average, |A~| -- the same
+// expressions for both cells of the face -- and the neighbour's normal flux Jacobian) and
+// keeps
+//   off-diagonal block:  cell L: block (L, R) = -aP/2 (A(n; u_R) - |A~|)
+//                        cell R: block (R, L) =  aP/2 (A(n; u_L) + |A~|)
+//   diagonal:            -sum_f aP/2 (A(n_out; u_c) + |A~|) over all faces of the cell,
+//                        in registers.
+// A(n; u) is linear in n, so the cell's own-state terms sum to A(S_c/2; u_c), S_c = sum of
+// aP n_out: zero for cells with planar faces (tetrahedra; the FP32 sum of the per-face terms
+// would only add rounding) and formed once from the closure vector otherwise (warped
+// hexahedra).  |A~| is even in n, so the diagonal takes -aP/2 |A~| from every face.  The row
+// is staged (contiguous in position space) in shared memory; the warp then
 // stores the 32 rows one after another, each as contiguous 128-byte pieces.  Each face is
 // evaluated by both of its cells: FP32 arithmetic is cheap next to the scattered block
 // stores and the re-read of every off-diagonal block that a face-then-diagonal assembly
@@ -242,8 +247,8 @@ __global__ void __launch_bounds__(64) k_jac_cell32(
     int nC, int nFi, const int* __restrict__ ipos, const int* __restrict__ prow,
     const int* __restrict__ cdiag, const int* __restrict__ ell, const int2* __restrict__ faceLR,
     const float4* __restrict__ faceNA32, const int* __restrict__ fslot,
-    const float* __restrict__ Whl, const double* __restrict__ Gb, double g,
-    float* __restrict__ J) {
+    const float* __restrict__ Whl, const double* __restrict__ Gb, const float4* __restrict__ Sc,
+    double g, float* __restrict__ J) {
   constexpr int kRow = (kW + 1) * 25;  // floats of a full block row
   __shared__ float stg[2][32][kRow];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -287,29 +292,34 @@ __global__ void __launch_bounds__(64) k_jac_cell32(
           sqrtf((gg - 1.0f) * (Ha - 0.5f * (ua[0] * ua[0] + ua[1] * ua[1] + ua[2] * ua[2])));
       float Ab[25];
       anfj<float>(n, ua, Ha, ca, gg, Ab);
-      const float v2L = L.u[0] * L.u[0] + L.u[1] * L.u[1] + L.u[2] * L.u[2];
-      const float vnL = L.u[0] * n[0] + L.u[1] * n[1] + L.u[2] * n[2];
-      const float v2R = R.u[0] * R.u[0] + R.u[1] * R.u[1] + R.u[2] * R.u[2];
-      const float vnR = R.u[0] * n[0] + R.u[1] * n[1] + R.u[2] * n[2];
       const float h = 0.5f * na.w;
-      if (f >= nFi) {  // boundary pair: diagonal term only
+      if (f >= nFi) {  // boundary pair: diagonal term only (its A(u_c) part is in S_c)
 #pragma unroll
-        for (int a = 0; a < 5; a++)
-#pragma unroll
-          for (int b = 0; b < 5; b++)
-            D[5 * a + b] += -h * (nfj<float>(a, b, n, L.u, L.H, gg, v2L, vnL) + Ab[5 * a + b]);
+        for (int k = 0; k < 25; k++) D[k] -= h * Ab[k];
         continue;
       }
+      // the neighbour's normal flux Jacobian with the face normal: +aP/2 for cell R, -aP/2 for L
+      const float v2Q = Q.u[0] * Q.u[0] + Q.u[1] * Q.u[1] + Q.u[2] * Q.u[2];
+      const float vnQ = Q.u[0] * n[0] + Q.u[1] * n[1] + Q.u[2] * n[2];
+      const float sh = isR ? h : -h;
       float* off = st + 25 * (fslot[2 * f + (isR ? 1 : 0)] - s0);
 #pragma unroll
       for (int a = 0; a < 5; a++)
 #pragma unroll
         for (int b = 0; b < 5; b++) {
-          const float bLR = -h * (nfj<float>(a, b, n, R.u, R.H, gg, v2R, vnR) - Ab[5 * a + b]);
-          const float bRL = h * (nfj<float>(a, b, n, L.u, L.H, gg, v2L, vnL) + Ab[5 * a + b]);
-          off[5 * a + b] = isR ? bRL : bLR;
-          D[5 * a + b] -= isR ? bLR : bRL;
+          off[5 * a + b] = sh * nfj<float>(a, b, n, Q.u, Q.H, gg, v2Q, vnQ) + h * Ab[5 * a + b];
+          D[5 * a + b] -= h * Ab[5 * a + b];
         }
+    }
+    if (Sc) {  // -A(S_c/2; u_c): the own-state terms of a cell whose faces do not close
+      const float4 S4 = __ldg(Sc + c);
+      const float Sh[3] = {0.5f * S4.x, 0.5f * S4.y, 0.5f * S4.z};
+      const float v2P = P.u[0] * P.u[0] + P.u[1] * P.u[1] + P.u[2] * P.u[2];
+      const float vnP = P.u[0] * Sh[0] + P.u[1] * Sh[1] + P.u[2] * Sh[2];
+#pragma unroll
+      for (int a = 0; a < 5; a++)
+#pragma unroll
+        for (int b = 0; b < 5; b++) D[5 * a + b] -= nfj<float>(a, b, Sh, P.u, P.H, gg, v2P, vnP);
     }
     float* dg = st + 25 * (cdiag[c] - s0);
 #pragma unroll
@@ -868,12 +878,14 @@ static int jac_assemble_t(fos_ctx* c, const double* y) {
       fos_launch(c, k_jac_cell32<4>, grid, 64, c->nC, c->nFi, (const int*)c->d_ipos,
                  (const int*)c->d_prow, (const int*)c->d_cdiag, (const int*)c->d_ell,
                  (const int2*)c->d_faceLR, (const float4*)c->d_faceNA32, (const int*)c->d_fslot,
-                 (const float*)c->d_Whl, (const double*)c->d_F, c->gamm, J);
+                 (const float*)c->d_Whl, (const double*)c->d_F, (const float4*)c->d_closure32,
+                 c->gamm, J);
     else
       fos_launch(c, k_jac_cell32<6>, grid, 64, c->nC, c->nFi, (const int*)c->d_ipos,
                  (const int*)c->d_prow, (const int*)c->d_cdiag, (const int*)c->d_ell,
                  (const int2*)c->d_faceLR, (const float4*)c->d_faceNA32, (const int*)c->d_fslot,
-                 (const float*)c->d_Whl, (const double*)c->d_F, c->gamm, J);
+                 (const float*)c->d_Whl, (const double*)c->d_F, (const float4*)c->d_closure32,
+                 c->gamm, J);
     FOS_LAUNCH_CHECK();
     return 0;
   } else {
