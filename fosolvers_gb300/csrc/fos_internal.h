@@ -92,8 +92,8 @@ struct fos_ctx {
   bool has_jac = false;
   // factors in two regions, so that each sweep streams one: the L blocks of every row (by
   // position), then the diagonal block and the U blocks of every row; diag blocks hold the
-  // inverse.  Block storage of slot s in row p: plst[p] + (s - prow[p]) below the diagonal,
-  // pdu[p] + (s - pdiag[p]) from it on.
+  // inverse; 25 entries per block, column-major.  Block storage of slot s in row p:
+  // plst[p] + (s - prow[p]) below the diagonal, pdu[p] + (s - pdiag[p]) from it on.
   double* d_LU = nullptr;     // [25*nnzb] factors (FP64)
   float* d_LU32 = nullptr;    // [25*nnzb] factors (FP32)
   int* d_plst = nullptr;      // [nC] storage block of the first L block of every position

@@ -398,7 +398,9 @@ __device__ __forceinline__ bool inv5(T a[25]) {
 //   D_p = P_pp -> inverted by Gauss--Jordan without pivoting across the five lanes
 // A lane only touches its own row of row p's blocks and reads finished blocks of earlier
 // rows from global memory, so the lanes of a row need no synchronisation until the
-// diagonal inversion (warp shuffles).
+// diagonal inversion (warp shuffles).  The factor blocks are stored column-major (entry
+// (i, j) at 5 j + i): a load instruction of the sweeps then reads five consecutive floats
+// per block row instead of five floats 20 bytes apart.
 template <typename TF>
 __device__ __forceinline__ TF from64(double x) {
   if constexpr (sizeof(TF) == 4) return d2f_trunc(x); else return (TF)x;
@@ -447,7 +449,7 @@ __global__ void __launch_bounds__(kT) k_ilu_factor(
 #pragma unroll
       for (int o = 0; o < kPre; o++)
         if (o < no) {
-          const TF* B = LU + 25 * (size_t)upd[o0 + o].y + 5 * a;
+          const TF* B = LU + 25 * (size_t)upd[o0 + o].y + 5 * a;  // column a
 #pragma unroll
           for (int k = 0; k < 5; k++) pre[o][k] = B[k];
         }
@@ -478,13 +480,13 @@ __global__ void __launch_bounds__(kT) k_ilu_factor(
       TF* Ar = sm(lrow, op.x - s0) + 5 * a;
 #pragma unroll
       for (int k = 0; k < 5; k++) A[k] = Ar[k];
-      const TF* B = (o < kPre) ? bsm(lrow, o) : LU + 25 * (size_t)op.y;
+      const TF* B = (o < kPre) ? bsm(lrow, o) : LU + 25 * (size_t)op.y;  // column-major
       TF* dst = sm(lrow, (op.z < 0 ? op.x : op.z) - s0) + 5 * a;
 #pragma unroll
       for (int b = 0; b < 5; b++) {
         TF acc = 0;
 #pragma unroll
-        for (int k = 0; k < 5; k++) acc += A[k] * B[5 * k + b];
+        for (int k = 0; k < 5; k++) acc += A[k] * B[5 * b + k];
         dst[b] = op.z < 0 ? acc : dst[b] - acc;
       }
     }
@@ -517,9 +519,9 @@ __global__ void __launch_bounds__(kT) k_ilu_factor(
   // block b of the row: L blocks into the L region, the diagonal and U blocks into the D/U one
   const int nb = prow[p + 1] - s0, nl = sd - s0, bl = plst[p], bdu = pdu[p];
   for (int b = 0; b < nb; b++) {
-    TF* dst = LU + 25 * (size_t)(b < nl ? bl + b : bdu + (b - nl)) + 5 * a;
+    TF* dst = LU + 25 * (size_t)(b < nl ? bl + b : bdu + (b - nl)) + a;  // row a, column-major
 #pragma unroll
-    for (int k = 0; k < 5; k++) dst[k] = sm(lrow, b)[5 * a + k];
+    for (int k = 0; k < 5; k++) dst[5 * k] = sm(lrow, b)[5 * a + k];
   }
 }
 
@@ -588,7 +590,8 @@ __global__ void __launch_bounds__(kRedThreads) k_ilu_out_sq(int nC, const int* _
 }
 
 // Triangular sweeps in position space, five lanes per block row (lane a owns component
-// a and reads row a of every 5x5 block).  The forward sweep overwrites rv with y in place
+// a and reads row a of every 5x5 block, entries 5 apart in the column-major storage, so
+// the five lanes of a row read consecutive floats).  The forward sweep overwrites rv with y in place
 // (a row reads only its own rv and earlier rows' y).
 //   forward:  y_p = r_p - sum_{q in lower(p)} L_pq y_q           (unit block diagonal)
 //   backward: z_p = inv(D_p) (y_p - sum_{q in upper(p)} U_pq z_q)
@@ -604,7 +607,7 @@ __device__ __forceinline__ void ilu_diag_store(int lane, int a, bool active, int
   if (!active) return;
   TF zz = 0;
 #pragma unroll
-  for (int b = 0; b < 5; b++) zz += __ldg(Dr + b) * comp[b];
+  for (int b = 0; b < 5; b++) zz += __ldg(Dr + 5 * b) * comp[b];
   zv[8 * (size_t)p + a] = zz;
   if (a < 3) zv[8 * (size_t)p + 5 + a] = TF(0);
 }
@@ -630,16 +633,16 @@ __global__ void __launch_bounds__(kT) k_ilu_fwd(int n, const int* __restrict__ r
   if (active) {
     acc = yv[8 * (size_t)p + a];
     const int s0 = prow[p], s1 = pdiag[p];
-    const TF* Lp = LU + 25 * (size_t)plst[p] + 5 * a;  // the row's L blocks, in order
+    const TF* Lp = LU + 25 * (size_t)plst[p] + a;  // the row's L blocks, in order
     for (int s = s0; s < s1; s++) {
       const TF* yq = yv + 8 * (size_t)pcol[s];
       const TF* B = Lp + 25 * (s - s0);
 #pragma unroll
-      for (int b = 0; b < 5; b++) acc -= __ldg(B + b) * yq[b];
+      for (int b = 0; b < 5; b++) acc -= __ldg(B + 5 * b) * yq[b];
     }
   }
   if constexpr (kDiag)
-    ilu_diag_store(lane, a, active, p, acc, LU + 25 * (size_t)(active ? pdu[p] : 0) + 5 * a, zv);
+    ilu_diag_store(lane, a, active, p, acc, LU + 25 * (size_t)(active ? pdu[p] : 0) + a, zv);
   else
     yv[8 * (size_t)p + a] = acc;
 }
@@ -658,7 +661,7 @@ __global__ void __launch_bounds__(kT) k_ilu_bwd(int n, const int* __restrict__ r
   const bool active = sub < 6 && t < n;
   const int p = active ? (rows ? rows[t] : p0 + t) : 0;
   TF acc = TF(0);
-  const TF* Dp = LU + 5 * a;  // inv(D_p), followed by the row's U blocks in order
+  const TF* Dp = LU + a;  // inv(D_p), followed by the row's U blocks in order
   if (active) {
     acc = yv[8 * (size_t)p + a];
     const int sd = pdiag[p], s1 = prow[p + 1];
@@ -667,7 +670,7 @@ __global__ void __launch_bounds__(kT) k_ilu_bwd(int n, const int* __restrict__ r
       const TF* zq = zv + 8 * (size_t)pcol[s];
       const TF* B = Dp + 25 * (s - sd);
 #pragma unroll
-      for (int b = 0; b < 5; b++) acc -= __ldg(B + b) * zq[b];
+      for (int b = 0; b < 5; b++) acc -= __ldg(B + 5 * b) * zq[b];
     }
   }
   ilu_diag_store(lane, a, active, p, acc, Dp, zv);
