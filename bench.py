@@ -49,8 +49,8 @@ GNN_BYTES_PER_CELL = 120 + 216 + 3 * 368 + 208
 # the operation's kernels, L2 flushed before every kernel, so an upper bound); traffic
 # grows with the cell count, so the full-size figure is this times nC.  Summary and
 # command: profiles/traffic_sine64_fp32.md
-TRAFFIC_FP32_BYTES_PER_CELL = {"residual": 234.9, "jv": 403.2, "pset": 2257.3,
-                               "ilu_apply": 1038.1, "gnn_apply": 1161.6}
+TRAFFIC_FP32_BYTES_PER_CELL = {"residual": 235.0, "jv": 403.1, "pset": 2214.1,
+                               "ilu_apply": 800.0, "gnn_apply": 1162.1}
 
 
 def parse():
