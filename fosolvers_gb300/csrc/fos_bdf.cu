@@ -638,7 +638,8 @@ extern "C" int fos_bdf_run(fos_ctx* c, double t0, double* y, const fos_bdf_opts*
     const double gamma = q == 1 ? opts->dt : 2.0 * opts->dt / 3.0;
     const double tn = t + opts->dt;
     fos_launch(c, k_hist, nb(N), kT, N, q, wk.yn, wk.ym, wk.hist);
-    FOS_CUDA(cudaMemcpyAsync(y, wk.yn, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+    // the Newton iteration starts from y_n, which y holds: yn was copied from y before the
+    // first step and from the accepted y after every step
     const bool reuse = opts->msbp > 1 && last_setup >= 0 && c->has_factor &&
                        s - last_setup < opts->msbp &&
                        std::fabs(gamma / gamma_setup - 1.0) <= 0.3;
