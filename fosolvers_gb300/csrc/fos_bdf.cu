@@ -132,17 +132,21 @@ __global__ void k_axpy(long n, double a, const double* __restrict__ x, double* _
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) y[i] += a * x[i];
 }
-// x += sum_l c[l] Z_l
+// s = sum_l c[l] Z_l, summed from x (acc) or from zero; then x = s, or, with yadd, yadd += s
+// and x is not touched (the first restart cycle's correction added straight to the Newton
+// iterate: the same sums as x = s followed by yadd += x)
 __global__ void k_comb(long n, int nv, const double* __restrict__ Z, long ldz,
-                       const double* __restrict__ cc, double* __restrict__ x) {
+                       const double* __restrict__ cc, double* __restrict__ x, int acc,
+                       double* __restrict__ yadd) {
   __shared__ double cs[kMaxVec];
   if (threadIdx.x < kMaxVec) cs[threadIdx.x] = threadIdx.x < nv ? cc[threadIdx.x] : 0.0;
   __syncthreads();
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double s = x[i];
+  double s = acc ? x[i] : 0.0;
   for (int l = 0; l < nv; l++) s += cs[l] * Z[(size_t)l * ldz + i];
-  x[i] = s;
+  if (yadd) yadd[i] += s;
+  else x[i] = s;
 }
 // hist = y_n (q=1) or 4/3 y_n - 1/3 y_{n-1} (q=2)
 __global__ void k_hist(long n, int q, const double* __restrict__ yn, const double* __restrict__ ym,
@@ -416,13 +420,16 @@ struct Driver {
       }
       // ||b|| = ||G|| (b = -G) for the linear tolerance and GMRES's first basis vector
       int its = 0;
-      rc = gmres(y, wk.f, gamma, std::sqrt(hb[1]), gn, &its);
+      bool added = false;  // GMRES added d to y itself (it converged in its first cycle)
+      rc = gmres(y, wk.f, gamma, std::sqrt(hb[1]), gn, &its, y, &added);
       st.n_lin_iters += its;
       st.n_newton++;
       if (rc < 0) return rc;
       if (rc == 3) return 3;  // zero pivot in the ILU(0) factorisation
-      fos_launch(c, k_axpy, nb(N), kT, N, 1.0, wk.d, y);
-      FOS_LAUNCH_CHECK();
+      if (!added) {
+        fos_launch(c, k_axpy, nb(N), kT, N, 1.0, wk.d, y);
+        FOS_LAUNCH_CHECK();
+      }
     }
     return 1;
   }
@@ -430,8 +437,11 @@ struct Driver {
   // this is flexible GMRES (Z_j = M_j(V_j) kept); in modes 2 and 4 it falls back to ILU(0)
   // -- restarting from the current iterate -- when the residual estimate stagnates (> 0.9
   // of the previous one) or the iteration count reaches that of the last
-  // ILU(0)-preconditioned solve.
-  int gmres(const double* y, const double* fy, double gamma, double ynorm, double bnorm, int* its) {
+  // ILU(0)-preconditioned solve.  With y_add (the Newton iterate, read by the Jv until the
+  // end), a solve that converges in its first cycle adds d to y_add instead of storing d
+  // (*added); otherwise d is left in wk.d.
+  int gmres(const double* y, const double* fy, double gamma, double ynorm, double bnorm, int* its,
+            double* y_add = nullptr, bool* added = nullptr) {
     const long N = wk.N;
     const int m = o.maxl;
     pc = o.precond;
@@ -459,9 +469,14 @@ struct Driver {
     // normalises it.
     std::vector<double> sig(m + 1, 1.0), sig2(m + 1, 1.0);
     double* d_sig2 = wk.sc + 5 * kMaxVec;
-    FOS_CUDA(cudaMemsetAsync(wk.d, 0, sizeof(double) * N, c->stream));
+    if (added) *added = false;
+    bool d_written = false;  // wk.d holds the correction of the cycles so far
     *its = 0;
-    if (bnorm == 0.0) return 0;
+    if (bnorm == 0.0) {  // d = 0
+      if (y_add) *added = true;
+      else FOS_CUDA(cudaMemsetAsync(wk.d, 0, sizeof(double) * N, c->stream));
+      return 0;
+    }
     const double* rvec = wk.b;
     double beta = bnorm;
     for (int cyc = 0; cyc <= o.max_restarts + extra_cycles; cyc++) {
@@ -563,9 +578,12 @@ struct Driver {
       for (int l = 0; l < kend; l++) yv[l] *= sig[l];  // z_l = sig[l] z'_l
       FOS_CUDA(cudaMemcpyAsync(wk.sc + 4 * kMaxVec, yv.data(), sizeof(double) * kend,
                                cudaMemcpyHostToDevice, c->stream));
+      double* yadd = (conv && !d_written && y_add) ? y_add : nullptr;
       fos_launch(c, k_comb, nb(N), kT, N, kend, (const double*)wk.Z, N,
-                 (const double*)(wk.sc + 4 * kMaxVec), wk.d);
+                 (const double*)(wk.sc + 4 * kMaxVec), wk.d, d_written ? 1 : 0, yadd);
       FOS_LAUNCH_CHECK();
+      if (yadd) *added = true;
+      else d_written = true;
       if (conv) {
         if (pure_ilu) set_ilu_ref(*its, std::fabs(g[kend]), bnorm);
         if (with_fallback && pc != 1) wk.learned_backoff = 0;  // the network won this solve
