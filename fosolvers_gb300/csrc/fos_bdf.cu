@@ -155,17 +155,20 @@ __global__ void k_hist(long n, int q, const double* __restrict__ yn, const doubl
   if (i >= n) return;
   h[i] = q == 1 ? yn[i] : (4.0 / 3.0) * yn[i] - (1.0 / 3.0) * ym[i];
 }
-// G = y - gamma f - hist; b = -G; part0 <- sum G^2, part1 <- sum y^2
+// G = y - gamma f - hist; b = -G (also into b2: the first Arnoldi vector, unnormalised);
+// part0 <- sum G^2, part1 <- sum y^2
 __global__ void __launch_bounds__(kT) k_newton_res(long n, const double* __restrict__ y,
                                                    const double* __restrict__ f,
                                                    const double* __restrict__ hist,
                                                    double gamma, double* __restrict__ b,
+                                                   double* __restrict__ b2,
                                                    double* __restrict__ part) {
   double acc[2] = {0.0, 0.0};
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     const double yi = y[i];
     const double G = yi - gamma * f[i] - hist[i];
     b[i] = -G;
+    b2[i] = -G;
     acc[0] += G * G;
     acc[1] += yi * yi;
   }
@@ -400,7 +403,7 @@ struct Driver {
       if (rc) return rc;
       st.n_rhs++;
       fos_launch(c, k_newton_res, kRedBlocks, kT, N, (const double*)y, (const double*)wk.f,
-                 hist, gamma, wk.b, wk.part);
+                 hist, gamma, wk.b, wk.V, wk.part);
       if ((rc = reduce(2, wk.sc))) return rc;
       FOS_CUDA(cudaMemcpyAsync(hb, wk.sc, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
       FOS_CUDA(cudaMemcpyAsync(c->h_scal, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -421,7 +424,7 @@ struct Driver {
       // ||b|| = ||G|| (b = -G) for the linear tolerance and GMRES's first basis vector
       int its = 0;
       bool added = false;  // GMRES added d to y itself (it converged in its first cycle)
-      rc = gmres(y, wk.f, gamma, std::sqrt(hb[1]), gn, &its, y, &added);
+      rc = gmres(y, wk.f, gamma, std::sqrt(hb[1]), gn, &its, y, &added, true);
       st.n_lin_iters += its;
       st.n_newton++;
       if (rc < 0) return rc;
@@ -439,9 +442,10 @@ struct Driver {
   // of the previous one) or the iteration count reaches that of the last
   // ILU(0)-preconditioned solve.  With y_add (the Newton iterate, read by the Jv until the
   // end), a solve that converges in its first cycle adds d to y_add instead of storing d
-  // (*added); otherwise d is left in wk.d.
+  // (*added); otherwise d is left in wk.d.  v0_is_b: V_0 already holds b (the Newton
+  // residual kernel wrote it there), used unnormalised in the first cycle.
   int gmres(const double* y, const double* fy, double gamma, double ynorm, double bnorm, int* its,
-            double* y_add = nullptr, bool* added = nullptr) {
+            double* y_add = nullptr, bool* added = nullptr, bool v0_is_b = false) {
     const long N = wk.N;
     const int m = o.maxl;
     pc = o.precond;
@@ -459,7 +463,8 @@ struct Driver {
     int extra_cycles = 0;
     std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), yv(m), hbuf(4 * kMaxVec);
     // The Arnoldi vectors are kept unnormalised: V_l holds W_l and v_l = sig[l] W_l with
-    // sig[l] = 1 / ||W_l|| (v_0 is normalised when it is formed).  The new vector of step j
+    // sig[l] = 1 / ||W_l|| (W_0 = b in a Newton solve's first cycle, else the normalised
+    // residual of the restart).  The new vector of step j
     // is J_G z'_j written straight into slot j+1, where z'_j = M(W_j) is the preconditioner
     // applied to the stored W_j; the Arnoldi relation uses z_j = sig[j] z'_j (the FD Jv and
     // ILU(0) are homogeneous, and flexible GMRES takes any z_j), so J_G z_j = sig[j] W_{j+1}
@@ -480,8 +485,13 @@ struct Driver {
     const double* rvec = wk.b;
     double beta = bnorm;
     for (int cyc = 0; cyc <= o.max_restarts + extra_cycles; cyc++) {
-      fos_launch(c, k_scale, nb(N), kT, N, rvec, 1.0 / beta, wk.V);
-      sig[0] = sig2[0] = 1.0;
+      if (cyc == 0 && v0_is_b) {  // W_0 = b, v_0 = b / beta
+        sig[0] = 1.0 / beta;
+        sig2[0] = sig[0] * sig[0];
+      } else {
+        fos_launch(c, k_scale, nb(N), kT, N, rvec, 1.0 / beta, wk.V);
+        sig[0] = sig2[0] = 1.0;
+      }
       FOS_CUDA(cudaMemcpyAsync(d_sig2, sig2.data(), sizeof(double), cudaMemcpyHostToDevice,
                                c->stream));
       bool fallback = false;
