@@ -52,43 +52,12 @@ __device__ __forceinline__ void block_reduce_store(double (&acc)[NV], int nv, do
   }
 }
 
-// The second stage of the reduction inside the first stage's kernel: the last block to
-// finish (its ticket taken after its partials are visible) forms out[l] for l < nv with
-// exactly the sums of a 256-thread block per l -- thread t adds part[l np + t + 256 k] in
-// order, each warp reduces by butterfly and keeps lane 0's value, lane 0 of a butterfly
-// over the 8 warp sums is the result -- one warp per l, and resets the ticket.  No second
-// launch.
-__device__ __forceinline__ void finish_last_block(int nv, const double* part,
-                                                  double* __restrict__ out, unsigned* ticket) {
-  __shared__ unsigned s_ticket;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) s_ticket = atomicAdd(ticket, 1u);
-  __syncthreads();
-  if (s_ticket != gridDim.x - 1) return;
-  __threadfence();
-  const int np = gridDim.x, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int l = wid; l < nv; l += kT / 32) {
-    double ws = 0.0;  // lane w ends with warp w's sum
-    for (int w = 0; w < kT / 32; w++) {
-      double s = 0.0;
-      for (int i = w * 32 + lane; i < np; i += kT) s += __ldcg(part + (size_t)l * np + i);
-      s = __shfl_sync(0xffffffffu, warp_sum(s), 0);
-      if (lane == w) ws = s;
-    }
-    const double tot = warp_sum(lane < kT / 32 ? ws : 0.0);
-    if (lane == 0) out[l] = tot;
-  }
-  if (threadIdx.x == 0) *ticket = 0u;
-}
-
 // h[l] = V_l . w for l < NV (NV fixed at compile time: accumulators stay in registers),
 // plus h[NV] = ||w||^2 when NRM
 template <int NV, bool NRM>
 __global__ void __launch_bounds__(kT) k_mdot(long n, const double* __restrict__ V, long ldv,
                                              const double* __restrict__ w,
-                                             double* __restrict__ part, double* __restrict__ out,
-                                             unsigned* ticket) {
+                                             double* __restrict__ part) {
   constexpr int NA = NV + (NRM ? 1 : 0);
   double acc[NA];
 #pragma unroll
@@ -100,7 +69,6 @@ __global__ void __launch_bounds__(kT) k_mdot(long n, const double* __restrict__ 
     if (NRM) acc[NA - 1] += wi * wi;
   }
   block_reduce_store<NA>(acc, NA, part);
-  finish_last_block(NA, part, out, ticket);
 }
 
 // w -= sum_l h[l] s2[l] V_l ; then part <- V_l . w (MODE 0, CGS2 second pass), ||w||^2
@@ -113,8 +81,7 @@ __global__ void __launch_bounds__(kT) k_update(long n, const double* __restrict_
                                                const double* __restrict__ h,
                                                const double* __restrict__ s2,
                                                double* __restrict__ w,
-                                               double* __restrict__ part,
-                                               double* __restrict__ out, unsigned* ticket) {
+                                               double* __restrict__ part) {
   __shared__ double hs[NV];
   if (threadIdx.x < NV) hs[threadIdx.x] = s2 ? h[threadIdx.x] * s2[threadIdx.x] : h[threadIdx.x];
   __syncthreads();
@@ -138,7 +105,23 @@ __global__ void __launch_bounds__(kT) k_update(long n, const double* __restrict_
     if (MODE != 0) acc[NA - 1] += wi * wi;
   }
   block_reduce_store<NA>(acc, NA, part);
-  finish_last_block(NA, part, out, ticket);
+}
+
+// out[l] = sum of part[l * np ...]
+__global__ void k_final(int nv, int np, const double* __restrict__ part, double* __restrict__ out) {
+  const int l = blockIdx.x;
+  if (l >= nv) return;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) s += part[(size_t)l * np + i];
+  __shared__ double sh[32];
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double t = threadIdx.x < (int)(blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+    t = warp_sum(t);
+    if (threadIdx.x == 0) out[l] = t;
+  }
 }
 
 __global__ void k_scale(long n, const double* __restrict__ x, double a, double* __restrict__ y) {
@@ -179,8 +162,7 @@ __global__ void __launch_bounds__(kT) k_newton_res(long n, const double* __restr
                                                    const double* __restrict__ hist,
                                                    double gamma, double* __restrict__ b,
                                                    double* __restrict__ b2,
-                                                   double* __restrict__ part,
-                                                   double* __restrict__ out, unsigned* ticket) {
+                                                   double* __restrict__ part) {
   double acc[2] = {0.0, 0.0};
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     const double yi = y[i];
@@ -191,7 +173,6 @@ __global__ void __launch_bounds__(kT) k_newton_res(long n, const double* __restr
     acc[1] += yi * yi;
   }
   block_reduce_store<2>(acc, 2, part);
-  finish_last_block(2, part, out, ticket);
 }
 
 // out = sum_l c[l] p[l] (up to 8 vectors, summed in order l = 0, 1, ...)
@@ -210,15 +191,13 @@ __global__ void k_lincomb(long n, Comb8 cb, double* __restrict__ out) {
 // part <- sum of (a_i / (rtol |w_i| + atol))^2 (weighted RMS norm, before the mean)
 __global__ void __launch_bounds__(kT) k_wrms_part(long n, const double* __restrict__ a,
                                                   const double* __restrict__ w, double rtol,
-                                                  double atol, double* __restrict__ part,
-                                                  double* __restrict__ out, unsigned* ticket) {
+                                                  double atol, double* __restrict__ part) {
   double acc[1] = {0.0};
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     const double e = a[i] / (rtol * fabs(w[i]) + atol);
     acc[0] += e * e;
   }
   block_reduce_store<1>(acc, 1, part);
-  finish_last_block(1, part, out, ticket);
 }
 
 inline int nb(long n) { return (int)((n + kT - 1) / kT); }
@@ -241,13 +220,11 @@ struct fos_bdf_work {
   // vectors of this and the previous step, scratch
   double* ay[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   double *ypred = nullptr, *E = nullptr, *Eprev = nullptr, *atmp = nullptr;
-  unsigned* ticket = nullptr;  // the reductions' last-block ticket (zero between kernels)
   ~fos_bdf_work() {
     for (double* p : {V, Z, w, yn, ym, hist, f, b, d, part, sc, yh, u, ypred, E, Eprev, atmp})
       if (p) cudaFree(p);
     for (double* p : ay)
       if (p) cudaFree(p);
-    if (ticket) cudaFree(ticket);
   }
 };
 void fos_bdf_work_free(fos_bdf_work* w) { delete w; }
@@ -274,8 +251,6 @@ int work_get(fos_ctx* c, int maxl, Work** out) {
     FOS_CUDA(cudaMalloc(p, sizeof(double) * N));
   FOS_CUDA(cudaMalloc(&wk->part, sizeof(double) * kRedBlocks * kMaxVec));
   FOS_CUDA(cudaMalloc(&wk->sc, sizeof(double) * 6 * kMaxVec));
-  FOS_CUDA(cudaMalloc(&wk->ticket, sizeof(unsigned)));
-  FOS_CUDA(cudaMemset(wk->ticket, 0, sizeof(unsigned)));
   *out = wk;
   return 0;
 }
@@ -324,12 +299,16 @@ struct Driver {
     ilu_ref_rate = (its > 0 && bnorm > 0.0 && res > 0.0) ? std::pow(res / bnorm, 1.0 / its) : 0.0;
   }
 
-  // V^T w (and ||w||^2 when NRM) into device out
+  int reduce(int nv, double* out) {  // k_final over wk.part into device out
+    fos_launch(c, k_final, nv, 256, nv, kRedBlocks, wk.part, out);
+    FOS_LAUNCH_CHECK();
+    return 0;
+  }
   template <bool NRM>
-  int mdot(int nv, const double* V, long ldv, const double* w, double* out) {
+  int mdot(int nv, const double* V, long ldv, const double* w) {
     switch (nv) {
 #define FOS_MDOT(K) \
-  case K: fos_launch(c, k_mdot<K, NRM>, kRedBlocks, kT, wk.N, V, ldv, w, wk.part, out, wk.ticket); break;
+  case K: fos_launch(c, k_mdot<K, NRM>, kRedBlocks, kT, wk.N, V, ldv, w, wk.part); break;
       FOS_MDOT(1) FOS_MDOT(2) FOS_MDOT(3) FOS_MDOT(4) FOS_MDOT(5) FOS_MDOT(6) FOS_MDOT(7)
       FOS_MDOT(8) FOS_MDOT(9) FOS_MDOT(10) FOS_MDOT(11) FOS_MDOT(12) FOS_MDOT(13) FOS_MDOT(14)
       FOS_MDOT(15) FOS_MDOT(16) FOS_MDOT(17) FOS_MDOT(18) FOS_MDOT(19) FOS_MDOT(20) FOS_MDOT(21)
@@ -341,13 +320,12 @@ struct Driver {
     FOS_LAUNCH_CHECK();
     return 0;
   }
-  // w -= V s2 h; its sums (MODE) into device out
   template <int MODE>
-  int update(int nv, const double* V, long ldv, const double* h, double* w, const double* s2,
-             double* out) {
+  int update(int nv, const double* V, long ldv, const double* h, double* w,
+             const double* s2 = nullptr) {
     switch (nv) {
 #define FOS_UPD(K) \
-  case K: fos_launch(c, k_update<K, MODE>, kRedBlocks, kT, wk.N, V, ldv, h, s2, w, wk.part, out, wk.ticket); break;
+  case K: fos_launch(c, k_update<K, MODE>, kRedBlocks, kT, wk.N, V, ldv, h, s2, w, wk.part); break;
       FOS_UPD(1) FOS_UPD(2) FOS_UPD(3) FOS_UPD(4) FOS_UPD(5) FOS_UPD(6) FOS_UPD(7) FOS_UPD(8)
       FOS_UPD(9) FOS_UPD(10) FOS_UPD(11) FOS_UPD(12) FOS_UPD(13) FOS_UPD(14) FOS_UPD(15)
       FOS_UPD(16) FOS_UPD(17) FOS_UPD(18) FOS_UPD(19) FOS_UPD(20) FOS_UPD(21) FOS_UPD(22)
@@ -425,8 +403,8 @@ struct Driver {
       if (rc) return rc;
       st.n_rhs++;
       fos_launch(c, k_newton_res, kRedBlocks, kT, N, (const double*)y, (const double*)wk.f,
-                 hist, gamma, wk.b, wk.V, wk.part, wk.sc, wk.ticket);
-      FOS_LAUNCH_CHECK();
+                 hist, gamma, wk.b, wk.V, wk.part);
+      if ((rc = reduce(2, wk.sc))) return rc;
       FOS_CUDA(cudaMemcpyAsync(hb, wk.sc, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
       FOS_CUDA(cudaMemcpyAsync(c->h_scal, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
       FOS_CUDA(cudaStreamSynchronize(c->stream));
@@ -538,12 +516,15 @@ struct Driver {
         // V^T w' (MODE 2) so the second pass needs no separate sweep over V for its
         // coefficients; otherwise it returns ||w'||^2 only (MODE 1).
         const bool fused = last_reorth;
-        if ((rc = mdot<true>(nv, wk.V, N, wj, wk.sc))) return rc;  // V^T w, ||w||^2
-        if (fused) {  // w -= V s2 h; V^T w, ||w||^2
-          if ((rc = update<2>(nv, wk.V, N, wk.sc, wj, d_sig2, wk.sc + kMaxVec))) return rc;
+        if ((rc = mdot<true>(nv, wk.V, N, wj))) return rc;              // V^T w, ||w||^2
+        if ((rc = reduce(nv + 1, wk.sc))) return rc;
+        if (fused) {
+          if ((rc = update<2>(nv, wk.V, N, wk.sc, wj, d_sig2))) return rc;  // w -= V s2 h; V^T w, ||w||^2
+          if ((rc = reduce(nv + 1, wk.sc + kMaxVec))) return rc;
           if ((rc = fetch(wk.sc, hbuf.data(), 2 * kMaxVec))) return rc;
-        } else {  // w -= V s2 h, ||w||^2
-          if ((rc = update<1>(nv, wk.V, N, wk.sc, wj, d_sig2, wk.sc + kMaxVec + nv))) return rc;
+        } else {
+          if ((rc = update<1>(nv, wk.V, N, wk.sc, wj, d_sig2))) return rc;  // w -= V s2 h, ||w||^2
+          if ((rc = reduce(1, wk.sc + kMaxVec + nv))) return rc;
           if ((rc = fetch(wk.sc, hbuf.data(), kMaxVec + nv + 1))) return rc;
         }
         double* col = &H[(size_t)(m + 1) * j];
@@ -552,9 +533,12 @@ struct Driver {
         last_reorth = hn2 < 0.5 * hbuf[nv];
         if (last_reorth) {
           const double* h2 = wk.sc + kMaxVec;  // V^T w' (device), from MODE 2 or a sweep
-          if (!fused)
-            if ((rc = mdot<false>(nv, wk.V, N, wj, wk.sc + kMaxVec))) return rc;
-          if ((rc = update<1>(nv, wk.V, N, h2, wj, d_sig2, wk.sc + 3 * kMaxVec))) return rc;
+          if (!fused) {
+            if ((rc = mdot<false>(nv, wk.V, N, wj))) return rc;
+            if ((rc = reduce(nv, wk.sc + kMaxVec))) return rc;
+          }
+          if ((rc = update<1>(nv, wk.V, N, h2, wj, d_sig2))) return rc;
+          if ((rc = reduce(1, wk.sc + 3 * kMaxVec))) return rc;
           if ((rc = fetch(wk.sc + kMaxVec, hbuf.data() + kMaxVec, 2 * kMaxVec + 1))) return rc;
           for (int l = 0; l < nv; l++) col[l] += sig[j] * sig[l] * hbuf[kMaxVec + l];
           hn2 = hbuf[3 * kMaxVec];
@@ -793,9 +777,8 @@ struct Adapt {
   }
   // ||a||_WRMS with weights from w
   int wrms(const double* a, const double* w, double rtol, double atol, double* out) {
-    fos_launch(c, k_wrms_part, kRedBlocks, kT, N, a, w, rtol, atol, wk.part, wk.sc + 5 * kMaxVec,
-               wk.ticket);
-    FOS_LAUNCH_CHECK();
+    fos_launch(c, k_wrms_part, kRedBlocks, kT, N, a, w, rtol, atol, wk.part);
+    if (int rc = dr.reduce(1, wk.sc + 5 * kMaxVec)) return rc;
     double h = 0.0;
     if (int rc = dr.fetch(wk.sc + 5 * kMaxVec, &h, 1)) return rc;
     *out = std::sqrt(h / (double)N);
