@@ -713,13 +713,10 @@ extern "C" int fos_bdf_run_host(fos_ctx* c, double t0, double* y, const fos_bdf_
   }
   Work* wk = nullptr;
   if (int rc = work_get(c, opts->maxl, &wk)) return rc;
-  const long N = 5L * c->nC;
-  FOS_CUDA(cudaMemcpyAsync(c->d_stage, y, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
-  if (int rc = fos_permute(c, c->d_stage, wk->yh, 0)) return rc;
+  if (int rc = fos_h2d_internal(c, y, wk->yh)) return rc;
   int rc = fos_bdf_run(c, t0, wk->yh, opts, stats);
   if (rc < 0) return rc;
-  if (int rc2 = fos_permute(c, wk->yh, c->d_stage, 1)) return rc2;
-  FOS_CUDA(cudaMemcpyAsync(y, c->d_stage, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream));
+  if (int rc2 = fos_d2h_reference(c, wk->yh, y)) return rc2;
   FOS_CUDA(cudaStreamSynchronize(c->stream));
   return rc;
 }

@@ -37,6 +37,10 @@ fos_ctx::~fos_ctx() {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h_scal) cudaFreeHost(h_scal);
+  for (cudaEvent_t e : ev_plane)
+    if (e) cudaEventDestroy(e);
+  if (ev_sync) cudaEventDestroy(ev_sync);
+  if (copy_stream) cudaStreamDestroy(copy_stream);
   fos_bdf_work_free(bdf);
   fos_ilut_destroy(ilut);
 }
@@ -373,19 +377,48 @@ extern "C" int fos_ctx_permute_dev(fos_ctx* c, const double* in, double* out, in
 
 // ------------------------------------------------------------------ host callbacks
 namespace {
-int h2d_internal(fos_ctx* c, const double* h, double* d_internal) {
-  FOS_CUDA(cudaMemcpyAsync(c->d_stage, h, sizeof(double) * 5 * (size_t)c->nC,
-                           cudaMemcpyHostToDevice, c->stream));
-  return fos_permute(c, c->d_stage, d_internal, 0);
-}
-int d2h_reference(fos_ctx* c, const double* d_internal, double* h) {
-  int rc = fos_permute(c, d_internal, c->d_stage, 1);
-  if (rc) return rc;
-  FOS_CUDA(cudaMemcpyAsync(h, c->d_stage, sizeof(double) * 5 * (size_t)c->nC,
-                           cudaMemcpyDeviceToHost, c->stream));
+int ensure_copy_stream(fos_ctx* c) {
+  if (c->copy_stream) return 0;
+  FOS_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+  for (cudaEvent_t& e : c->ev_plane)
+    FOS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  FOS_CUDA(cudaEventCreateWithFlags(&c->ev_sync, cudaEventDisableTiming));
   return 0;
 }
 }  // namespace
+
+// Five planes (one per conserved variable): the copy of plane q + 1 runs while plane q is
+// permuted, so only one plane's permutation is not hidden behind the copies.
+int fos_h2d_internal(fos_ctx* c, const double* h, double* d_internal) {
+  if (int rc = ensure_copy_stream(c)) return rc;
+  const size_t n = (size_t)c->nC;
+  // the staging buffer is free once the work queued so far on c->stream is done
+  FOS_CUDA(cudaEventRecord(c->ev_sync, c->stream));
+  FOS_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ev_sync, 0));
+  for (int q = 0; q < 5; q++) {
+    FOS_CUDA(cudaMemcpyAsync(c->d_stage + q * n, h + q * n, sizeof(double) * n,
+                             cudaMemcpyHostToDevice, c->copy_stream));
+    FOS_CUDA(cudaEventRecord(c->ev_plane[q], c->copy_stream));
+    FOS_CUDA(cudaStreamWaitEvent(c->stream, c->ev_plane[q], 0));
+    if (int rc = fos_permute_plane(c, c->d_stage, d_internal, 0, q)) return rc;
+  }
+  return 0;
+}
+int fos_d2h_reference(fos_ctx* c, const double* d_internal, double* h) {
+  if (int rc = ensure_copy_stream(c)) return rc;
+  const size_t n = (size_t)c->nC;
+  for (int q = 0; q < 5; q++) {
+    if (int rc = fos_permute_plane(c, d_internal, c->d_stage, 1, q)) return rc;
+    FOS_CUDA(cudaEventRecord(c->ev_plane[q], c->stream));
+    FOS_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ev_plane[q], 0));
+    FOS_CUDA(cudaMemcpyAsync(h + q * n, c->d_stage + q * n, sizeof(double) * n,
+                             cudaMemcpyDeviceToHost, c->copy_stream));
+  }
+  // later work on c->stream (and a synchronisation of it) comes after the copies
+  FOS_CUDA(cudaEventRecord(c->ev_sync, c->copy_stream));
+  FOS_CUDA(cudaStreamWaitEvent(c->stream, c->ev_sync, 0));
+  return 0;
+}
 
 extern "C" int fos_euler_rhs(double t, const double* y, double* ydot, void* user_data) {
   (void)t;
@@ -394,12 +427,12 @@ extern "C" int fos_euler_rhs(double t, const double* y, double* ydot, void* user
     fos_set_error("fos_euler_rhs: bad arguments");
     return -1;
   }
-  int rc = h2d_internal(c, y, c->d_y);
+  int rc = fos_h2d_internal(c, y, c->d_y);
   if (rc) return rc;
   FOS_CUDA(cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream));
   rc = fos_residual_launch(c, c->d_y, nullptr, nullptr, nullptr, c->d_f, 0.0, 0.0, 0);
   if (rc) return rc;
-  rc = d2h_reference(c, c->d_f, ydot);
+  rc = fos_d2h_reference(c, c->d_f, ydot);
   if (rc) return rc;
   int* hflag = (int*)c->h_scal;
   FOS_CUDA(cudaMemcpyAsync(hflag, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -440,7 +473,7 @@ extern "C" int fos_euler_pset(double t, const double* y, const double* fy, int j
     fos_set_error("fos_euler_pset: bad arguments");
     return -1;
   }
-  int rc = h2d_internal(c, y, c->d_y);
+  int rc = fos_h2d_internal(c, y, c->d_y);
   if (rc) return rc;
   rc = fos_euler_pset_dev(c, t, c->d_y, jok, jcur, gamma);
   if (rc) return rc;
@@ -456,11 +489,11 @@ extern "C" int fos_euler_psol(double t, const double* y, const double* fy, const
     fos_set_error("fos_euler_psol: bad arguments");
     return -1;
   }
-  int rc = h2d_internal(c, r, c->d_y);
+  int rc = fos_h2d_internal(c, r, c->d_y);
   if (rc) return rc;
   rc = fos_euler_psol_dev(c, c->d_y, c->d_z);
   if (rc) return rc;
-  rc = d2h_reference(c, c->d_z, z);
+  rc = fos_d2h_reference(c, c->d_z, z);
   if (rc) return rc;
   FOS_CUDA(cudaStreamSynchronize(c->stream));
   return 0;

@@ -39,6 +39,11 @@ void fos_bdf_work_free(fos_bdf_work* w);
 struct fos_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
+  // host <-> device state copies run plane by plane on their own stream, each overlapping
+  // the permutation of the plane before (created at the first host-buffer call)
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_plane[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev_sync = nullptr;
   int nC = 0, nE = 0, nPi = 0, nPb = 0, nP = 0, flags = 0;
   int nFi = 0, nFb = 0, nF = 0;  // internal faces: interior first, boundary after
   double gamm = 1.4, r = 1.0;
@@ -145,6 +150,13 @@ int fos_residual_launch(fos_ctx* c, const double* y, const double* v, const doub
 int fos_norm2_dev(fos_ctx* c, const double* x, long n, double* d_out_sq);
 int fos_sum_partials(fos_ctx* c, int np, double* d_out);  // sum of c->d_red[0..np) in order
 int fos_permute(fos_ctx* c, const double* in, double* out, int dir);
+// plane q (0..4) only: out + q nC from in + q nC
+int fos_permute_plane(fos_ctx* c, const double* in, double* out, int dir, int q);
+// host state (reference order) -> device d_internal, and back; the copies run plane by plane
+// on the copy stream, overlapped with the permutations on c->stream; d2h leaves c->stream
+// waiting for the last copy (synchronise c->stream before reading h)
+int fos_h2d_internal(fos_ctx* c, const double* h, double* d_internal);
+int fos_d2h_reference(fos_ctx* c, const double* d_internal, double* h);
 int fos_jv_sigma(fos_ctx* c, double* d_scal, double ynorm, double eps);
 int fos_prim_hl_launch(fos_ctx* c, const double* y);  // FP32 (hi, lo) primitives
 int fos_prim_launch(fos_ctx* c, const double* y);

@@ -435,10 +435,10 @@ __global__ void __launch_bounds__(kThreads) k_cell32(
   gather_epilogue(nC, c, acc, __ldg(invV + c), mode, vv, fy, d_s, a, b, out, flag);
 }
 
-__global__ void k_permute(int nC, const int* __restrict__ idx, const double* __restrict__ in,
-                          double* __restrict__ out) {
+__global__ void k_permute(int nC, int nplanes, const int* __restrict__ idx,
+                          const double* __restrict__ in, double* __restrict__ out) {
   const long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= 5L * nC) return;
+  if (k >= (long)nplanes * nC) return;
   const int q = (int)(k / nC), i = (int)(k - (long)q * nC);
   out[k] = in[(size_t)q * nC + idx[i]];
 }
@@ -566,7 +566,15 @@ int fos_jv_sigma(fos_ctx* c, double* d_scal, double ynorm, double eps) {
 
 int fos_permute(fos_ctx* c, const double* in, double* out, int dir) {
   const int* idx = dir == 0 ? c->d_new2old : c->d_old2new;
-  fos_launch(c, k_permute, nblk(5L * c->nC), kThreads, c->nC, idx, in, out);
+  fos_launch(c, k_permute, nblk(5L * c->nC), kThreads, c->nC, 5, idx, in, out);
+  FOS_LAUNCH_CHECK();
+  return 0;
+}
+
+int fos_permute_plane(fos_ctx* c, const double* in, double* out, int dir, int q) {
+  const int* idx = dir == 0 ? c->d_new2old : c->d_old2new;
+  const size_t off = (size_t)q * c->nC;
+  fos_launch(c, k_permute, nblk(c->nC), kThreads, c->nC, 1, idx, in + off, out + off);
   FOS_LAUNCH_CHECK();
   return 0;
 }

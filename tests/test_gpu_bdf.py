@@ -73,6 +73,22 @@ def test_bump_cfl5_matches_oracle(cuda):
     assert rel_err(y, y_ref) <= 1e-10
 
 
+@pytest.mark.parametrize("name,scale,precond,maxl", [("bump192", 24, 1, 5), ("sod16", 8, 0, 2)])
+def test_restarted_gmres_matches_oracle(cuda, name, scale, precond, maxl):
+    """GMRES(maxl) short enough that every solve restarts (the bump with ILU(0): about 35
+    Krylov iterations per Newton solve; Sod unpreconditioned: 3): the first cycle's unscaled
+    first vector, the correction kept for the restart residual, and the true-residual
+    restart, against the oracle at a Newton tolerance of 1e-11."""
+    c = Case(M.make_workload(name, scale=scale))
+    kw = dict(nsteps=2, newton_rtol=1e-11, maxl=maxl, max_restarts=40)
+    y_ref, st_ref = oracle_run(c, use_prec=precond, **kw)
+    y, st = gpu_run(c, precond=precond, **kw)
+    print("restarted", name, precond, maxl, st, st_ref)
+    assert st["n_lin_iters"] > maxl * st["n_newton"]  # solves restarted
+    assert st["n_jv"] > st["n_lin_iters"]  # restart residuals
+    assert rel_err(y, y_ref) <= 1e-10
+
+
 def test_unpreconditioned_matches_oracle(cuda):
     c = Case(M.make_workload("sod16", scale=8))
     y_ref, _ = oracle_run(c, nsteps=5, use_prec=0)
