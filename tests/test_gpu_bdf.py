@@ -9,7 +9,7 @@ import pytest
 
 from fosolvers_gb300 import mesh as M
 from fosolvers_gb300.euler import FLUX_FP32, ILU_COLOR, ILU_FP32
-from helpers import Case, field_errors, hex_workload, rel_err, with_all_conditions
+from helpers import Case, field_errors, hex_workload, perturbed, rel_err, with_all_conditions
 from oracle import pyoracle as O
 
 pytestmark = pytest.mark.gpu
@@ -87,6 +87,35 @@ def test_restarted_gmres_matches_oracle(cuda, name, scale, precond, maxl):
     assert st["n_lin_iters"] > maxl * st["n_newton"]  # solves restarted
     assert st["n_jv"] > st["n_lin_iters"]  # restart residuals
     assert rel_err(y, y_ref) <= 1e-10
+
+
+@pytest.mark.parametrize("pinned", [False, True])
+def test_host_buffer_entry_points_match_device(cuda, pinned):
+    """The host-buffer entry points on a pageable and on a page-locked array, copied plane
+    by plane on the copy stream with the permutations overlapped: fos_bdf_run_host equals
+    fos_bdf_run on the device bit for bit, and the rhs callback equals the one on a
+    pageable copy."""
+    import torch
+    c = Case(M.make_workload("sine96", scale=8, seed=1), flags=FLUX_FP32 | ILU_FP32 | ILU_COLOR)
+    y_dev, _ = gpu_run(c, nsteps=3)
+    keep = []  # the tensors that own the host buffers
+
+    def host(a):
+        t = torch.from_numpy(a.copy())
+        keep.append(t.pin_memory() if pinned else t)
+        return keep[-1].numpy()
+
+    yh = host(c.y0)
+    opts = c.gpu.bdf_defaults(order=c.wl.order, dt=c.wl.dt, nsteps=3, precond=1)
+    rc, st = c.gpu.bdf_run_host(yh, opts)
+    assert rc == 0, st
+    assert np.array_equal(yh, y_dev)
+    y1 = perturbed(c.y0, c.nC, 5)
+    f_ref = np.zeros_like(y1)
+    assert c.gpu.rhs(0.0, y1.copy(), f_ref) == 0
+    yin, fout = host(y1), host(np.zeros_like(y1))
+    assert c.gpu.rhs(0.0, yin, fout) == 0
+    assert np.array_equal(fout, f_ref)
 
 
 def test_unpreconditioned_matches_oracle(cuda):
