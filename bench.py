@@ -619,8 +619,8 @@ def main():
             cpu["residual_evals_per_s"] = cb["residual_evals_per_s_sample"] * cb["sample_cells"] / nC
         except Exception as exc:  # the baseline never blocks the GPU line
             cpu = {"value": None, "error": repr(exc)}
-    # the benchmark spec's absolute rates at the workload's cell count (device-resident, CUDA
-    # events): residual evaluations/s and Jv/s from the per-operation timing
+    # absolute rates at the workload's cell count (device-resident, CUDA events):
+    # residual evaluations/s and Jv/s from the per-operation timing
     thr = {"bdf_steps_per_s": value, "cells": nC}
     if roof and roof.get("per_op"):
         po = roof["per_op"]

@@ -1,5 +1,5 @@
 """numpy reference of the learned preconditioner (forward, loss, backward) -- TEST
-INFRASTRUCTURE ONLY, the checker for the GPU network kernels.
+INFRASTRUCTURE ONLY, the oracle the GPU network kernels are tested against.
 
 Same model and parameter layout as the library's network, with BF16 rounding at the
 same points: weights; h0, m and h after each layer.  Sums are in float32.  It runs in
