@@ -399,8 +399,9 @@ __device__ __forceinline__ bool inv5(T a[25]) {
 // A lane only touches its own row of row p's blocks and reads finished blocks of earlier
 // rows from global memory, so the lanes of a row need no synchronisation until the
 // diagonal inversion (warp shuffles).  The factor blocks are stored column-major (entry
-// (i, j) at 5 j + i): a load instruction of the sweeps then reads five consecutive floats
-// per block row instead of five floats 20 bytes apart.
+// (i, j) at 5 j + i), so each store instruction here (lane a writes entry (a, k)) and each
+// load instruction of the sweeps touches five consecutive floats per block row instead of
+// five floats 20 bytes apart.
 template <typename TF>
 __device__ __forceinline__ TF from64(double x) {
   if constexpr (sizeof(TF) == 4) return d2f_trunc(x); else return (TF)x;
@@ -591,8 +592,8 @@ __global__ void __launch_bounds__(kRedThreads) k_ilu_out_sq(int nC, const int* _
 
 // Triangular sweeps in position space, five lanes per block row (lane a owns component
 // a and reads row a of every 5x5 block, entries 5 apart in the column-major storage, so
-// the five lanes of a row read consecutive floats).  The forward sweep overwrites rv with y in place
-// (a row reads only its own rv and earlier rows' y).
+// the five lanes of a row read consecutive floats).  The forward sweep overwrites rv with
+// y in place (a row reads only its own rv and earlier rows' y).
 //   forward:  y_p = r_p - sum_{q in lower(p)} L_pq y_q           (unit block diagonal)
 //   backward: z_p = inv(D_p) (y_p - sum_{q in upper(p)} U_pq z_q)
 // z_p = inv(D_p) comp, comp = the row's five components gathered from its lanes; stored with
