@@ -80,6 +80,9 @@ def parse():
                     help="preconditioner set-up policy of every arm: 1 = pset each BDF step; "
                          "m > 1 = CVODE's (at most m steps between set-ups, or on a 30%% gamma "
                          "change or a Newton failure)")
+    ap.add_argument("--tight-rtol", type=float, default=1e-9,
+                    help="Newton tolerance of the untimed tightened-tolerance comparison of the "
+                         "arm with the FP64 path (0: skip)")
     ap.add_argument("--no-cvode", action="store_true",
                     help="skip the arms under CVODE's set-up policy (cvode_setup_policy)")
     ap.add_argument("--ilut", action="store_true",
@@ -296,64 +299,134 @@ def allmax(pg, x: float, device=None) -> float:
 
 
 # ------------------------------------------------------------------ CPU oracle baseline
-def cpu_oracle_sample(workload: str, steps: int, warmup: int, sample_scale: int = 32):
-    """The oracle (C restatement of the reference arithmetic, OpenMP on all host cores,
-    atomic-scatter pair loop like Euler.f90:84-154) running fixed-step BDF on a
-    sample of the same workload; BDF steps/s scaled to the full cell count."""
+# The oracle is the reference arithmetic restated in C (the Fortran reference cannot be built
+# here: no Fortran compiler), timed as the "tuned" build: the host's instruction set, like the
+# reference's own -march=native build, and OpenMP with the reference's structure -- the
+# residual's face loop in parallel with atomic scatter (Euler.f90:71-155), the Jacobian
+# assembly, SPARSKIT ilu0/lusol and the Krylov driver serial.
+def _oracle_context(wl, grid: dict, threads: int):
     from fosolvers_gb300 import mesh as M
-    from fosolvers_gb300.euler import PolyFvGrid
+    from oracle import pyoracle as O
+    O.set_default("tuned")
+    ibc = M.ibc_for(wl.mesh, wl.bc_gid)
+    return O.Euler(grid, ibc, wl.bc_type, wl.bc_param, wl.gamm, wl.r, wl.elem_state,
+                   threads=threads)
+
+
+def cpu_oracle_fullsize(wl, grid: dict, nsteps: int = 1, msbp: int = 1) -> dict:
+    """cpu_baseline of the GPU arm: the oracle on the same workload at its full size -- the
+    residual, Jv and ILU(0) apply rates (the ILU(0) factored once in the reference's natural
+    order) and `nsteps` whole BDF steps from the initial state (about 15-25 s of CPU work at
+    96^3 x 6 on a 16-core host)."""
+    from fosolvers_gb300 import mesh as M
     from oracle import pyoracle as O
     threads = os.cpu_count() or 1
-    wl = M.make_workload(workload, scale=sample_scale)
-    grid = PolyFvGrid.from_mesh(wl.mesh)
-    ibc = M.ibc_for(wl.mesh, wl.bc_gid)
-    e = O.Euler(grid.__dict__, ibc, wl.bc_type, wl.bc_param, wl.gamm, wl.r, wl.elem_state,
-                threads=threads)
-    y = M.soa(wl.elem_state, grid.nC)
-    rhs, pset, psol = e.callbacks()
-    if warmup:
-        yw = y.copy()
-        O.bdf_run(5 * grid.nC, rhs, pset, psol, e.h, yw,
-                  O.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=warmup))
-    t0 = time.perf_counter()
-    rc, st = O.bdf_run(5 * grid.nC, rhs, pset, psol, e.h, y,
-                       O.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=steps))
-    dt = time.perf_counter() - t0
-    # residual evaluations/s on the same sample
+    t_setup = time.perf_counter()
+    e = _oracle_context(wl, grid, threads)
+    nC = grid["nC"]
+    y = M.soa(wl.elem_state, nC)
     f = np.zeros_like(y)
-    t1 = time.perf_counter()
-    nrep = 5
-    for _ in range(nrep):
-        e.rhs(0.0, y, f)
-    trhs = (time.perf_counter() - t1) / nrep
+    gamma = wl.dt * (2.0 / 3.0 if wl.order == 2 else 1.0)
+    e.rhs(0.0, y, f)  # first touch of the work arrays
+    setup_s = time.perf_counter() - t_setup
+
+    def timed(fn, reps):
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        return (time.perf_counter() - t0) / reps
+
+    t_rhs = timed(lambda: e.rhs(0.0, y, f), 3)
+    v = np.random.default_rng(0).normal(size=y.size)
+    out = np.empty_like(y)
+    work = (np.empty_like(y), np.empty_like(y))
+    ynorm = float(np.linalg.norm(y))
+    eps = float(np.sqrt(np.finfo(np.float64).eps))
+    t_jv = timed(lambda: e.jv(y, f, v, out, 1.0, -gamma, ynorm, eps, work), 3)
+    t0 = time.perf_counter()
+    rc_p, _ = e.pset(0.0, y, f, 0, gamma)
+    t_pset = time.perf_counter() - t0
+    z = np.empty_like(y)
+    t_psol = timed(lambda: e.psol(0.0, None, None, v, z, gamma), 2)
+    rhs, pset, psol = e.callbacks()
+    yb = y.copy()
+    t0 = time.perf_counter()
+    rc, st = O.bdf_run(y.size, rhs, pset, psol, e.h, yb,
+                       O.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=nsteps, msbp=msbp))
+    t_bdf = time.perf_counter() - t0
     e.close()
-    full = FULL_CELLS if workload == "sine96" else None
-    scale = (full / grid.nC) if full else 1.0
-    per_step = dt / max(st["n_steps"], 1)
     return {
-        "value": 1.0 / (per_step * scale), "unit": UNIT, "cores": threads, "kind": "port",
-        "sample": (f"{st['n_steps']} BDF steps of the same workload at {sample_scale}^3 x 6 = "
-                   f"{grid.nC} tets ({per_step:.3f} s/step, {st['n_newton']} Newton, "
-                   f"{st['n_lin_iters']} Krylov iterations), scaled by the cell ratio "
-                   f"{scale:.1f} to {full or grid.nC} tets; OpenMP only in the residual loops "
-                   f"as in the reference, ILU(0)/Krylov serial"),
-        "residual_evals_per_s_sample": 1.0 / trhs, "sample_cells": grid.nC, "rc": rc,
+        "value": st["n_steps"] / t_bdf if rc == 0 else None, "unit": UNIT, "cores": threads,
+        "kind": "port",
+        "sample": (f"{st['n_steps']} whole BDF step(s) of the workload at its full size ({nC} "
+                   f"cells: {st['n_newton']} Newton, {st['n_lin_iters']} Krylov iterations, "
+                   f"{t_bdf:.2f} s) plus one residual, Jv, pset and ILU(0) apply timed "
+                   f"separately; the oracle built for this host's ISA, OpenMP in the residual "
+                   f"loops (atomic scatter as Euler.f90:71-155), the rest serial as in the "
+                   f"reference (no extrapolation)"),
+        "rc": rc, "setup_s": round(setup_s, 2),
+        "per_op": {"residual_evals_per_s": 1.0 / t_rhs, "jv_per_s": 1.0 / t_jv,
+                   "ilu_apply_per_s": 1.0 / t_psol, "pset_s": t_pset, "pset_rc": rc_p},
+        "oracle_lib": os.path.relpath(O.lib_path(), ROOT),
     }
 
 
 def run_reference(args, world, rank, pg):
+    """The reference arm: the oracle (the reference arithmetic restated in C, tuned build,
+    OpenMP residual loops on every host core) on the bench workload at its full size, from
+    the oracle's own grid construction (polyGrid%up + getNeibPolyFvGrid + sortPolyFvGrid
+    restated), through its CVODE-shaped callbacks and fixed-step BDF Newton--GMRES(30)
+    driver with SPARSKIT ilu0 in the reference's natural cell order: W untimed BDF steps,
+    then K timed BDF steps from the same initial state.  Nothing of the GPU library runs."""
     if rank != 0:
         return
-    cb = cpu_oracle_sample(args.workload, args.steps, args.warmup)
+    from fosolvers_gb300 import mesh as M
+    from oracle import pyoracle as O
+    threads = os.cpu_count() or 1
+    t_setup = time.perf_counter()
+    wl = M.make_workload(args.workload, scale=args.scale)
+    O.set_default("tuned")
+    grid = O.grid_build(wl.mesh)
+    e = _oracle_context(wl, grid, threads)
+    nC = grid["nC"]
+    y0 = M.soa(wl.elem_state, nC)
+    rhs, pset, psol = e.callbacks()
+    opts = lambda n: O.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=n, msbp=args.msbp)
+    setup_s = time.perf_counter() - t_setup
+    if args.warmup:
+        yw = y0.copy()
+        rc_w, _ = O.bdf_run(y0.size, rhs, pset, psol, e.h, yw, opts(args.warmup))
+        assert rc_w == 0, f"oracle warm-up failed: {rc_w}"
+    y = y0.copy()
+    t0 = time.perf_counter()
+    rc, st = O.bdf_run(y0.size, rhs, pset, psol, e.h, y, opts(args.steps))
+    dt = time.perf_counter() - t0
+    e.close()
+    assert rc == 0, f"oracle run failed: {rc} {st}"
+    value = args.steps / dt
+    size = "at its full size" if args.scale is None else f"at scale {args.scale}"
+    sample = (f"{args.steps} BDF steps of the workload {size} ({nC} cells) after "
+              f"{args.warmup} untimed ones, from the same initial state ({st['n_newton']} "
+              f"Newton, {st['n_lin_iters']} Krylov iterations, {dt:.1f} s); the oracle built "
+              f"for this host's ISA, OpenMP on {threads} threads in the residual loops "
+              f"(atomic scatter as Euler.f90:71-155), Jacobian, ilu0/lusol and Krylov serial "
+              f"as in the reference")
     line = {
-        "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / cb["value"],
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded mesh and state)",
-        "config": {"workload": workload_desc(args.workload), "runner": "CPU oracle (reference "
-                   "arithmetic restated in C; the Fortran reference cannot be compiled here)"},
-        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
-        "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "config": {"workload": workload_desc(args.workload) if args.scale is None else
+                   f"{args.workload} at scale {args.scale}", "cells": nC,
+                   "pset": "every BDF step" if args.msbp == 1 else f"CVODE policy, MSBP {args.msbp}",
+                   "runner": "CPU oracle (the reference arithmetic restated in C; the Fortran "
+                             "reference cannot be compiled here)",
+                   "oracle_lib": os.path.relpath(O.lib_path(), ROOT),
+                   "setup_s": round(setup_s, 2)},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "stats": st,
     }
     print(json.dumps(line), flush=True)
 
@@ -415,6 +488,12 @@ def field_rel_err(a, b, nC):
          float((a[1:4] - b[1:4]).norm(dim=0).max() / b[1:4].norm(dim=0).max()),
          float((a[4] - b[4]).abs().max() / b[4].abs().max())]
     return max(e)
+
+
+def cell_rel_err(a, b, nC):
+    """largest per-cell relative error ||a_c - b_c|| / ||b_c|| over the 5 conserved values."""
+    a, b = a.reshape(5, nC), b.reshape(5, nC)
+    return float(((a - b).norm(dim=0) / b.norm(dim=0)).max())
 
 
 def main():
@@ -530,7 +609,10 @@ def main():
 
         R = args.op_reps
         t_rhs = timeit(lambda: ctx.rhs_dev(0.0, y, f), 3 * R)
-        t_jv = timeit(lambda: ctx.jv_dev(0.0, y, f, v, out, 1.0, -gamma, ynorm), 3 * R)
+        # Jv as the Krylov driver calls it: ||v|| known from the preconditioner's output pass
+        vnorm = float(torch.linalg.norm(v))
+        t_jv = timeit(lambda: ctx.jv_dev_vnorm(0.0, y, f, v, out, 1.0, -gamma, ynorm, vnorm),
+                      3 * R)
         t_pset = timeit(lambda: ctx.pset_dev(0.0, y, 0, gamma), max(2, R // 2))
         t_psol = timeit(lambda: ctx.psol_dev(v, out), R)
         lev = info["nlev_fwd"] + info["nlev_bwd"]
@@ -560,6 +642,16 @@ def main():
     info = ctx.info()
     y_out = torch.empty_like(y)
     ctx.to_reference(y, y_out)
+    # the same K steps of this arm at a tightened Newton tolerance (untimed): the state
+    # difference from the FP64 path at the same tolerance shows how much of the difference at
+    # the workload's 1e-8 is the Newton tolerance rather than the arithmetic
+    y_tight = None
+    if args.tight_rtol > 0 and args.mode != "fp64" and not args.no_compare:
+        yt = y0.clone()
+        rc_t, st_t = ctx.bdf_run(yt, mk(args.steps, newton_rtol=args.tight_rtol, max_newton=20))
+        if rc_t == 0:
+            y_tight = torch.empty_like(yt)
+            ctx.to_reference(yt, y_tight)
     ctx.close()
 
     # the plain FP64 ILU(0)-GMRES path on the same mesh and state: the target's denominator
@@ -568,8 +660,8 @@ def main():
         ctx64 = make_ctx(grid, ibc, wl, "fp64", args.ilu_order, stream)
         y064 = torch.empty_like(y0_ref)
         ctx64.to_internal(y0_ref, y064)
-        mk64 = lambda n, **kw: ctx64.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=n, precond=1,
-                                                  msbp=args.msbp, **kw)
+        mk64 = lambda n, **kw: ctx64.bdf_defaults(**{**dict(order=wl.order, dt=wl.dt, nsteps=n,
+                                                            precond=1, msbp=args.msbp), **kw})
         ms64, st64, _, _, y64 = timed_bdf(ctx64, y064, mk64, args, dev, stream, pg)
         v64 = world * args.steps / (allmax(pg, ms64, dev) / 1000.0)
         yb = torch.empty_like(y)
@@ -580,6 +672,34 @@ def main():
                 # error reflects that tolerance at 26.5M unknowns, the l2 error the precision
                 "state_rel_err_vs_fp64": field_rel_err(y_out, yb, nC),
                 "state_rel_l2_vs_fp64": float((y_out - yb).norm() / yb.norm())}
+        vs64["state_cell_rel_err_vs_fp64"] = cell_rel_err(y_out, yb, nC)
+        # yardstick: the FP64 flux with the learned preconditioner, i.e. the FP64 path's own
+        # arithmetic on another Krylov path, against the FP64 ILU(0) path -- the difference
+        # the Newton tolerance alone allows between two FP64 runs
+        if gnn is not None:
+            ctx64.attach_gnn(gnn)
+            yl = y064.clone()
+            rc_l, _ = ctx64.bdf_run(yl, mk64(args.steps, precond=2))
+            ctx64.attach_gnn(None)
+            if rc_l == 0:
+                ylb = torch.empty_like(yl)
+                ctx64.to_reference(yl, ylb)
+                vs64["fp64_learned_vs_fp64"] = {
+                    "state_rel_err": field_rel_err(ylb, yb, nC),
+                    "state_cell_rel_err": cell_rel_err(ylb, yb, nC),
+                    "state_rel_l2": float((ylb - yb).norm() / yb.norm())}
+        if y_tight is not None:
+            yt64 = y064.clone()
+            rc_t, _ = ctx64.bdf_run(yt64, mk64(args.steps, newton_rtol=args.tight_rtol,
+                                               max_newton=20))
+            if rc_t == 0:
+                ytb = torch.empty_like(yt64)
+                ctx64.to_reference(yt64, ytb)
+                vs64["tight_newton_rtol"] = {
+                    "newton_rtol": args.tight_rtol,
+                    "state_rel_err_vs_fp64": field_rel_err(y_tight, ytb, nC),
+                    "state_cell_rel_err_vs_fp64": cell_rel_err(y_tight, ytb, nC),
+                    "state_rel_l2_vs_fp64": float((y_tight - ytb).norm() / ytb.norm())}
         if cvode is not None:
             mk64c = lambda n, **kw: ctx64.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=n,
                                                        precond=1, msbp=20, **kw)
@@ -613,10 +733,9 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         try:
-            cb = cpu_oracle_sample(args.workload, 2, 0)
-            cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
-            cpu["residual_evals_per_s_sample"] = cb["residual_evals_per_s_sample"]
-            cpu["residual_evals_per_s"] = cb["residual_evals_per_s_sample"] * cb["sample_cells"] / nC
+            cb = cpu_oracle_fullsize(wl, grid.__dict__, nsteps=1, msbp=args.msbp)
+            cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "per_op",
+                                      "oracle_lib")}
         except Exception as exc:  # the baseline never blocks the GPU line
             cpu = {"value": None, "error": repr(exc)}
     # absolute rates at the workload's cell count (device-resident, CUDA events):
@@ -628,8 +747,11 @@ def main():
             thr["residual_evals_per_s"] = round(1e3 / po["residual"]["ms"], 1)
         if "jv" in po:
             thr["jv_per_s"] = round(1e3 / po["jv"]["ms"], 1)
-    if cpu and cpu.get("residual_evals_per_s"):
-        thr["cpu_residual_evals_per_s"] = round(cpu["residual_evals_per_s"], 2)
+        if "ilu_apply" in po:
+            thr["ilu_apply_per_s"] = round(1e3 / po["ilu_apply"]["ms"], 1)
+    if cpu and cpu.get("per_op"):
+        thr["cpu"] = {k: (round(v, 3) if isinstance(v, float) else v)
+                      for k, v in cpu["per_op"].items()}
 
     if rank == 0:
         line = {

@@ -77,6 +77,8 @@ _SIGS = {
     "fos_euler_rhs_dev_static": (C.c_int, [_vp, C.c_double, _vp, _vp]),
     "fos_euler_jv_dev": (C.c_int, [_vp, C.c_double, _vp, _vp, _vp, _vp, C.c_double, C.c_double,
                                    C.c_double, C.c_double]),
+    "fos_euler_jv_dev_vnorm": (C.c_int, [_vp, C.c_double, _vp, _vp, _vp, _vp, C.c_double,
+                                         C.c_double, C.c_double, C.c_double, C.c_double]),
     "fos_euler_pset_dev": (C.c_int, [_vp, C.c_double, _vp, C.c_int, _ip, C.c_double]),
     "fos_euler_psol_dev": (C.c_int, [_vp, _vp, _vp]),
     "fos_euler_jac_copy": (C.c_long, [_vp, _ip, _ip, _dp]),

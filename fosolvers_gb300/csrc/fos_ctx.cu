@@ -465,6 +465,19 @@ extern "C" int fos_euler_jv_dev(fos_ctx* c, double t, const double* y, const dou
   return fos_residual_launch(c, y, v, c->d_scal + 1, fy, out, a, b, 1);
 }
 
+extern "C" int fos_euler_jv_dev_vnorm(fos_ctx* c, double t, const double* y, const double* fy,
+                                      const double* v, double* out, double a, double b,
+                                      double ynorm, double vnorm, double eps) {
+  (void)t;
+  if (!c || !y || !fy || !v || !out || !(vnorm >= 0.0)) {
+    fos_set_error("fos_euler_jv_dev_vnorm: bad arguments");
+    return -1;
+  }
+  int rc = fos_jv_sigma_known(c, c->d_scal, ynorm, vnorm, eps);
+  if (rc) return rc;
+  return fos_residual_launch(c, y, v, c->d_scal + 1, fy, out, a, b, 1);
+}
+
 extern "C" int fos_euler_pset(double t, const double* y, const double* fy, int jok, int* jcur,
                               double gamma, void* user_data) {
   (void)fy;

@@ -158,6 +158,7 @@ int fos_permute_plane(fos_ctx* c, const double* in, double* out, int dir, int q)
 int fos_h2d_internal(fos_ctx* c, const double* h, double* d_internal);
 int fos_d2h_reference(fos_ctx* c, const double* d_internal, double* h);
 int fos_jv_sigma(fos_ctx* c, double* d_scal, double ynorm, double eps);
+int fos_jv_sigma_known(fos_ctx* c, double* d_scal, double ynorm, double vnorm, double eps);
 int fos_prim_hl_launch(fos_ctx* c, const double* y);  // FP32 (hi, lo) primitives
 int fos_prim_launch(fos_ctx* c, const double* y);
 int fos_gnn_precond(fos_ctx* c, const double* y, const double* r, double gamma, double* z);

@@ -488,6 +488,14 @@ __global__ void k_sigma(double* scal, double ynorm, double eps) {
   scal[2] = s > 0.0 ? 1.0 / s : 0.0;
 }
 
+// the same with ||v||_2 supplied by the caller (no reduction pass over v)
+__global__ void k_sigma_known(double* scal, double ynorm, double vnorm, double eps) {
+  const double s = vnorm > 0.0 ? eps * (1.0 + ynorm) / vnorm : 0.0;
+  scal[0] = vnorm * vnorm;
+  scal[1] = s;
+  scal[2] = s > 0.0 ? 1.0 / s : 0.0;
+}
+
 inline int nblk(long n, int t = kThreads) { return (int)((n + t - 1) / t); }
 
 }  // namespace
@@ -560,6 +568,12 @@ int fos_sum_partials(fos_ctx* c, int np, double* d_out) {
 
 int fos_jv_sigma(fos_ctx* c, double* d_scal, double ynorm, double eps) {
   fos_launch(c, k_sigma, 1, 1, d_scal, ynorm, eps);
+  FOS_LAUNCH_CHECK();
+  return 0;
+}
+
+int fos_jv_sigma_known(fos_ctx* c, double* d_scal, double ynorm, double vnorm, double eps) {
+  fos_launch(c, k_sigma_known, 1, 1, d_scal, ynorm, vnorm, eps);
   FOS_LAUNCH_CHECK();
   return 0;
 }

@@ -190,6 +190,17 @@ class FOEuler:
                                                  v_dev.data_ptr(), out_dev.data_ptr(), a, b,
                                                  ynorm, eps), "jv_dev")
 
+    def jv_dev_vnorm(self, t, y_dev, fy_dev, v_dev, out_dev, a, b, ynorm, vnorm,
+                     eps=0.0) -> int:
+        """jv_dev with ||v||_2 known to the caller (no reduction pass over v)."""
+        if eps <= 0.0:
+            eps = float(np.sqrt(np.finfo(np.float32).eps)) if self.flags & FLUX_FP32 \
+                else float(np.sqrt(np.finfo(np.float64).eps))
+        return check(_lib.lib().fos_euler_jv_dev_vnorm(self._h, t, y_dev.data_ptr(),
+                                                       fy_dev.data_ptr(), v_dev.data_ptr(),
+                                                       out_dev.data_ptr(), a, b, ynorm, vnorm,
+                                                       eps), "jv_dev_vnorm")
+
     def pset_dev(self, t, y_dev, jok, gamma):
         jcur = C.c_int(0)
         rc = _lib.lib().fos_euler_pset_dev(self._h, t, y_dev.data_ptr(), jok, C.byref(jcur), gamma)

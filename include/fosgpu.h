@@ -136,6 +136,13 @@ int fos_euler_rhs_dev_static(const fos_ctx* ctx, double t, const double* y, doub
  * a = 1, b = -gamma gives J_G v; a = 0, b = 1 gives J_f v. */
 int fos_euler_jv_dev(fos_ctx* ctx, double t, const double* y, const double* fy, const double* v,
                      double* out, double a, double b, double ynorm, double eps);
+/* The same product with ||v||_2 = vnorm supplied by the caller, as a Krylov method that
+ * keeps its basis norms has it (CVODE's SPGMR passes unit basis vectors to the difference
+ * quotient, and this library's driver takes ||v||^2 from the preconditioner's output pass):
+ * no reduction pass over v.  vnorm = 0 gives out = a*v. */
+int fos_euler_jv_dev_vnorm(fos_ctx* ctx, double t, const double* y, const double* fy,
+                           const double* v, double* out, double a, double b, double ynorm,
+                           double vnorm, double eps);
 int fos_euler_pset_dev(fos_ctx* ctx, double t, const double* y, int jok, int* jcur,
                        double gamma);
 int fos_euler_psol_dev(fos_ctx* ctx, const double* r, double* z);

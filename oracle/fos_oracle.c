@@ -1272,6 +1272,19 @@ static int nk_matvec(nk_op* op, const double* v, double* out) {
   for (int i = 0; i < n; i++) out[i] = op->a_coef * v[i] + op->b_coef * ((op->ftmp[i] - op->fy[i]) / s);
   return rc;
 }
+/* The driver's finite-difference Jv as one call (CPU per-operation timing and tests):
+ * out = a v + b (f(y + s v) - fy)/s, s = eps (1 + ynorm)/||v||; ytmp, ftmp: n doubles */
+int o_jv(int n, o_rhs_fn f, void* ud, double t, const double* y, const double* fy,
+         const double* v, double* out, double a, double b, double ynorm, double eps,
+         double* ytmp, double* ftmp) {
+  o_bdf_stats st;
+  memset(&st, 0, sizeof st);
+  nk_op op;
+  memset(&op, 0, sizeof op);
+  op.n = n; op.f = f; op.ud = ud; op.t = t; op.a_coef = a; op.b_coef = b; op.ynorm = ynorm;
+  op.eps = eps; op.y = y; op.fy = fy; op.ytmp = ytmp; op.ftmp = ftmp; op.st = &st;
+  return nk_matvec(&op, v, out);
+}
 static int nk_prec(nk_op* op, const double* r, double* z, double delta) {
   if (!op->use_prec) {
     memcpy(z, r, sizeof(double) * op->n);

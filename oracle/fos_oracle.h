@@ -137,6 +137,11 @@ typedef struct {
   double last_gnorm;
 } o_bdf_stats;
 void o_bdf_defaults(o_bdf_opts* o);
+/* the driver's finite-difference Jv: out = a v + b (f(y + s v) - fy)/s,
+ * s = eps (1 + ynorm)/||v||_2; ytmp and ftmp are n-double work arrays */
+int o_jv(int n, o_rhs_fn f, void* ud, double t, const double* y, const double* fy,
+         const double* v, double* out, double a, double b, double ynorm, double eps,
+         double* ytmp, double* ftmp);
 /* fixed-step BDF1/BDF2 Newton--GMRES(maxl) with right preconditioning, CGS + DGKS Arnoldi.
  * y in/out (length n). returns 0 on success, >0 if a step failed to converge. */
 int o_bdf_run(int n, o_rhs_fn rhs, o_pset_fn pset, o_psol_fn psol, void* ud, double t0,

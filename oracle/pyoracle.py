@@ -90,6 +90,8 @@ _SIGS = {
     "o_ilut": (C.c_int, [C.c_int, _dp, _ip, _ip, C.c_int, C.c_double, _dp, _ip, _ip, C.c_int,
                          _dp, _ip]),
     "o_bdf_defaults": (None, [C.POINTER(BdfOpts)]),
+    "o_jv": (C.c_int, [C.c_int, _vp, _vp, C.c_double, _dp, _dp, _dp, _dp, C.c_double,
+                       C.c_double, C.c_double, C.c_double, _dp, _dp]),
     "o_bdf_run": (C.c_int, [C.c_int, _vp, _vp, _vp, _vp, C.c_double, _dp, C.POINTER(BdfOpts),
                             C.POINTER(BdfStats)]),
     "o_newton_solve": (C.c_int, [C.c_int, _vp, _vp, _dp, C.c_double, C.c_double, C.c_int, C.c_int,
@@ -100,20 +102,35 @@ _SIGS = {
                                  C.POINTER(AdaptStats)]),
 }
 
-_lib = None
+_libs: dict = {}
+_default = "checker"
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        path = _build.build()
+def lib(variant: str | None = None):
+    """The oracle library: "checker" (portable build, the default) or "tuned" (the same
+    source built for the host's instruction set, for CPU timing; bit-identical results)."""
+    v = variant or _default
+    if v not in _libs:
+        path = _build.build() if v == "checker" else _build.build_tuned()
         l = C.CDLL(str(path))
         for name, (res, args) in _SIGS.items():
             f = getattr(l, name)
             f.restype = res
             f.argtypes = args
-        _lib = l
-    return _lib
+        _libs[v] = l
+    return _libs[v]
+
+
+def set_default(variant: str) -> None:
+    """Library used by every later call that names none ("checker" or "tuned")."""
+    global _default
+    if variant not in ("checker", "tuned"):
+        raise ValueError(variant)
+    _default = variant
+
+
+def lib_path(variant: str | None = None) -> str:
+    return lib(variant)._name
 
 
 def dp(a):
@@ -146,9 +163,9 @@ def lusol(n, y, alu, jlu, ju):
     return x
 
 
-def grid_build(mesh) -> dict:
+def grid_build(mesh, variant=None) -> dict:
     """Reference face construction (polyGrid%up + getNeib + sort) on a Mesh."""
-    L = lib()
+    L = lib(variant)
     pN = np.ascontiguousarray(mesh.pN, np.float64)
     iNE = np.ascontiguousarray(mesh.iNE, np.int32)
     g = L.og_grid_build(mesh.nN, dp(pN), mesh.nE, iNE.shape[1],
@@ -173,8 +190,9 @@ def grid_build(mesh) -> dict:
 class Euler:
     """oe_ctx: the reference foeuler module state restated on the CPU."""
 
-    def __init__(self, grid, iBC, bc_type, bc_param, gamm, r, elem_state, threads=1):
-        L = lib()
+    def __init__(self, grid, iBC, bc_type, bc_param, gamm, r, elem_state, threads=1,
+                 variant=None):
+        self.L = L = lib(variant)
         self.nC, self.nE = grid["nC"] if isinstance(grid, dict) else grid.nC, \
             grid["nE"] if isinstance(grid, dict) else grid.nE
         gg = grid if isinstance(grid, dict) else grid.__dict__
@@ -196,25 +214,25 @@ class Euler:
         self.set_threads(threads)
 
     def set_threads(self, n):
-        lib().oe_set_threads(self.h, int(n))
+        self.L.oe_set_threads(self.h, int(n))
 
     def set_ilu_order(self, old2new):
         """ILU(0) cell order (old -> new, 0-based); None = natural reference order."""
         if old2new is None:
-            lib().oe_set_ilu_order(self.h, None)
+            self.L.oe_set_ilu_order(self.h, None)
         else:
             self._perm = np.ascontiguousarray(old2new, np.int32)
-            lib().oe_set_ilu_order(self.h, ip(self._perm))
+            self.L.oe_set_ilu_order(self.h, ip(self._perm))
 
     def set_ilut(self, lfil=50, droptol=1e-6):
         """pset/psol with ILUT (the ILU class of numerics/sparse.f90) instead of ilu0;
         lfil=None goes back to ilu0."""
-        lib().oe_set_ilut(self.h, -1 if lfil is None else int(lfil), float(droptol))
+        self.L.oe_set_ilut(self.h, -1 if lfil is None else int(lfil), float(droptol))
 
     def ilut_factors(self):
         """(alu, jlu, ju) of the last ILUT factorisation, MSR arrays trimmed to their use."""
         alu, jlu, ju = _dp(), _ip(), _ip()
-        iwk = lib().oe_ilut_factors(self.h, C.byref(alu), C.byref(jlu), C.byref(ju))
+        iwk = self.L.oe_ilut_factors(self.h, C.byref(alu), C.byref(jlu), C.byref(ju))
         if iwk < 0:
             raise RuntimeError("no ILUT set")
         n = 5 * self.nC
@@ -225,7 +243,7 @@ class Euler:
 
     def close(self):
         if self.h:
-            lib().oe_free(self.h)
+            self.L.oe_free(self.h)
             self.h = None
 
     def __del__(self):
@@ -235,19 +253,19 @@ class Euler:
             pass
 
     def rhs(self, t, y, ydot):
-        return lib().oe_rhs(t, dp(y), dp(ydot), self.h)
+        return self.L.oe_rhs(t, dp(y), dp(ydot), self.h)
 
     def pset(self, t, y, fy, jok, gamma):
         jc = C.c_int(0)
-        rc = lib().oe_pset(t, dp(y), dp(fy) if fy is not None else None, jok, C.byref(jc), gamma,
+        rc = self.L.oe_pset(t, dp(y), dp(fy) if fy is not None else None, jok, C.byref(jc), gamma,
                            self.h)
         return rc, jc.value
 
     def psol(self, t, y, fy, r, z, gamma, delta=0.0, lr=1):
-        return lib().oe_psol(t, None, None, dp(r), dp(z), gamma, delta, lr, self.h)
+        return self.L.oe_psol(t, None, None, dp(r), dp(z), gamma, delta, lr, self.h)
 
     def jac(self, y, maxFace):
-        ptr = lib().oe_jac(self.h, dp(y))
+        ptr = self.L.oe_jac(self.h, dp(y))
         n = 5 * (5 * maxFace + 5) * self.nC
         a = np.ctypeslib.as_array(ptr, shape=(n,)).copy()
         # Fortran JacC(5, 5*(maxFace+1), nC) column-major -> [cell, block col, row]
@@ -255,7 +273,7 @@ class Euler:
 
     def pmat(self):
         a, ja, ia = _dp(), _ip(), _ip()
-        nnz = lib().oe_pmat(self.h, C.byref(a), C.byref(ja), C.byref(ia))
+        nnz = self.L.oe_pmat(self.h, C.byref(a), C.byref(ja), C.byref(ia))
         n = 5 * self.nC
         return (np.ctypeslib.as_array(a, shape=(nnz,)).copy(),
                 np.ctypeslib.as_array(ja, shape=(nnz,)).copy(),
@@ -265,11 +283,18 @@ class Euler:
         rho = np.zeros(self.nE)
         rhou = np.zeros(3 * self.nE)
         rE = np.zeros(self.nE)
-        lib().oe_elem_state(self.h, dp(rho), dp(rhou), dp(rE))
+        self.L.oe_elem_state(self.h, dp(rho), dp(rhou), dp(rE))
         return rho, rhou.reshape(-1, 3), rE
 
+    def jv(self, y, fy, v, out, a, b, ynorm, eps, work=None):
+        """The oracle driver's finite-difference Jv (o_jv) through this context's rhs."""
+        if work is None:
+            work = (np.empty_like(y), np.empty_like(y))
+        return self.L.o_jv(y.size, C.cast(self.L.oe_rhs, _vp), self.h, 0.0, dp(y), dp(fy), dp(v),
+                           dp(out), a, b, ynorm, eps, dp(work[0]), dp(work[1]))
+
     def callbacks(self):
-        L = lib()
+        L = self.L
         return (C.cast(L.oe_rhs, _vp), C.cast(L.oe_pset, _vp), C.cast(L.oe_psol, _vp))
 
 
@@ -281,11 +306,11 @@ def bdf_defaults(**kw) -> BdfOpts:
     return o
 
 
-def bdf_run(n, rhs, pset, psol, ud, y, opts, t0=0.0):
+def bdf_run(n, rhs, pset, psol, ud, y, opts, t0=0.0, variant=None):
     """rhs/pset/psol: raw C function pointers (c_void_p) or ctypes CFUNCTYPE objects."""
     st = BdfStats()
     as_vp = lambda f: f if isinstance(f, (C.c_void_p, int)) or f is None else C.cast(f, _vp)
-    rc = lib().o_bdf_run(n, as_vp(rhs), as_vp(pset), as_vp(psol), ud, t0, dp(y), C.byref(opts),
+    rc = lib(variant).o_bdf_run(n, as_vp(rhs), as_vp(pset), as_vp(psol), ud, t0, dp(y), C.byref(opts),
                          C.byref(st))
     return rc, st.as_dict()
 

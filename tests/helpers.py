@@ -108,3 +108,17 @@ def field_errors(a: np.ndarray, b: np.ndarray) -> dict:
             "rhou": float(np.abs(a[1:4] - b[1:4]).max() / max(mom, 1e-300)),
             "rhoE": float(np.abs(a[4] - b[4]).max() / np.abs(b[4]).max()),
             "per_component": [float(np.abs(a[q] - b[q]).max()) for q in range(5)]}
+
+
+def cell_errors(a: np.ndarray, b: np.ndarray) -> dict:
+    """Per-cell relative errors: the largest ||a_c - b_c|| / ||b_c|| over cells (the 5-vector
+    of conserved variables of cell c), and per field the largest |a - b| / |b| of density and
+    energy (bounded away from zero; momentum components cross zero, so momentum enters
+    through the cell vector only)."""
+    a = a.reshape(5, -1)
+    b = b.reshape(5, -1)
+    nb = np.sqrt((b ** 2).sum(0))
+    nd = np.sqrt(((a - b) ** 2).sum(0))
+    return {"cell": float((nd / nb).max()),
+            "rho": float((np.abs(a[0] - b[0]) / np.abs(b[0])).max()),
+            "rhoE": float((np.abs(a[4] - b[4]) / np.abs(b[4])).max())}

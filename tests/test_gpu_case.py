@@ -83,3 +83,54 @@ def test_adaptive_case_matches_oracle(cuda, tmp_path):
     print("adaptive case", res["steps"], n_acc, rel_err(res["y"], y_ref))
     assert res["steps"] == n_acc
     assert rel_err(res["y"], y_ref) <= 1e-9
+
+
+def _duct_case(tmp_path, t_final, t_int):
+    """The reference's examples/foeuler/duct case directory (mesh, bc, ic and fl as the
+    reference ships them, from tests/golden/duct.npz) with the run control shortened."""
+    from test_meshio import write_duct_case
+    case = write_duct_case(tmp_path / "duct")
+    (case / "sim").write_text(f"{t_final!r}  # final time [s]\n{t_int!r}  # output interval [s]\n")
+    return case
+
+
+def test_duct_example_fixed_steps_match_oracle(cuda, tmp_path):
+    """examples/foeuler/duct (65,483 tetrahedra; total-pressure inflow, code 11, on group 5;
+    static-pressure outflow, code 20, on group 3; walls elsewhere; SI units, R = 287.058):
+    six BDF2 steps at CFL 5 on the initial state with GMRES(30) + ILU(0) in FP64, written as
+    rst_<k>.vtk every three steps; the state must match the oracle's within 1e-10 and the
+    files must carry it."""
+    from fosolvers_gb300.case import load_case
+    ci = load_case(_duct_case(tmp_path, 1.0, 1.0))
+    c_snd = np.sqrt(ci.gamm * ci.r * ci.ic["T0"])
+    from fosolvers_gb300.euler import PolyFvGrid
+    dt = 5.0 * float(np.cbrt(PolyFvGrid.from_mesh(ci.mesh).v).min()) / c_snd
+    case = _duct_case(tmp_path, 6 * dt, 3 * dt)
+    out = tmp_path / "out"
+    res = run_case(case, out, dt=dt, order=2, log=lambda s: None)
+    assert res["steps"] == 6 and res["outputs"] == 2 and res["cells"] == 65483
+
+    wl = workload_from_case(case, dt=dt, order=2, nsteps=6)
+    c = Case(wl)
+    c.match_ilu_order()
+    rhs, pset, psol = c.oracle.callbacks()
+    y_ref = c.y0.copy()
+    rc, st = O.bdf_run(c.N, rhs, pset, psol, c.oracle.h, y_ref,
+                       O.bdf_defaults(order=2, dt=dt, nsteps=6, use_prec=1))
+    assert rc == 0, st
+    err = rel_err(res["y"], y_ref)
+    print("duct parity", dt, err, res["stats"], st)
+    assert err <= 1e-10
+    nC = c.nC
+    # the inflow drives the gas: momentum appears and the pressure leaves its initial value
+    rho, u, p, T = primitives(res["y"], nC, wl.r, wl.gamm)
+    assert np.abs(u).max() > 1e-3 and p.max() > 0.9e5
+    for k in range(3):
+        assert (out / f"rst_{k}.vtk").exists()
+    mesh_out, data = read_vtk(out / "rst_2.vtk")
+    assert mesh_out.nE == wl.mesh.nE
+    np.testing.assert_array_equal(data["cell"]["density"][:nC], rho)
+    np.testing.assert_array_equal(data["cell"]["velocity"][:nC], u)
+    np.testing.assert_array_equal(data["cell"]["pressure"][:nC], p)
+    np.testing.assert_array_equal(data["cell"]["temperature"][:nC], T)
+

@@ -263,3 +263,32 @@ def test_anfj_is_abs_of_nfj(seed):
     expect = absA.real.copy()
     expect[1:4, 0] -= abs(u @ n) * u
     assert np.abs(_anfj(n, u, H, c, g) - expect).max() <= 1e-10 * np.abs(absA).max()
+
+
+def test_tuned_build_is_bit_identical():
+    """The CPU baseline times the oracle built for the host's instruction set; with
+    multiply-add contraction off in both builds it must compute exactly what the checker
+    computes: residual, grid, and two BDF2 steps with ILU(0) (single thread, so the
+    summation order is fixed)."""
+    from fosolvers_gb300 import mesh as M
+    wl = M.make_workload("sine96", scale=6, seed=1)
+    grids = [O.grid_build(wl.mesh, variant=v) for v in ("checker", "tuned")]
+    for k in ("iEP", "aP", "normP", "v", "neib"):
+        assert np.array_equal(grids[0][k], grids[1][k]), k
+    ibc = M.ibc_for(wl.mesh, wl.bc_gid)
+    out = []
+    for v in ("checker", "tuned"):
+        e = O.Euler(grids[0], ibc, wl.bc_type, wl.bc_param, wl.gamm, wl.r, wl.elem_state,
+                    variant=v)
+        y = M.soa(wl.elem_state, grids[0]["nC"])
+        f = np.zeros_like(y)
+        assert e.rhs(0.0, y, f) == 0
+        rhs, pset, psol = e.callbacks()
+        rc, st = O.bdf_run(y.size, rhs, pset, psol, e.h, y,
+                           O.bdf_defaults(order=2, dt=wl.dt, nsteps=2), variant=v)
+        assert rc == 0
+        out.append((f, y, st))
+        e.close()
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2]

@@ -52,7 +52,8 @@ def test_two_replicas_take_the_slowest_time(tmp_path):
 def test_reference_arm_under_torchrun_prints_one_line():
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2",
            "--master-addr", "127.0.0.1", "--master-port", str(free_port()), str(ROOT / "bench.py"),
-           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0"]
+           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0",
+           "--scale", "8"]
     env = dict(os.environ, OMP_NUM_THREADS="2")
     p = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT, env=env)
     assert p.returncode == 0, p.stderr[-2000:]
