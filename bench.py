@@ -61,10 +61,11 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="sine96")
     ap.add_argument("--scale", type=int, default=None, help="hexes along x (small cases)")
-    ap.add_argument("--mode", choices=["fp64", "fp32", "fp32ilu"], default="fp32",
+    ap.add_argument("--mode", choices=["fp64", "fp32", "fp32h", "fp32ilu"], default="fp32",
                     help="fp64: FP64 flux + FP64 ILU(0); fp32: FP32 flux + FP32 ILU(0); "
-                         "fp32ilu: FP64 flux + FP32 ILU(0) (shocked flows, where the FP32 flux's "
-                         "rounding floor reaches the Newton tolerance)")
+                         "fp32h: FP32 flux with FP64 faces where the density or pressure jump "
+                         "exceeds 5%% and on boundaries (shocked flows) + FP32 ILU(0); "
+                         "fp32ilu: FP64 flux + FP32 ILU(0)")
     ap.add_argument("--precond", choices=["ilu", "none", "learned"], default="learned",
                     help="learned: the trained network in FGMRES with ILU(0) fallback")
     ap.add_argument("--weights", default=None, help="network weights (.npy) for --precond learned")
@@ -447,8 +448,9 @@ PRECOND = {"none": 0, "ilu": 1, "learned": 2}
 
 
 def make_ctx(grid, ibc, wl, mode, ilu_order, stream):
-    from fosolvers_gb300.euler import FLUX_FP32, ILU_COLOR, ILU_FP32, FOEuler
-    flags = {"fp32": FLUX_FP32 | ILU_FP32, "fp32ilu": ILU_FP32, "fp64": 0}[mode]
+    from fosolvers_gb300.euler import FLUX_FP32, FLUX_HYBRID, ILU_COLOR, ILU_FP32, FOEuler
+    flags = {"fp32": FLUX_FP32 | ILU_FP32, "fp32h": FLUX_FP32 | FLUX_HYBRID | ILU_FP32,
+             "fp32ilu": ILU_FP32, "fp64": 0}[mode]
     if ilu_order == "color":
         flags |= ILU_COLOR
     return FOEuler(grid, ibc, wl.bc_type, wl.bc_param, wl.gamm, wl.r, flags=flags, stream=stream)
@@ -488,6 +490,13 @@ def field_rel_err(a, b, nC):
          float((a[1:4] - b[1:4]).norm(dim=0).max() / b[1:4].norm(dim=0).max()),
          float((a[4] - b[4]).abs().max() / b[4].abs().max())]
     return max(e)
+
+
+def per_variable_err(a, b, nC):
+    """max |a - b| / max |b| of each conserved variable (rho, rho u, rho v, rho w, rho E)."""
+    a, b = a.reshape(5, nC), b.reshape(5, nC)
+    names = ("rho", "rhou", "rhov", "rhow", "rhoE")
+    return {n: float((a[q] - b[q]).abs().max() / b[q].abs().max()) for q, n in enumerate(names)}
 
 
 def cell_rel_err(a, b, nC):
@@ -624,7 +633,7 @@ def main():
         #   Jv        + v, f(y) in per cell (80)
         #   ILU apply the factors (25 values per block) + r in / z out (80 per cell)
         #   pset      state in, geometry, J written, J read and LU written by the factor
-        gb = 8 + (16 if args.mode == "fp32" else 32)
+        gb = 8 + (16 if args.mode in ("fp32", "fp32h") else 32)
         ops = {
             "residual": {"ms": t_rhs, "bytes": 88 * a_ + gb * f_, "count": st["n_rhs"] - st["n_jv"]},
             "jv": {"ms": t_jv, "bytes": 168 * a_ + gb * f_, "count": st["n_jv"]},
@@ -671,7 +680,8 @@ def main():
                 # both runs converge Newton to ||G||_2 <= 1e-8 ||y||_2; the max-norm field
                 # error reflects that tolerance at 26.5M unknowns, the l2 error the precision
                 "state_rel_err_vs_fp64": field_rel_err(y_out, yb, nC),
-                "state_rel_l2_vs_fp64": float((y_out - yb).norm() / yb.norm())}
+                "state_rel_l2_vs_fp64": float((y_out - yb).norm() / yb.norm()),
+                "state_err_per_variable": per_variable_err(y_out, yb, nC)}
         vs64["state_cell_rel_err_vs_fp64"] = cell_rel_err(y_out, yb, nC)
         # yardstick: the FP64 flux with the learned preconditioner, i.e. the FP64 path's own
         # arithmetic on another Krylov path, against the FP64 ILU(0) path -- the difference
@@ -759,6 +769,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
             "dtype": {"fp64": "f64", "fp32": "f32 flux/ILU, f64 Newton+Krylov",
+                      "fp32h": "f32 flux (f64 on faces with >5% jumps and boundaries), f32 "
+                               "ILU, f64 Newton+Krylov",
                       "fp32ilu": "f64 flux, f32 ILU, f64 Newton+Krylov"}[args.mode],
             "data": "synthetic (seeded mesh and state)",
             "config": {"workload": workload_desc(args.workload) if args.scale is None else

@@ -82,6 +82,7 @@ _SIGS = {
     "fos_euler_pset_dev": (C.c_int, [_vp, C.c_double, _vp, C.c_int, _ip, C.c_double]),
     "fos_euler_psol_dev": (C.c_int, [_vp, _vp, _vp]),
     "fos_euler_jac_copy": (C.c_long, [_vp, _ip, _ip, _dp]),
+    "fos_euler_jac_set": (C.c_int, [_vp, _dp]),
     "fos_gnn_create": (C.c_int, [C.POINTER(_vp), C.c_uint]),
     "fos_gnn_destroy": (None, [_vp]),
     "fos_gnn_num_params": (C.c_int, []),
@@ -97,6 +98,8 @@ _SIGS = {
     "fos_ilut_factor_dev": (C.c_int, [_vp, _vp, _vp, _vp, C.c_double, _vp]),
     "fos_ilut_solve_dev": (C.c_int, [_vp, _vp, _vp, _vp]),
     "fos_ilut_status": (C.c_int, [_vp]),
+    "fos_ctx_set_flux_threshold": (C.c_int, [_vp, C.c_double]),
+    "fos_ilut_set_wait_limit": (C.c_int, [_vp, C.c_long, C.c_int]),
     "fos_ilut_copy": (C.c_long, [_vp, _dp, _ip, _ip, C.c_long]),
     "fos_ilut_info": (C.c_int, [_vp, _lp]),
     "fos_ilut_destroy": (None, [_vp]),

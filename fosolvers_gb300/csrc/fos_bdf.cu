@@ -601,8 +601,9 @@ struct Driver {
       }
       if (fallback) {  // continue with ILU(0) from the current iterate
         st.n_fallback++;
-        // exponential back-off: skip the network for the next 1, 2, 4, ... 64 solves
-        wk.learned_backoff = wk.learned_backoff ? std::min(2 * wk.learned_backoff, 64) : 1;
+        // exponential back-off: skip the network for the next 1, 4, 16, ... solves, so a
+        // network that keeps losing to ILU(0) costs a vanishing share of a long run
+        wk.learned_backoff = wk.learned_backoff ? std::min(4 * wk.learned_backoff, 1 << 20) : 1;
         wk.learned_skip = wk.learned_backoff;
         pc = 1;
         if (int rc = ensure_pset()) return rc;
@@ -686,9 +687,10 @@ extern "C" int fos_bdf_run(fos_ctx* c, double t0, double* y, const fos_bdf_opts*
     if (nrc < 0) return nrc;
     const bool conv = nrc == 0;
     if (nrc >= 2) status = nrc;
-    if (!conv) {
+    if (!conv) {  // the failed step is not taken: y goes back to the last accepted state
       st.fails++;
       if (!status) status = 1;
+      FOS_CUDA(cudaMemcpyAsync(y, wk.yn, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
       break;
     }
     std::swap(wk.ym, wk.yn);

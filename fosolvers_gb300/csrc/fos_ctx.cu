@@ -33,7 +33,7 @@ fos_ctx::~fos_ctx() {
                   d_bcT, d_bcP, d_W, d_Whl, d_ell, d_F, d_stage, d_y, d_f, d_z, d_red, d_scal,
                   d_flag, d_prow, d_pcol, d_pdiag, d_cdiag, d_ipos, d_ord, d_fslot, d_Jraw,
                   d_LU, d_LU32, d_lrows_f, d_lrows_b, d_upd_ptr, d_upd, d_ilu_tmp, d_Jb, d_ierr,
-                  d_closure32, d_pia, d_pja, d_pa, d_vol, d_ilut_x, d_plst, d_pdu};
+                  d_closure32, d_pia, d_pja, d_pa, d_vol, d_ilut_x, d_plst, d_pdu, d_fsel};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h_scal) cudaFreeHost(h_scal);
@@ -326,6 +326,10 @@ extern "C" int fos_ctx_create(fos_ctx** out, int nC, int nE, int nPi, int nPb, c
   FOS_TRY(upload(&c->d_cent, cent.data(), cent.size()));
   FOS_TRY(upload(&c->d_ell, ell.data(), ell.size()));
   FOS_TRY(dalloc(&c->d_Whl, 16 * (size_t)nC));
+  if (flags & FOS_FLUX_HYBRID) {
+    FOS_TRY(dalloc(&c->d_fsel, (size_t)nP));
+    FOS_TRY(cudaMemset(c->d_fsel, 0, (size_t)nP) == cudaSuccess ? 0 : -100);
+  }
   FOS_TRY(upload(&c->d_invV, invV.data(), nC));
   FOS_TRY(upload(&c->d_bcT, bcType, nBC));
   FOS_TRY(upload(&c->d_bcP, bcParam, (size_t)maxP * nBC));
@@ -348,6 +352,15 @@ extern "C" int fos_ctx_create(fos_ctx** out, int nC, int nE, int nPi, int nPb, c
 }
 
 extern "C" void fos_ctx_destroy(fos_ctx* ctx) { delete ctx; }
+
+extern "C" int fos_ctx_set_flux_threshold(fos_ctx* ctx, double theta) {
+  if (!ctx || !(theta > 0.0) || !(ctx->flags & FOS_FLUX_HYBRID)) {
+    fos_set_error("fos_ctx_set_flux_threshold: bad arguments or no FOS_FLUX_HYBRID");
+    return -1;
+  }
+  ctx->hyb_theta = theta;
+  return 0;
+}
 
 extern "C" int fos_ctx_set_stream(fos_ctx* ctx, void* stream) {
   if (!ctx) return -1;

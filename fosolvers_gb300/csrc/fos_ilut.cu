@@ -49,6 +49,8 @@ struct fos_ilut {
   int* h_ctr = nullptr;    // pinned copy
   int fepoch = 0;
   int cap = 256;           // working-row capacity (entries of L and of U)
+  long spin_limit = 0;     // polls of one dependency wait before giving up (0: kSpinLimit)
+  int withhold = -1;       // failure injection: a row that is never published (-1: none)
   bool factored = false;
   long launches = 0;
   ~fos_ilut();
@@ -79,8 +81,8 @@ __device__ __forceinline__ void st_release(int* p, int v) {
 
 // Spin until flag[j] >= epoch; false when the limit ran out or another warp already gave
 // up (the error word is set), so no wait outlives a failure.
-__device__ __forceinline__ bool wait_row(const int* flag, int j, int epoch, int* ctr) {
-  for (long it = 0; it < kSpinLimit; it++) {
+__device__ __forceinline__ bool wait_row(const int* flag, int j, int epoch, int* ctr, long spin) {
+  for (long it = 0; it < spin; it++) {
     if (ld_acquire(flag + j) >= epoch) return true;
     if (*(volatile int*)(ctr + 3) == kErrTimeout) return false;
     if (it > 8) __nanosleep(32);
@@ -147,7 +149,8 @@ __global__ void __launch_bounds__(32 * kWarps) k_ilut_factor(
     int lfil, double droptol, int cap, int epoch, int* __restrict__ Lcol,
     double* __restrict__ Lval, int* __restrict__ Lcnt, int* __restrict__ Ucol,
     double* __restrict__ Uval, int* __restrict__ Ucnt, double* __restrict__ dinv,
-    int* __restrict__ levL, int* __restrict__ done, int* __restrict__ ctr) {
+    int* __restrict__ levL, int* __restrict__ done, int* __restrict__ ctr, long spin,
+    int withhold) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned hmask = 4u * cap - 1u;
@@ -236,7 +239,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_ilut_factor(
       // lane 0 waits for the pivot row; every lane then acquires the flag itself, which
       // orders its reads of the row after the pivot warp's release
       bool ready = false;
-      if (lane == 0) ready = wait_row(done, jrow, epoch, ctr);
+      if (lane == 0) ready = wait_row(done, jrow, epoch, ctr, spin);
       if (!__shfl_sync(~0u, ready, 0)) { ok = false; break; }
       (void)ld_acquire(done + jrow);
       const double fact = __dmul_rn(lval[jj], dinv[jrow]);
@@ -290,7 +293,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_ilut_factor(
         dinv[ii] = 0.0;
         levL[ii] = 1;
         __threadfence();
-        st_release(done + ii, epoch);
+        if (ii != withhold) st_release(done + ii, epoch);
       }
       __syncwarp();
       continue;
@@ -333,7 +336,7 @@ __global__ void __launch_bounds__(32 * kWarps) k_ilut_factor(
     }
     __threadfence();
     __syncwarp();
-    if (lane == 0) st_release(done + ii, epoch);
+    if (lane == 0 && ii != withhold) st_release(done + ii, epoch);
     // L part afterwards, off the rows-below path: the lfil largest multipliers (:236-254);
     // only the sweeps read it, after this kernel
     const int keepl = min(len, lfil);
@@ -376,9 +379,10 @@ __device__ __forceinline__ bool pending(double v) {
   return __double_as_longlong(v) == (long long)kPending;
 }
 // wait for an unknown: bounded spin, false (and the error word set) when the limit ran out
-__device__ __forceinline__ double wait_value(const double* x, int j, double v, int* ctr, bool& ok) {
+__device__ __forceinline__ double wait_value(const double* x, int j, double v, int* ctr, bool& ok,
+                                             long spin) {
   for (long it = 0; pending(v); it++) {
-    if (it >= kSpinLimit) { atomicCAS(ctr + 3, 0, kErrTimeout); ok = false; return 0.0; }
+    if (it >= spin) { atomicCAS(ctr + 3, 0, kErrTimeout); ok = false; return 0.0; }
     if (*(volatile int*)(ctr + 3) == kErrTimeout) { ok = false; return 0.0; }
     if (it > 8) __nanosleep(32);
     v = ld_poll(x + j);
@@ -396,7 +400,7 @@ __global__ void k_fill_pending(long n, double* __restrict__ x) {
 // ran out makes the sum NaN, so the failure reaches callers that only look at the result
 // (the Krylov driver's non-finite checks) as well as fos_ilut_status.
 __device__ __forceinline__ double row_dot(const int* __restrict__ col, const double* __restrict__ val,
-                                         int cnt, const double* x, int* ctr, int lane) {
+                                         int cnt, const double* x, int* ctr, int lane, long spin) {
   double s = 0.0;
   bool ok = true;
   for (int k = lane; k < cnt; k += 64) {
@@ -404,10 +408,10 @@ __device__ __forceinline__ double row_dot(const int* __restrict__ col, const dou
     const bool two = k + 32 < cnt;
     const int j1 = two ? col[k + 32] : j0;
     double v0 = ld_poll(x + j0), v1 = ld_poll(x + j1);
-    v0 = wait_value(x, j0, v0, ctr, ok);
+    v0 = wait_value(x, j0, v0, ctr, ok, spin);
     s += val[k] * v0;
     if (two) {
-      v1 = wait_value(x, j1, v1, ctr, ok);
+      v1 = wait_value(x, j1, v1, ctr, ok, spin);
       s += val[k + 32] * v1;
     }
   }
@@ -427,7 +431,8 @@ __global__ void __launch_bounds__(256) k_ilut_fwd(int n, int lfil, const int* __
                                                   const int* __restrict__ Lcnt,
                                                   const int* __restrict__ perm,
                                                   const double* y, double* z, double* x,
-                                                  int* __restrict__ ctr) {
+                                                  int* __restrict__ ctr, long spin,
+                                                  int withhold) {
   const int lane = threadIdx.x & 31;
   const size_t slot = (size_t)(lfil > 0 ? lfil : 1);
   for (;;) {
@@ -437,10 +442,11 @@ __global__ void __launch_bounds__(256) k_ilut_fwd(int n, int lfil, const int* __
     if (t >= n) return;
     const int i = perm[t];
     const double yi = y[i];  // own operand first, so its load overlaps the dependency polls
-    const double s = row_dot(Lcol + (size_t)i * slot, Lval + (size_t)i * slot, Lcnt[i], z, ctr, lane);
+    const double s = row_dot(Lcol + (size_t)i * slot, Lval + (size_t)i * slot, Lcnt[i], z, ctr, lane,
+                             spin);
     if (lane == 0) {
       x[i] = __longlong_as_double((long long)kPending);
-      st_publish(z + i, yi - s);
+      if (i != withhold) st_publish(z + i, yi - s);
     }
   }
 }
@@ -453,7 +459,7 @@ __global__ void __launch_bounds__(256) k_ilut_bwd(int n, int lfil, const int* __
                                                   const double* __restrict__ dinv,
                                                   const int* __restrict__ perm,
                                                   const double* __restrict__ z, double* x,
-                                                  int* __restrict__ ctr) {
+                                                  int* __restrict__ ctr, long spin) {
   const int lane = threadIdx.x & 31;
   const size_t slot = (size_t)(lfil > 0 ? lfil : 1);
   for (;;) {
@@ -463,7 +469,8 @@ __global__ void __launch_bounds__(256) k_ilut_bwd(int n, int lfil, const int* __
     if (t >= n) return;
     const int i = perm[t];
     const double zi = z[i], di = dinv[i];
-    const double s = row_dot(Ucol + (size_t)i * slot, Uval + (size_t)i * slot, Ucnt[i], x, ctr, lane);
+    const double s = row_dot(Ucol + (size_t)i * slot, Uval + (size_t)i * slot, Ucnt[i], x, ctr, lane,
+                             spin);
     if (lane == 0) st_publish(x + i, di * (zi - s));
   }
 }
@@ -636,7 +643,9 @@ int fos_ilut_factor_on(fos_ilut* f, const int* ia, const int* ja, const double* 
     k_ilut_factor<<<grid, 32 * kWarps, smem, s>>>(f->n, ia, ja, a, f->lfil, droptol, f->cap,
                                                   f->fepoch, f->d_Lcol, f->d_Lval, f->d_Lcnt,
                                                   f->d_Ucol, f->d_Uval, f->d_Ucnt, f->d_dinv,
-                                                  f->d_levL, f->d_done, f->d_ctr);
+                                                  f->d_levL, f->d_done, f->d_ctr,
+                                                  f->spin_limit > 0 ? f->spin_limit : kSpinLimit,
+                                                  f->withhold);
     f->launches++;
     FOS_CUDA(cudaGetLastError());
     FOS_CUDA(cudaMemcpyAsync(f->h_ctr, f->d_ctr, 8 * sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -667,6 +676,7 @@ int fos_ilut_solve_on(fos_ilut* f, const double* y, double* x, cudaStream_t s) {
     return -1;
   }
   FOS_CUDA(cudaMemsetAsync(f->d_ctr, 0, 4 * sizeof(int), s));
+  const long spin = f->spin_limit > 0 ? f->spin_limit : kSpinLimit;
   k_fill_pending<<<(f->n + 255) / 256, 256, 0, s>>>(f->n, f->d_z);
   // rows in flight: kLookahead levels of the average width, at least one CTA per SM
   auto sweep_grid = [&](int nlev) {
@@ -675,9 +685,10 @@ int fos_ilut_solve_on(fos_ilut* f, const double* y, double* x, cudaStream_t s) {
     return std::min(grid_for((const void*)k_ilut_fwd, 256, 0, 8, f->n), (int)((warps + 7) / 8));
   };
   k_ilut_fwd<<<sweep_grid(f->nlevF), 256, 0, s>>>(f->n, f->lfil, f->d_Lcol, f->d_Lval, f->d_Lcnt,
-                                                  f->d_permF, y, f->d_z, x, f->d_ctr);
+                                                  f->d_permF, y, f->d_z, x, f->d_ctr, spin,
+                                                  f->withhold);
   k_ilut_bwd<<<sweep_grid(f->nlevB), 256, 0, s>>>(f->n, f->lfil, f->d_Ucol, f->d_Uval, f->d_Ucnt,
-                                                  f->d_dinv, f->d_permB, f->d_z, x, f->d_ctr);
+                                                  f->d_dinv, f->d_permB, f->d_z, x, f->d_ctr, spin);
   f->launches += 3;
   FOS_CUDA(cudaGetLastError());
   return 0;
@@ -690,6 +701,17 @@ extern "C" int fos_ilut_factor_dev(fos_ilut* f, const int* ia, const int* ja, co
 
 extern "C" int fos_ilut_solve_dev(fos_ilut* f, const double* y, double* x, void* stream) {
   return fos_ilut_solve_on(f, y, x, (cudaStream_t)stream);
+}
+
+// Failure injection for tests: the wait limit and a row that is never published.
+extern "C" int fos_ilut_set_wait_limit(fos_ilut* f, long polls, int withhold_row) {
+  if (!f || withhold_row < -1 || withhold_row >= f->n) {
+    fos_set_error("fos_ilut_set_wait_limit: bad arguments");
+    return -1;
+  }
+  f->spin_limit = polls > 0 ? polls : 0;
+  f->withhold = withhold_row;
+  return 0;
 }
 
 // Solve status after the stream has drained: 0, or -6 when a dependency wait ran out.

@@ -65,6 +65,9 @@ struct fos_ctx {
   double* d_invV = nullptr;   // [nC]
   float4* d_closure32 = nullptr;  // [nC] sum of outward aP n over the cell's faces (FP32 flux);
                                   // null when every cell is closed
+  unsigned char* d_fsel = nullptr;  // [nF] FOS_FLUX_HYBRID: 1 = face evaluated in FP64 by the
+                                    // last residual (interior faces; written by the L cell)
+  double hyb_theta = 0.05;          // relative density / pressure jump that selects FP64
   int* d_bcT = nullptr;       // [nBC]
   double* d_bcP = nullptr;    // [maxP*nBC]
 

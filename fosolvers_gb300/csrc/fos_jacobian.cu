@@ -1026,6 +1026,32 @@ extern "C" long fos_euler_jac_copy(fos_ctx* c, int* rowptr, int* col, double* va
   return c->nnzb;
 }
 
+// The caller's Jacobian blocks in the layout fos_euler_jac_copy returns (rows and columns by
+// ILU position, row-major 5x5 blocks, before scaling by -gamma/v); the next pset with jok = 1
+// factors P = I - gamma diag(1/v) J from them.
+extern "C" int fos_euler_jac_set(fos_ctx* c, const double* val) {
+  if (!c || !val) {
+    fos_set_error("fos_euler_jac_set: bad arguments");
+    return -1;
+  }
+  if (c->flags & FOS_PREC_ILUT) {
+    fos_set_error("fos_euler_jac_set: not available with FOS_PREC_ILUT");
+    return -1;
+  }
+  if (int rc = fos_jac_setup(c)) return rc;
+  const size_t n = 25 * (size_t)c->nnzb;
+  FOS_CUDA(cudaStreamSynchronize(c->stream));
+  if (c->flags & FOS_ILU_FP32) {
+    std::vector<float> tmp(n);
+    for (size_t k = 0; k < n; k++) tmp[k] = (float)val[k];
+    FOS_CUDA(cudaMemcpy(c->d_Jraw, tmp.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+  } else {
+    FOS_CUDA(cudaMemcpy(c->d_Jraw, val, n * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  c->has_jac = true;
+  return 0;
+}
+
 extern "C" int fos_ctx_ilu_order(const fos_ctx* c, int* old2pos) {
   if (!c || !old2pos || c->h_ilu_pos.empty()) {
     fos_set_error("fos_ctx_ilu_order: no factorisation set up yet");

@@ -268,41 +268,44 @@ __device__ __forceinline__ void load_hl(const float* __restrict__ W, int c, PHL&
   P.s = e.x;
 }
 
-// FP32 Roe flow from means / jumps (shared by the interior and boundary kernels)
-__device__ __forceinline__ void roe_split_mj(float rm, float dr, float um, float du, float vm,
-                                             float dv, float wm, float dww, float Hm, float dH,
-                                             float dp, float sL, float sR, float nx, float ny,
-                                             float nz, float aP, float gm1, float dF[5],
-                                             float dw[5]) {
-  const float unm = um * nx + vm * ny + wm * nz;
-  const float dun = du * nx + dv * ny + dww * nz;
-  const float mm = rm * unm + 0.25f * dr * dun;  // mean of m = rho un
-  const float dm = rm * dun + dr * unm;          // jump of m
-  const float h = 0.5f * aP;
+// Roe flow from means / jumps in flux-difference form (the interior faces of the FP32 flux,
+// in FP32; with FOS_FLUX_HYBRID the faces with large jumps, in FP64): dF = aP (F_R - F_L).n / 2
+// expanded with d(ab) = mean(a) d(b) + d(a) mean(b) and mean(ab) = mean(a) mean(b) + d(a) d(b)/4,
+// and dw = aP |A~| (U_R - U_L) / 2 from the Roe average (Euler.f90:90-126)
+template <typename T>
+__device__ __forceinline__ void roe_split_mj(T rm, T dr, T um, T du, T vm, T dv, T wm, T dww,
+                                             T Hm, T dH, T dp, T sL, T sR, T nx, T ny, T nz,
+                                             T aP, T gm1, T dF[5], T dw[5]) {
+  const T half = T(0.5), quarter = T(0.25);
+  const T unm = um * nx + vm * ny + wm * nz;
+  const T dun = du * nx + dv * ny + dww * nz;
+  const T mm = rm * unm + quarter * dr * dun;  // mean of m = rho un
+  const T dm = rm * dun + dr * unm;            // jump of m
+  const T h = half * aP;
   dF[0] = h * dm;
   dF[1] = h * (mm * du + dm * um + dp * nx);
   dF[2] = h * (mm * dv + dm * vm + dp * ny);
   dF[3] = h * (mm * dww + dm * wm + dp * nz);
   dF[4] = h * (mm * dH + dm * Hm);
-  const float kap = 0.5f * (sR - sL) / (sL + sR);
-  const float ua = um + kap * du, va = vm + kap * dv, wa = wm + kap * dww, Ha = Hm + kap * dH;
-  const float rhoA = sL * sR;
-  const float q2 = ua * ua + va * va + wa * wa;
-  const float c2 = gm1 * (Ha - 0.5f * q2);
-  const float ca = sqrtf(c2);
-  const float ic2 = 1.0f / c2;
-  const float unA = ua * nx + va * ny + wa * nz;
-  const float au = fabsf(unA);
-  const float wE = dr - dp * ic2;
-  float d0 = au * wE;
-  float d1 = au * (wE * ua + rhoA * (du - nx * dun));
-  float d2 = au * (wE * va + rhoA * (dv - ny * dun));
-  float d3 = au * (wE * wa + rhoA * (dww - nz * dun));
-  float d4 = au * (wE * (0.5f * q2) + rhoA * (ua * du + va * dv + wa * dww - unA * dun));
-  const float s1 = fabsf(unA - ca) * (0.5f * (dp - rhoA * ca * dun) * ic2);
+  const T kap = half * (sR - sL) / (sL + sR);
+  const T ua = um + kap * du, va = vm + kap * dv, wa = wm + kap * dww, Ha = Hm + kap * dH;
+  const T rhoA = sL * sR;
+  const T q2 = ua * ua + va * va + wa * wa;
+  const T c2 = gm1 * (Ha - half * q2);
+  const T ca = sqrt(c2);
+  const T ic2 = T(1) / c2;
+  const T unA = ua * nx + va * ny + wa * nz;
+  const T au = fabs(unA);
+  const T wE = dr - dp * ic2;
+  T d0 = au * wE;
+  T d1 = au * (wE * ua + rhoA * (du - nx * dun));
+  T d2 = au * (wE * va + rhoA * (dv - ny * dun));
+  T d3 = au * (wE * wa + rhoA * (dww - nz * dun));
+  T d4 = au * (wE * (half * q2) + rhoA * (ua * du + va * dv + wa * dww - unA * dun));
+  const T s1 = fabs(unA - ca) * (half * (dp - rhoA * ca * dun) * ic2);
   d0 += s1; d1 += s1 * (ua - nx * ca); d2 += s1 * (va - ny * ca); d3 += s1 * (wa - nz * ca);
   d4 += s1 * (Ha - unA * ca);
-  const float s2 = fabsf(unA + ca) * (0.5f * (dp + rhoA * ca * dun) * ic2);
+  const T s2 = fabs(unA + ca) * (half * (dp + rhoA * ca * dun) * ic2);
   d0 += s2; d1 += s2 * (ua + nx * ca); d2 += s2 * (va + ny * ca); d3 += s2 * (wa + nz * ca);
   d4 += s2 * (Ha + unA * ca);
   dw[0] = h * d0; dw[1] = h * d1; dw[2] = h * d2; dw[3] = h * d3; dw[4] = h * d4;
@@ -315,21 +318,21 @@ __device__ __forceinline__ void roe_split_mj(float rm, float dr, float um, float
 //     zero normal velocity and the flow reduces to aP (0, (p + rho un (un + c)) n, 0), c^2 =
 //     (g-1)(H - |u_t|^2/2); the difference aP rho un (-1, (un + c) n - u, -H) is formed in
 //     FP32 from the FP32 primitives (k_prim_hl, same state as y + s v);
-//   other conditions: k_face64's FP64 flow (interior and ghost primitives from the conserved
-//     variables) minus the own flux, in FP64.
+//   other conditions (and walls too with FOS_FLUX_HYBRID, all64): k_face64's FP64 flow
+//     (interior and ghost primitives from the conserved variables) minus the own flux, in FP64.
 __global__ void __launch_bounds__(kThreads) k_bface32(
     int nFi, int nF, int nC, const int2* __restrict__ faceLR, const double2* __restrict__ faceNA,
     const float4* __restrict__ faceNA32, const float* __restrict__ Whl, float gm1f,
     const double* __restrict__ y, const double* __restrict__ v, const double* __restrict__ d_s,
     const int* __restrict__ bcT, const double* __restrict__ bcP, int maxP, double g, double r,
-    double* __restrict__ F) {
+    double* __restrict__ F, int all64) {
   const int f = nFi + blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nF) return;
   const int2 lr = __ldg(faceLR + f);
   const int row = lr.y;
   const int type = row > 0 ? bcT[row - 1] : FOS_BC_WALL;
   double2* F2 = reinterpret_cast<double2*>(F + 6 * (size_t)f);
-  if (type == FOS_BC_WALL) {
+  if (type == FOS_BC_WALL && !all64) {
     const float4 na = __ldg(faceNA32 + f);
     const float4* w4 = reinterpret_cast<const float4*>(Whl + 16 * (size_t)lr.x);
     const float4 a = __ldg(w4), b = __ldg(w4 + 1);  // (rho, u, v, w), (H, p, ...) hi parts
@@ -374,14 +377,21 @@ __global__ void __launch_bounds__(kThreads) k_bface32(
 // Each face is evaluated twice -- cheap FP32 arithmetic in exchange for the 2 x 48 B per face
 // a face-flow array costs in HBM traffic.  Cells that are not closed (Sc non-null: warped
 // faces) also take the own-flux sum the difference form leaves out, -F(u_c).S_c.
-template <int kW>
+// kHyb (FOS_FLUX_HYBRID): a face whose relative density or pressure jump exceeds theta is
+// evaluated in FP64 (the same expressions, from the FP64 values of the (hi, lo) pairs and
+// the FP64 geometry); both cells decide from the same face-oriented values, so they agree.
+// A residual (mode 0) records the choice per face (fsel, written by the face's L cell); a
+// Jv (mode 1) reuses it, so f(y + s v) and f(y) evaluate every face the same way.
+template <int kW, bool kHyb>
 __global__ void __launch_bounds__(kThreads) k_cell32(
     int nC, int nFi, const int* __restrict__ ell, const int2* __restrict__ faceLR,
     const float4* __restrict__ faceNA, const float* __restrict__ W, float gm1,
     const double* __restrict__ Fb, const float4* __restrict__ Sc,
     const double* __restrict__ invV, int mode,
     const double* __restrict__ vv, const double* __restrict__ fy, const double* __restrict__ d_s,
-    double a, double b, double* __restrict__ out, int* __restrict__ flag) {
+    double a, double b, double* __restrict__ out, int* __restrict__ flag,
+    const double2* __restrict__ faceNA64, unsigned char* __restrict__ fsel, float theta,
+    double gm1d) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nC) return;
   int e[kW];
@@ -411,10 +421,39 @@ __global__ void __launch_bounds__(kThreads) k_cell32(
         m[j] = 0.5f * (L.h[j] + R.h[j]) + 0.5f * (L.l[j] + R.l[j]);
         d[j] = (R.h[j] - L.h[j]) + (R.l[j] - L.l[j]);
       }
-      roe_split_mj(m[0], d[0], m[1], d[1], m[2], d[2], m[3], d[3], m[4], d[4], d[5], L.s, R.s,
-                   na.x, na.y, na.z, na.w, gm1, dF, dw);
+      bool f64 = false;
+      if (kHyb) {
+        if (mode == 0 || !fsel) {
+          f64 = fabsf(d[0]) > theta * fminf(L.h[0], R.h[0]) ||
+                fabsf(d[5]) > theta * fminf(L.h[5], R.h[5]);
+          if (mode == 0 && fsel && !isR) fsel[f] = f64 ? 1 : 0;
+        } else {
+          f64 = __ldg(fsel + f) != 0;
+        }
+      }
+      if (kHyb && f64) {
+        double md[6], dd[6], rl = 0.0, rr = 0.0;
 #pragma unroll
-      for (int q = 0; q < 5; q++) t[q] = f2d_bits(fmaf(sw, dw[q], dF[q]));
+        for (int j = 0; j < 6; j++) {
+          const double xl = f2d_bits(L.h[j]) + f2d_bits(L.l[j]);
+          const double xr = f2d_bits(R.h[j]) + f2d_bits(R.l[j]);
+          md[j] = 0.5 * (xl + xr);
+          dd[j] = xr - xl;
+          if (j == 0) { rl = xl; rr = xr; }
+        }
+        const double2 n01 = __ldg(faceNA64 + 2 * (size_t)f), n2a = __ldg(faceNA64 + 2 * (size_t)f + 1);
+        double dF64[5], dw64[5];
+        roe_split_mj<double>(md[0], dd[0], md[1], dd[1], md[2], dd[2], md[3], dd[3], md[4],
+                             dd[4], dd[5], sqrt(rl), sqrt(rr), n01.x, n01.y, n2a.x, n2a.y, gm1d,
+                             dF64, dw64);
+#pragma unroll
+        for (int q = 0; q < 5; q++) t[q] = isR ? dF64[q] + dw64[q] : dF64[q] - dw64[q];
+      } else {
+        roe_split_mj<float>(m[0], d[0], m[1], d[1], m[2], d[2], m[3], d[3], m[4], d[4], d[5],
+                            L.s, R.s, na.x, na.y, na.z, na.w, gm1, dF, dw);
+#pragma unroll
+        for (int q = 0; q < 5; q++) t[q] = f2d_bits(fmaf(sw, dw[q], dF[q]));
+      }
     } else {  // boundary face (cell is L): the FP64 difference of k_bface32
       const double2* F2 = reinterpret_cast<const double2*>(Fb + 6 * (size_t)f);
       const double2 a0 = __ldg(F2), a1 = __ldg(F2 + 1), a2 = __ldg(F2 + 2);
@@ -433,6 +472,12 @@ __global__ void __launch_bounds__(kThreads) k_cell32(
     acc[4] -= f2d_bits(t * P.h[4]);
   }
   gather_epilogue(nC, c, acc, __ldg(invV + c), mode, vv, fy, d_s, a, b, out, flag);
+}
+
+using cell32_fn = decltype(&k_cell32<4, false>);
+cell32_fn cell32_kernel(int ell_w, bool hyb) {
+  if (ell_w == 4) return hyb ? k_cell32<4, true> : k_cell32<4, false>;
+  return hyb ? k_cell32<6, true> : k_cell32<6, false>;
 }
 
 __global__ void k_permute(int nC, int nplanes, const int* __restrict__ idx,
@@ -505,21 +550,18 @@ int fos_residual_launch(fos_ctx* c, const double* y, const double* v, const doub
   const double gm1 = c->gamm - 1.0;
   if (c->flags & FOS_FLUX_FP32) {
     fos_launch(c, k_prim_hl, nblk(c->nC), kThreads, c->nC, y, v, d_s, gm1, c->d_Whl);
+    const bool hyb = (c->flags & FOS_FLUX_HYBRID) != 0;
     if (c->nFb)
       fos_launch(c, k_bface32, nblk(c->nFb), kThreads, c->nFi, c->nF, c->nC,
                  (const int2*)c->d_faceLR, (const double2*)c->d_faceNA,
                  (const float4*)c->d_faceNA32, (const float*)c->d_Whl, (float)gm1, y, v, d_s,
-                 (const int*)c->d_bcT, (const double*)c->d_bcP, c->maxP, c->gamm, c->r, c->d_F);
-    if (c->ell_w == 4)
-      fos_launch(c, k_cell32<4>, nblk(c->nC), kThreads, c->nC, c->nFi, (const int*)c->d_ell,
-                 (const int2*)c->d_faceLR, (const float4*)c->d_faceNA32, (const float*)c->d_Whl,
-                 (float)gm1, (const double*)c->d_F, (const float4*)c->d_closure32,
-                 (const double*)c->d_invV, mode, v, fy, d_s, a, b, out, c->d_flag);
-    else
-      fos_launch(c, k_cell32<6>, nblk(c->nC), kThreads, c->nC, c->nFi, (const int*)c->d_ell,
-                 (const int2*)c->d_faceLR, (const float4*)c->d_faceNA32, (const float*)c->d_Whl,
-                 (float)gm1, (const double*)c->d_F, (const float4*)c->d_closure32,
-                 (const double*)c->d_invV, mode, v, fy, d_s, a, b, out, c->d_flag);
+                 (const int*)c->d_bcT, (const double*)c->d_bcP, c->maxP, c->gamm, c->r, c->d_F,
+                 hyb ? 1 : 0);
+    fos_launch(c, cell32_kernel(c->ell_w, hyb), nblk(c->nC), kThreads, c->nC, c->nFi,
+               (const int*)c->d_ell, (const int2*)c->d_faceLR, (const float4*)c->d_faceNA32,
+               (const float*)c->d_Whl, (float)gm1, (const double*)c->d_F,
+               (const float4*)c->d_closure32, (const double*)c->d_invV, mode, v, fy, d_s, a, b,
+               out, c->d_flag, (const double2*)c->d_faceNA, c->d_fsel, (float)c->hyb_theta, gm1);
   } else {
     fos_launch(c, k_prim64, nblk(c->nC), kThreads, c->nC, y, v, d_s, gm1, c->d_W);
     fos_launch(c, k_face64, nblk(c->nF), kThreads, c->nFi, c->nF, c->nC,
@@ -662,21 +704,17 @@ extern "C" int fos_euler_rhs_dev_static(const fos_ctx* c, double t, const double
     float* Whl = reinterpret_cast<float*>(bytes);
     double* F = reinterpret_cast<double*>(bytes + kStaticCellBytes);
     k_prim_hl<<<nblk(c->nC), kThreads, 0, s>>>(c->nC, y, nullptr, nullptr, gm1, Whl);
+    const bool hyb = (c->flags & FOS_FLUX_HYBRID) != 0;
     if (c->nFb)
       k_bface32<<<nblk(c->nFb), kThreads, 0, s>>>(c->nFi, c->nF, c->nC, c->d_faceLR,
                                                   c->d_faceNA, c->d_faceNA32, Whl, (float)gm1, y,
                                                   nullptr, nullptr, c->d_bcT, c->d_bcP, c->maxP,
-                                                  c->gamm, c->r, F);
-    if (c->ell_w == 4)
-      k_cell32<4><<<nblk(c->nC), kThreads, 0, s>>>(c->nC, c->nFi, c->d_ell, c->d_faceLR,
-                                                   c->d_faceNA32, Whl, (float)gm1, F,
-                                                   c->d_closure32, c->d_invV, 0, nullptr,
-                                                   nullptr, nullptr, 0.0, 0.0, ydot, nullptr);
-    else
-      k_cell32<6><<<nblk(c->nC), kThreads, 0, s>>>(c->nC, c->nFi, c->d_ell, c->d_faceLR,
-                                                   c->d_faceNA32, Whl, (float)gm1, F,
-                                                   c->d_closure32, c->d_invV, 0, nullptr,
-                                                   nullptr, nullptr, 0.0, 0.0, ydot, nullptr);
+                                                  c->gamm, c->r, F, hyb ? 1 : 0);
+    // the face choice of the hybrid flux is made from this state (no record kept)
+    cell32_kernel(c->ell_w, hyb)<<<nblk(c->nC), kThreads, 0, s>>>(
+        c->nC, c->nFi, c->d_ell, c->d_faceLR, c->d_faceNA32, Whl, (float)gm1, F, c->d_closure32,
+        c->d_invV, 0, nullptr, nullptr, nullptr, 0.0, 0.0, ydot, nullptr, c->d_faceNA, nullptr,
+        (float)c->hyb_theta, gm1);
   } else {
     double* W = reinterpret_cast<double*>(bytes);
     double* F = reinterpret_cast<double*>(bytes + kStaticCellBytes);

@@ -27,6 +27,7 @@ FLUX_FP64, FLUX_FP32 = 0, 1
 ORDER_RCM, ORDER_NATURAL = 0, 2
 ILU_FP32, ILU_COLOR = 4, 8
 PREC_ILUT = 16  # pset/psol with ILUT (FP64) instead of block ILU(0)
+FLUX_HYBRID = 32  # with FLUX_FP32: faces with large density / pressure jumps in FP64
 
 
 @dataclass
@@ -220,6 +221,12 @@ class FOEuler:
         check(L.fos_euler_jac_copy(self._h, iptr(rowptr), iptr(col), dptr(val)), "jac_copy")
         return rowptr, col, val.reshape(nnzb, 5, 5)
 
+    def set_jacobian(self, val: np.ndarray):
+        """Replace the stored Jacobian blocks (val[nnzb, 5, 5], the layout of jacobian());
+        the next pset with jok = 1 factors P from them."""
+        v = np.ascontiguousarray(val, np.float64).reshape(-1)
+        check(_lib.lib().fos_euler_jac_set(self._h, dptr(v)), "jac_set")
+
     # ---------------------------------------------------------------- driver
     @staticmethod
     def bdf_defaults(**kw) -> BdfOpts:
@@ -252,6 +259,11 @@ class FOEuler:
                                                C.byref(ad), C.byref(st), C.byref(ast)),
                    "fos_bdf_adaptive")
         return rc, st.as_dict(), ast.as_dict()
+
+    def set_flux_threshold(self, theta: float):
+        """Relative density / pressure jump above which a face of the FLUX_HYBRID flux is
+        evaluated in FP64 (default 0.05)."""
+        check(_lib.lib().fos_ctx_set_flux_threshold(self._h, float(theta)), "set_flux_threshold")
 
     def set_ilut(self, lfil: int = 50, droptol: float = 1e-6):
         """ILUT parameters of a context created with PREC_ILUT (fopbc's fill 50 and drop

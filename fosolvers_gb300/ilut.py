@@ -84,6 +84,12 @@ class ILU:
         check(_lib.lib().fos_ilut_status(self.handle), "fos_ilut_status")
         return x.cpu().numpy()
 
+    def set_wait_limit(self, polls: int = 0, withhold_row: int = -1):
+        """Failure injection: the polls of every dependency wait (0: the default) and a row
+        that is never published (-1: none), for the following factor and solve calls."""
+        check(_lib.lib().fos_ilut_set_wait_limit(self.handle, int(polls), int(withhold_row)),
+              "fos_ilut_set_wait_limit")
+
     def msr(self):
         """(alu, jlu, ju): the factors in ilut's MSR layout, 1-based values."""
         L = _lib.lib()

@@ -48,8 +48,15 @@ enum {
   FOS_ORDER_NATURAL = 2,
   FOS_ILU_FP32 = 4,    /* ILU(0) factors and apply in FP32 */
   FOS_ILU_COLOR = 8,   /* ILU(0) on a multicolour ordering (few levels) */
-  FOS_PREC_ILUT = 16   /* pset/psol factor P with ILUT (FP64) instead of block ILU(0);
+  FOS_PREC_ILUT = 16,  /* pset/psol factor P with ILUT (FP64) instead of block ILU(0);
                           parameters from fos_ctx_set_ilut, default lfil 50, droptol 1e-6 */
+  FOS_FLUX_HYBRID = 32 /* with FOS_FLUX_FP32: interior faces whose relative density or
+                          pressure jump exceeds a threshold (fos_ctx_set_flux_threshold,
+                          default 0.05) and all boundary faces are evaluated in FP64, the rest
+                          in FP32 -- for shocked flows, where the FP32 rounding of the large
+                          jumps puts the Newton residual's floor above its tolerance.  A
+                          residual evaluation records the choice per face; a Jv reuses the
+                          choice of the last residual on the context */
 };
 
 /* ------------------------------------------------------------------ setup */
@@ -85,6 +92,10 @@ int fos_ctx_create(fos_ctx** out, int nC, int nE, int nPi, int nPb, const int* i
                    int nBC, const int* bcType, const double* bcParam, int maxP, double gamm,
                    double r, int index_base, int flags);
 void fos_ctx_destroy(fos_ctx* ctx);
+/* FOS_FLUX_HYBRID threshold: a face is evaluated in FP64 when |rho_R - rho_L| or
+ * |p_R - p_L| exceeds theta times the smaller of the two sides' values.  Returns 0, or -1 for
+ * theta <= 0 or a context without FOS_FLUX_HYBRID. */
+int fos_ctx_set_flux_threshold(fos_ctx* ctx, double theta);
 /* CUDA stream (cudaStream_t as void*) for all subsequent launches; NULL = legacy default */
 int fos_ctx_set_stream(fos_ctx* ctx, void* stream);
 /* out[0..8] = nC, nPi, nPb, nlev_fwd, nlev_bwd, nnzb, bandwidth, flags,
@@ -126,7 +137,9 @@ int fos_euler_rhs_dev(fos_ctx* ctx, double t, const double* y, double* ydot);
  * up the array's device address (make that first call before any stream capture).  All
  * calls share the array: calls whose kernels overlap on the GPU (other streams, other
  * threads) race and must be serialised by the caller.  No part of the array needs to start
- * at zero.  Non-finite results are not flagged (use fos_euler_rhs for that). */
+ * at zero.  Non-finite results are not flagged (use fos_euler_rhs for that).  The array's
+ * address is looked up once per device and kept, so the library must not be used across a
+ * cudaDeviceReset; the kernels of this call are not counted in fos_ctx_info's launches. */
 #define FOS_STATIC_MAX_CELLS 65536
 #define FOS_STATIC_MAX_FACES 147456
 int fos_euler_rhs_dev_static(const fos_ctx* ctx, double t, const double* y, double* ydot);
@@ -151,6 +164,12 @@ int fos_euler_psol_dev(fos_ctx* ctx, const double* r, double* z);
  * positions).  rowptr nC+1, col nnzb, val 25*nnzb (row-major blocks).  Pass NULL to
  * query nnzb through the return value. */
 long fos_euler_jac_copy(fos_ctx* ctx, int* rowptr, int* col, double* val);
+/* The inverse of fos_euler_jac_copy: replace J by the caller's blocks (val 25*nnzb, the same
+ * layout), e.g. a Jacobian assembled elsewhere or modified; the next fos_euler_pset[_dev]
+ * with jok = 1 factors P = I - gamma diag(1/v) J from it (CVODE's jok contract: J kept, only
+ * gamma new).  With FOS_ILU_FP32 the blocks are stored rounded to FP32.  No counterpart in
+ * the reference (its pset is a stub).  Returns 0, or < 0 (FOS_PREC_ILUT contexts: -1). */
+int fos_euler_jac_set(fos_ctx* ctx, const double* val);
 
 /* ------------------------------------------------------------------ learned preconditioner */
 
@@ -199,6 +218,13 @@ int fos_ilut_factor_dev(fos_ilut* f, const int* ia, const int* ja, const double*
 int fos_ilut_solve_dev(fos_ilut* f, const double* y, double* x, void* stream);
 /* after the stream has drained: 0, or -6 when a solve's dependency wait ran out */
 int fos_ilut_status(fos_ilut* f);
+/* Failure injection (tests of the bounded waits; no counterpart in the reference): every
+ * dependency wait of the following factor and solve calls gives up after `polls` polls
+ * (<= 0: the default 2^23), and row `withhold_row` (>= 0) is never published -- the factor
+ * does not release it and the forward sweep does not store its unknown -- so every wait on
+ * it runs out: fos_ilut_factor_dev returns -6 and a solve leaves fos_ilut_status at -6 with
+ * NaN in the rows that waited.  withhold_row = -1 publishes every row again. */
+int fos_ilut_set_wait_limit(fos_ilut* f, long polls, int withhold_row);
 /* the factors in ilut's MSR layout on the host (1-based values): alu(1:n) the inverted
  * diagonal, jlu(1:n+1) row pointers, ju(1:n) the start of each U row; returns the used
  * length (all three pointers null: only the length), < 0 on error */
@@ -228,7 +254,7 @@ typedef struct {
                          falling back to ILU(0) when it stagnates, falls behind the mean
                          residual reduction per iteration of the last ILU(0)-preconditioned
                          solve, or needs more iterations than that solve, after which the next
-                         1, 2, 4, ... 64 solves (doubling per consecutive fallback, reset
+                         1, 4, 16, ... solves (four times more per consecutive fallback, reset
                          when the network converges a solve) use ILU(0) alone; 3 = learned network
                          without fallback (evaluation); 4 = ILU(0) followed by the learned
                          correction, z = u + N(y; u) with u = ILU(0) r, with the fallback
@@ -261,7 +287,8 @@ int fos_linear_solve_dev(fos_ctx* ctx, double t, const double* y, const double* 
                          fos_bdf_stats* stats);
 /* Advance y (device, internal order, 5*nC) by opts->nsteps fixed BDF steps from t0.
  * Returns 0, > 0 if a step failed to converge (1), hit a non-finite residual (2) or a
- * zero pivot (3); < 0 on errors. */
+ * zero pivot (3); < 0 on errors.  A failed step is not taken: y is left at the last
+ * accepted step (time stats->t, stats->n_steps steps taken). */
 int fos_bdf_run(fos_ctx* ctx, double t0, double* y, const fos_bdf_opts* opts,
                 fos_bdf_stats* stats);
 /* Same with y a HOST array in the caller's (reference) cell order: copied to the device,

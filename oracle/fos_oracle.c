@@ -1469,9 +1469,10 @@ int o_bdf_run(int n, o_rhs_fn rhs, o_pset_fn pset, o_psol_fn psol, void* ud, dou
       last_setup = s;
       gamma_setup = gamma;
     }
-    if (nrc) {
+    if (nrc) { /* the failed step is not taken: y goes back to the last accepted state */
       st->fails++;
       status = nrc == 1 ? 1 : nrc;
+      memcpy(y, yn, sizeof(double) * n);
       break;
     }
     memcpy(ynm1, yn, sizeof(double) * n);

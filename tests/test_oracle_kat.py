@@ -292,3 +292,27 @@ def test_tuned_build_is_bit_identical():
     assert np.array_equal(out[0][0], out[1][0])
     assert np.array_equal(out[0][1], out[1][1])
     assert out[0][2] == out[1][2]
+
+
+def test_failed_step_keeps_last_accepted_state():
+    """A BDF step whose Newton iteration fails (GMRES(1) without restarts or preconditioner,
+    an unreachable linear tolerance, two Newton iterations, the supersonic bump at CFL ~5) is
+    not taken: the driver returns 1 and y is the last accepted state."""
+    from fosolvers_gb300 import mesh as M
+    wl = M.make_workload("bump192", scale=8)
+    g = O.grid_build(wl.mesh)
+    e = O.Euler(g, M.ibc_for(wl.mesh, wl.bc_gid), wl.bc_type, wl.bc_param, wl.gamm, wl.r,
+                wl.elem_state)
+    y0 = M.soa(wl.elem_state, g["nC"])
+    rhs, pset, psol = e.callbacks()
+    y = y0.copy()
+    rc, st = O.bdf_run(y.size, rhs, pset, psol, e.h, y,
+                       O.bdf_defaults(order=1, dt=wl.dt, nsteps=2, maxl=1, max_restarts=0,
+                                      lin_rtol=1e-30, max_newton=2, use_prec=0))
+    assert rc == 1 and st["n_steps"] == 0 and st["fails"] == 1 and st["n_newton"] == 2
+    assert np.array_equal(y, y0)
+    # the same context advances normally afterwards
+    rc, st = O.bdf_run(y.size, rhs, pset, psol, e.h, y,
+                       O.bdf_defaults(order=1, dt=wl.dt, nsteps=1))
+    assert rc == 0 and st["n_steps"] == 1
+    e.close()

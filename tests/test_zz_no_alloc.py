@@ -40,12 +40,24 @@ def test_static_scratch_residual_matches_rhs_dev(cuda, flags, name):
         assert rel_err(a, b) <= 1e-11
 
 
-def test_static_scratch_refuses_large_grid(cuda):
+@pytest.mark.parametrize("grid", ["cells", "faces"])
+def test_static_scratch_refuses_large_grid(cuda, grid):
+    """Two limits: 65,536 cells (a 24^3 x 6 tetrahedral box has 82,944) and 147,456 faces (a
+    38^3 hexahedral box has 54,872 cells, under the cell limit, and 168,948 faces)."""
     import torch
     from fosolvers_gb300 import _lib
-    c = Case(M.make_workload("sine96", scale=24, seed=5))  # 82,944 cells > 65,536
+    if grid == "cells":
+        c = Case(M.make_workload("sine96", scale=24, seed=5))
+    else:
+        m = M.box_mesh(38, 38, 38, jitter=0.1, seed=5, cells="hex")
+        st = M.sine_state(m.centroids(), 5)
+        c = Case(M.Workload("hex38", m, st, np.zeros(0, np.int32), np.zeros(0, np.int32),
+                            np.zeros((0, 5)), order=2, dt=5e-4, nsteps=1))
+        assert c.nC <= 65536 and c.grid.nP > 147456
     y = torch.zeros(c.N, dtype=torch.float64, device="cuda")
     out = torch.zeros_like(y)
     rc = _lib.lib().fos_euler_rhs_dev_static(c.gpu.handle, 0.0, y.data_ptr(), out.data_ptr())
     assert rc == -1
-    assert "at most 65536 cells" in _lib.last_error()
+    msg = _lib.last_error()
+    assert "at most 65536 cells and 147456 faces" in msg
+    assert (f"{c.nC} cells" in msg) and (f"{c.grid.nP} faces" in msg)
