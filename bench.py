@@ -49,7 +49,7 @@ GNN_BYTES_PER_CELL = 120 + 216 + 3 * 368 + 208
 # the operation's kernels, L2 flushed before every kernel, so an upper bound); traffic
 # grows with the cell count, so the full-size figure is this times nC.  Summary and
 # command: profiles/traffic_sine64_fp32.md
-TRAFFIC_FP32_BYTES_PER_CELL = {"residual": 235.0, "jv": 403.1, "pset": 2214.1,
+TRAFFIC_FP32_BYTES_PER_CELL = {"residual": 235.0, "jv": 403.1,
                                "ilu_apply": 800.0, "gnn_apply": 1162.1}
 
 
@@ -634,13 +634,21 @@ def main():
         #   ILU apply the factors (25 values per block) + r in / z out (80 per cell)
         #   pset      state in, geometry, J written, J read and LU written by the factor
         gb = 8 + (16 if args.mode in ("fp32", "fp32h") else 32)
+        #   pset      FP32 factors (fused set-up: J assembled inside the factor, never stored):
+        #             state in (40 per cell), face pair and geometry, the factors written
+        #             (25 values per block), and every inv(D_q) and U_qp block read once by the
+        #             rows below it (one per cell and one per interior face);
+        #             FP64: state, geometry, J written, J read and the factors written
+        if fb == 4:
+            pset_bytes = 40 * a_ + gb * f_ + 25 * fb * nnzb + 25 * fb * (a_ + grid.nPi)
+        else:
+            pset_bytes = 48 * a_ + gb * f_ + 3 * 25 * fb * nnzb
         ops = {
             "residual": {"ms": t_rhs, "bytes": 88 * a_ + gb * f_, "count": st["n_rhs"] - st["n_jv"]},
             "jv": {"ms": t_jv, "bytes": 168 * a_ + gb * f_, "count": st["n_jv"]},
             "ilu_apply": {"ms": t_psol, "bytes": 25 * fb * nnzb + 80 * a_,
                           "count": st["n_psol"] - n_gnn, "levels": lev},
-            "pset": {"ms": t_pset, "bytes": 48 * a_ + gb * f_ + 3 * 25 * fb * nnzb,
-                     "count": st["n_pset"]},
+            "pset": {"ms": t_pset, "bytes": pset_bytes, "count": st["n_pset"]},
         }
         if gnn is not None:
             t_gnn = timeit(lambda: gnn.apply_dev(ctx, y, v, out, gamma), R)

@@ -33,7 +33,8 @@ fos_ctx::~fos_ctx() {
                   d_bcT, d_bcP, d_W, d_Whl, d_ell, d_F, d_stage, d_y, d_f, d_z, d_red, d_scal,
                   d_flag, d_prow, d_pcol, d_pdiag, d_cdiag, d_ipos, d_ord, d_fslot, d_Jraw,
                   d_LU, d_LU32, d_lrows_f, d_lrows_b, d_upd_ptr, d_upd, d_ilu_tmp, d_Jb, d_ierr,
-                  d_closure32, d_pia, d_pja, d_pa, d_vol, d_ilut_x, d_plst, d_pdu, d_fsel};
+                  d_closure32, d_pia, d_pja, d_pa, d_vol, d_ilut_x, d_plst, d_pdu, d_fsel,
+                  d_yJ};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h_scal) cudaFreeHost(h_scal);
@@ -534,6 +535,21 @@ extern "C" int fos_euler_pset_dev(fos_ctx* c, double t, const double* y, int jok
   }
   int rc = fos_jac_setup(c);
   if (rc) return rc;
+  if (fos_pset_is_fused(c)) {
+    // J is assembled inside the factor; jok = 1 reassembles it from the state of the last
+    // jok = 0 call (the same J, bit for bit), or factors the caller's J (fos_euler_jac_set)
+    if (jok == 0 || !c->has_jac) {
+      FOS_CUDA(cudaMemcpyAsync(c->d_yJ, y, 5 * sizeof(double) * (size_t)c->nC,
+                               cudaMemcpyDeviceToDevice, c->stream));
+      c->has_jac = true;
+      c->jraw_valid = false;
+      c->jac_user = false;
+      if (jcur) *jcur = 1;
+      return fos_pset_fused(c, y, gamma);
+    }
+    if (jcur) *jcur = 0;
+    return c->jac_user ? fos_ilu_factor(c, gamma) : fos_pset_fused(c, c->d_yJ, gamma);
+  }
   if (jok == 0 || !c->has_jac) {
     rc = fos_jac_assemble(c, y);
     if (rc) return rc;

@@ -97,7 +97,11 @@ struct fos_ctx {
   void* d_Jraw = nullptr;     // [25*nnzb] unscaled Jacobian blocks (FP64, FP32 for FOS_ILU_FP32)
   void* d_Jb = nullptr;       // [25*nFb] boundary-face diagonal terms (same type)
   int* d_ierr = nullptr;
-  bool has_jac = false;
+  bool has_jac = false;       // a Jacobian exists for pset(jok = 1): in d_Jraw, or (the fused
+                              // FP32 set-up) as the state d_yJ it is assembled from
+  bool jraw_valid = false;    // d_Jraw holds that Jacobian
+  bool jac_user = false;      // d_Jraw came from fos_euler_jac_set (factored from d_Jraw)
+  double* d_yJ = nullptr;     // [5*nC] fused set-up: the state of the last assembly (jok = 0)
   // factors in two regions, so that each sweep streams one: the L blocks of every row (by
   // position), then the diagonal block and the U blocks of every row; diag blocks hold the
   // inverse; 25 entries per block, column-major.  Block storage of slot s in row p:
@@ -168,6 +172,9 @@ int fos_gnn_precond(fos_ctx* c, const double* y, const double* r, double gamma, 
 // fos_jacobian.cu
 int fos_jac_setup(fos_ctx* c);
 int fos_jac_assemble(fos_ctx* c, const double* y);
+// FP32 block ILU(0) without ILUT: pset assembles J inside the factor (k_pset32)
+bool fos_pset_is_fused(const fos_ctx* c);
+int fos_pset_fused(fos_ctx* c, const double* y, double gamma);
 int fos_ilu_factor(fos_ctx* c, double gamma);
 // z = P^-1 r; with d_zsq also ||z||^2 into d_zsq (device), from the same pass over z
 int fos_ilu_apply(fos_ctx* c, const double* r, double* z, double* d_zsq = nullptr);

@@ -242,6 +242,88 @@ __device__ __forceinline__ PrimT<float> load_prim_f32(const float* __restrict__ 
 // evaluated by both of its cells: FP32 arithmetic is cheap next to the scattered block
 // stores and the re-read of every off-diagonal block that a face-then-diagonal assembly
 // costs.
+// One block row of the FP32 Jacobian for cell c (the body of k_jac_cell32, shared with the
+// fused set-up k_pset32): the row's blocks go to st (row-major 25-float blocks at
+// st + 25 (slot - s0)); sdiag = the diagonal block's slot - s0.  The multiply-adds are
+// written out (fmaf), so both kernels produce the same bits.
+template <int kW>
+__device__ __forceinline__ void jac_row32(int c, int nFi, int s0, int sdiag,
+                                          const int* __restrict__ ell,
+                                          const int2* __restrict__ faceLR,
+                                          const float4* __restrict__ faceNA32,
+                                          const int* __restrict__ fslot,
+                                          const float* __restrict__ Whl,
+                                          const double* __restrict__ Gb,
+                                          const float4* __restrict__ Sc, float gg,
+                                          float* __restrict__ st) {
+  const PrimT<float> P = load_prim_f32(Whl, c);
+  float D[25];
+#pragma unroll
+  for (int k = 0; k < 25; k++) D[k] = 0.0f;
+#pragma unroll 1
+  for (int k = 0; k < kW; k++) {
+    const int ek = __ldg(ell + (size_t)kW * c + k);
+    if (ek < 0) continue;
+    const int f = ek >> 1;
+    const bool isR = ek & 1;
+    const int2 lr = __ldg(faceLR + f);
+    const float4 na = __ldg(faceNA32 + f);
+    const float n[3] = {na.x, na.y, na.z};
+    PrimT<float> Q;
+    if (f < nFi) {
+      Q = load_prim_f32(Whl, isR ? lr.x : lr.y);
+    } else {  // ghost primitives of k_jac_ghost64
+      const double2* G2 = reinterpret_cast<const double2*>(Gb + 6 * (size_t)f);
+      const double2 a0 = __ldg(G2), a1 = __ldg(G2 + 1), a2 = __ldg(G2 + 2);
+      Q = {{d2f_trunc(a0.x), d2f_trunc(a0.y), d2f_trunc(a1.x)}, d2f_trunc(a1.y),
+           d2f_trunc(a2.x)};
+    }
+    const PrimT<float>& L = (f < nFi && isR) ? Q : P;
+    const PrimT<float>& R = (f < nFi && isR) ? P : Q;
+    const float inv = 1.0f / (L.s + R.s);
+    const float ua[3] = {(L.s * L.u[0] + R.s * R.u[0]) * inv, (L.s * L.u[1] + R.s * R.u[1]) * inv,
+                         (L.s * L.u[2] + R.s * R.u[2]) * inv};
+    const float Ha = (L.s * L.H + R.s * R.H) * inv;
+    const float ca =
+        sqrtf((gg - 1.0f) * (Ha - 0.5f * (ua[0] * ua[0] + ua[1] * ua[1] + ua[2] * ua[2])));
+    float Ab[25];
+    anfj<float>(n, ua, Ha, ca, gg, Ab);
+    const float h = 0.5f * na.w;
+    if (f >= nFi) {  // boundary pair: diagonal term only (its A(u_c) part is in S_c)
+#pragma unroll
+      for (int q = 0; q < 25; q++) D[q] = fmaf(-h, Ab[q], D[q]);
+      continue;
+    }
+    // the neighbour's normal flux Jacobian with the face normal: +aP/2 for cell R, -aP/2 for L
+    const float v2Q = Q.u[0] * Q.u[0] + Q.u[1] * Q.u[1] + Q.u[2] * Q.u[2];
+    const float vnQ = Q.u[0] * n[0] + Q.u[1] * n[1] + Q.u[2] * n[2];
+    const float sh = isR ? h : -h;
+    float* off = st + 25 * (fslot[2 * f + (isR ? 1 : 0)] - s0);
+#pragma unroll
+    for (int a = 0; a < 5; a++)
+#pragma unroll
+      for (int b = 0; b < 5; b++) {
+        off[5 * a + b] =
+            fmaf(h, Ab[5 * a + b], __fmul_rn(sh, nfj<float>(a, b, n, Q.u, Q.H, gg, v2Q, vnQ)));
+        D[5 * a + b] = fmaf(-h, Ab[5 * a + b], D[5 * a + b]);
+      }
+  }
+  if (Sc) {  // -A(S_c/2; u_c): the own-state terms of a cell whose faces do not close
+    const float4 S4 = __ldg(Sc + c);
+    const float Sh[3] = {0.5f * S4.x, 0.5f * S4.y, 0.5f * S4.z};
+    const float v2P = P.u[0] * P.u[0] + P.u[1] * P.u[1] + P.u[2] * P.u[2];
+    const float vnP = P.u[0] * Sh[0] + P.u[1] * Sh[1] + P.u[2] * Sh[2];
+#pragma unroll
+    for (int a = 0; a < 5; a++)
+#pragma unroll
+      for (int b = 0; b < 5; b++)
+        D[5 * a + b] = __fsub_rn(D[5 * a + b], nfj<float>(a, b, Sh, P.u, P.H, gg, v2P, vnP));
+  }
+  float* dg = st + 25 * sdiag;
+#pragma unroll
+  for (int k = 0; k < 25; k++) dg[k] = D[k];
+}
+
 template <int kW>
 __global__ void __launch_bounds__(64) k_jac_cell32(
     int nC, int nFi, const int* __restrict__ ipos, const int* __restrict__ prow,
@@ -259,71 +341,8 @@ __global__ void __launch_bounds__(64) k_jac_cell32(
     const int p = ipos[c];
     s0 = prow[p];
     nbk = prow[p + 1] - s0;
-    const float gg = d2f_trunc(g);
-    const PrimT<float> P = load_prim_f32(Whl, c);
-    float D[25];
-#pragma unroll
-    for (int k = 0; k < 25; k++) D[k] = 0.0f;
-#pragma unroll 1
-    for (int k = 0; k < kW; k++) {
-      const int ek = __ldg(ell + (size_t)kW * c + k);
-      if (ek < 0) continue;
-      const int f = ek >> 1;
-      const bool isR = ek & 1;
-      const int2 lr = __ldg(faceLR + f);
-      const float4 na = __ldg(faceNA32 + f);
-      const float n[3] = {na.x, na.y, na.z};
-      PrimT<float> Q;
-      if (f < nFi) {
-        Q = load_prim_f32(Whl, isR ? lr.x : lr.y);
-      } else {  // ghost primitives of k_jac_ghost64
-        const double2* G2 = reinterpret_cast<const double2*>(Gb + 6 * (size_t)f);
-        const double2 a0 = __ldg(G2), a1 = __ldg(G2 + 1), a2 = __ldg(G2 + 2);
-        Q = {{d2f_trunc(a0.x), d2f_trunc(a0.y), d2f_trunc(a1.x)}, d2f_trunc(a1.y),
-             d2f_trunc(a2.x)};
-      }
-      const PrimT<float>& L = (f < nFi && isR) ? Q : P;
-      const PrimT<float>& R = (f < nFi && isR) ? P : Q;
-      const float inv = 1.0f / (L.s + R.s);
-      const float ua[3] = {(L.s * L.u[0] + R.s * R.u[0]) * inv, (L.s * L.u[1] + R.s * R.u[1]) * inv,
-                           (L.s * L.u[2] + R.s * R.u[2]) * inv};
-      const float Ha = (L.s * L.H + R.s * R.H) * inv;
-      const float ca =
-          sqrtf((gg - 1.0f) * (Ha - 0.5f * (ua[0] * ua[0] + ua[1] * ua[1] + ua[2] * ua[2])));
-      float Ab[25];
-      anfj<float>(n, ua, Ha, ca, gg, Ab);
-      const float h = 0.5f * na.w;
-      if (f >= nFi) {  // boundary pair: diagonal term only (its A(u_c) part is in S_c)
-#pragma unroll
-        for (int k = 0; k < 25; k++) D[k] -= h * Ab[k];
-        continue;
-      }
-      // the neighbour's normal flux Jacobian with the face normal: +aP/2 for cell R, -aP/2 for L
-      const float v2Q = Q.u[0] * Q.u[0] + Q.u[1] * Q.u[1] + Q.u[2] * Q.u[2];
-      const float vnQ = Q.u[0] * n[0] + Q.u[1] * n[1] + Q.u[2] * n[2];
-      const float sh = isR ? h : -h;
-      float* off = st + 25 * (fslot[2 * f + (isR ? 1 : 0)] - s0);
-#pragma unroll
-      for (int a = 0; a < 5; a++)
-#pragma unroll
-        for (int b = 0; b < 5; b++) {
-          off[5 * a + b] = sh * nfj<float>(a, b, n, Q.u, Q.H, gg, v2Q, vnQ) + h * Ab[5 * a + b];
-          D[5 * a + b] -= h * Ab[5 * a + b];
-        }
-    }
-    if (Sc) {  // -A(S_c/2; u_c): the own-state terms of a cell whose faces do not close
-      const float4 S4 = __ldg(Sc + c);
-      const float Sh[3] = {0.5f * S4.x, 0.5f * S4.y, 0.5f * S4.z};
-      const float v2P = P.u[0] * P.u[0] + P.u[1] * P.u[1] + P.u[2] * P.u[2];
-      const float vnP = P.u[0] * Sh[0] + P.u[1] * Sh[1] + P.u[2] * Sh[2];
-#pragma unroll
-      for (int a = 0; a < 5; a++)
-#pragma unroll
-        for (int b = 0; b < 5; b++) D[5 * a + b] -= nfj<float>(a, b, Sh, P.u, P.H, gg, v2P, vnP);
-    }
-    float* dg = st + 25 * (cdiag[c] - s0);
-#pragma unroll
-    for (int k = 0; k < 25; k++) dg[k] = D[k];
+    jac_row32<kW>(c, nFi, s0, cdiag[c] - s0, ell, faceLR, faceNA32, fslot, Whl, Gb, Sc,
+                  d2f_trunc(g), st);
   }
   __syncwarp();
   // the warp's rows, one after another: row r = [25 s0_r, 25 (s0_r + nbk_r)) of J
@@ -470,7 +489,7 @@ __global__ void __launch_bounds__(kT) k_ilu_factor(
       const bool dg = (s0 + b) == sd;
 #pragma unroll
       for (int k = 0; k < 5; k++)
-        sm(lrow, b)[5 * a + k] = ((dg && k == a) ? TF(1) : TF(0)) - sc * (TF)src[k];
+        sm(lrow, b)[5 * a + k] = fma(-sc, (TF)src[k], (dg && k == a) ? TF(1) : TF(0));
     }
   }
   __syncwarp();  // the five lanes of a row see each other's operand rows
@@ -523,6 +542,117 @@ __global__ void __launch_bounds__(kT) k_ilu_factor(
     TF* dst = LU + 25 * (size_t)(b < nl ? bl + b : bdu + (b - nl)) + a;  // row a, column-major
 #pragma unroll
     for (int k = 0; k < 5; k++) dst[5 * k] = sm(lrow, b)[5 * a + k];
+  }
+}
+
+// Fused FP32 set-up: one level (colour) of the block ILU(0) factorisation of
+// P = I - gamma diag(1/v) J with the rows of J assembled in the same kernel, so J is never
+// written to or read back from HBM.  A warp takes 32 rows of the level:
+//   A. thread per row: the row's Jacobian blocks (jac_row32, the arithmetic of k_jac_cell32)
+//      staged in shared memory, then P = delta - (gamma/v) J in place (the same fmaf as
+//      k_ilu_factor, so the factors equal the two-kernel path's bit for bit);
+//   B. five lanes per row, six rows at a time (k_ilu_factor's scheme): the update operations
+//      with the finished rows of earlier levels (inv(D_q), U_qj from LU), the Gauss--Jordan
+//      inverse of the diagonal block across the row's five lanes, and the column-major stores
+//      into the L and D/U regions.
+template <int kW>
+__global__ void __launch_bounds__(64) k_pset32(
+    int n, const int* __restrict__ rows, int p0, const int* __restrict__ prow,
+    const int* __restrict__ pdiag, const int* __restrict__ ord, const double* __restrict__ invV,
+    double gamma, int nFi, const int* __restrict__ ell, const int2* __restrict__ faceLR,
+    const float4* __restrict__ faceNA32, const int* __restrict__ fslot,
+    const float* __restrict__ Whl, const double* __restrict__ Gb, const float4* __restrict__ Sc,
+    double g, const int* __restrict__ upd_ptr, const int3* __restrict__ upd,
+    const int* __restrict__ plst, const int* __restrict__ pdu, float* __restrict__ LU,
+    int* __restrict__ ierr) {
+  constexpr int kRow = (kW + 1) * 25;
+  __shared__ float stg[2][32][kRow];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int t0 = (blockIdx.x * 2 + warp) * 32;  // first row of the warp within the level
+  const int t = t0 + lane;
+  // A: this lane's row
+  int p = 0, s0 = 0, nb = 0, sd = 0;
+  if (t < n) {
+    p = rows ? rows[t] : p0 + t;
+    s0 = prow[p];
+    nb = prow[p + 1] - s0;
+    sd = pdiag[p] - s0;
+    const int c = ord[p];
+    float* st = stg[warp][lane];
+    jac_row32<kW>(c, nFi, s0, sd, ell, faceLR, faceNA32, fslot, Whl, Gb, Sc, d2f_trunc(g), st);
+    const float sc = d2f_trunc(gamma * invV[c]);
+    for (int b = 0; b < nb; b++) {
+      float* blk = st + 25 * b;
+#pragma unroll
+      for (int k = 0; k < 25; k++)
+        blk[k] = fmaf(-sc, blk[k], (b == sd && k % 6 == 0) ? 1.0f : 0.0f);
+    }
+  }
+  __syncwarp();
+  // B: rows r0 .. r0 + 5 of the warp, five lanes each (lane a owns row a of every block)
+  const int sub = lane / 5, a = lane - 5 * sub;
+  for (int r0 = 0; r0 < 32; r0 += 6) {
+    const int r = r0 + sub;
+    const int src = (sub < 6 && r < 32) ? r : 0;
+    const int pr = __shfl_sync(0xffffffffu, p, src);
+    const int s0r = __shfl_sync(0xffffffffu, s0, src);
+    const int nbr = __shfl_sync(0xffffffffu, nb, src);
+    const int sdr = __shfl_sync(0xffffffffu, sd, src);
+    const bool active = sub < 6 && r < 32 && t0 + r < n;
+    float* st = stg[warp][src];
+    float D[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    if (active) {
+      const int o0 = upd_ptr[pr], o1 = upd_ptr[pr + 1];
+      for (int o = o0; o < o1; o++) {
+        const int3 op = upd[o];
+        float A[5];
+        const float* Ar = st + 25 * (op.x - s0r) + 5 * a;
+#pragma unroll
+        for (int k = 0; k < 5; k++) A[k] = Ar[k];
+        const float* B = LU + 25 * (size_t)op.y;  // column-major, finished in earlier levels
+        float* dst = st + 25 * ((op.z < 0 ? op.x : op.z) - s0r) + 5 * a;
+#pragma unroll
+        for (int b = 0; b < 5; b++) {
+          float acc = 0.0f;
+#pragma unroll
+          for (int k = 0; k < 5; k++) acc += A[k] * __ldg(B + 5 * b + k);
+          dst[b] = op.z < 0 ? acc : dst[b] - acc;
+        }
+      }
+#pragma unroll
+      for (int b = 0; b < 5; b++) D[b] = st[25 * sdr + 5 * a + b];
+    }
+    const int base = lane - a;
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+      float rk[5];
+#pragma unroll
+      for (int b = 0; b < 5; b++) rk[b] = __shfl_sync(0xffffffffu, D[b], base + k < 32 ? base + k : 0);
+      const float piv = rk[k];
+      ok &= !(active && piv == 0.0f);
+      const float ip = 1.0f / piv;
+      if (a == k) {
+#pragma unroll
+        for (int b = 0; b < 5; b++) D[b] = (b == k) ? ip : D[b] * ip;
+      } else {
+        const float f = D[k];
+#pragma unroll
+        for (int b = 0; b < 5; b++) D[b] = (b == k) ? -f * ip : D[b] - f * (rk[b] * ip);
+      }
+    }
+    if (active) {
+      if (!ok) atomicMin(ierr, pr + 1);
+#pragma unroll
+      for (int b = 0; b < 5; b++) st[25 * sdr + 5 * a + b] = D[b];
+      const int bl = plst[pr], bdu = pdu[pr];
+      for (int b = 0; b < nbr; b++) {
+        float* dst = LU + 25 * (size_t)(b < sdr ? bl + b : bdu + (b - sdr)) + a;
+#pragma unroll
+        for (int k = 0; k < 5; k++) dst[5 * k] = st[25 * b + 5 * a + k];
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -856,7 +986,10 @@ int fos_jac_setup(fos_ctx* c) {
   if (!rows_f.empty() && (up(&c->d_lrows_f, rows_f) || up(&c->d_lrows_b, rows_b))) return -100;
   const bool f32 = (c->flags & FOS_ILU_FP32) != 0;
   const size_t jb = f32 ? sizeof(float) : sizeof(double);
-  FOS_CUDA(cudaMalloc((void**)&c->d_Jraw, 25 * jb * (size_t)c->nnzb));
+  if (fos_pset_is_fused(c))  // J is assembled inside the factor; only its state is kept
+    FOS_CUDA(cudaMalloc((void**)&c->d_yJ, 5 * sizeof(double) * (size_t)nC));
+  else
+    FOS_CUDA(cudaMalloc((void**)&c->d_Jraw, 25 * jb * (size_t)c->nnzb));
   FOS_CUDA(cudaMalloc((void**)&c->d_Jb, 25 * jb * (size_t)std::max(c->nFb, 1)));
   FOS_CUDA(cudaMalloc((void**)&c->d_ilu_tmp, 16 * sizeof(double) * (size_t)nC));  // 2 AoS vectors
   FOS_CUDA(cudaMalloc((void**)&c->d_ierr, sizeof(int)));
@@ -867,8 +1000,22 @@ int fos_jac_setup(fos_ctx* c) {
   return 0;
 }
 
+bool fos_pset_is_fused(const fos_ctx* c) {
+  return (c->flags & FOS_ILU_FP32) && !(c->flags & FOS_PREC_ILUT);
+}
+
+// storage for J on the fused path, made when J is first asked for (fos_euler_jac_copy /
+// fos_euler_jac_set)
+static int ensure_jraw(fos_ctx* c) {
+  if (c->d_Jraw) return 0;
+  const size_t jb = (c->flags & FOS_ILU_FP32) ? sizeof(float) : sizeof(double);
+  FOS_CUDA(cudaMalloc((void**)&c->d_Jraw, 25 * jb * (size_t)c->nnzb));
+  return 0;
+}
+
 template <typename TJ>
 static int jac_assemble_t(fos_ctx* c, const double* y) {
+  if (int rc = ensure_jraw(c)) return rc;
   TJ* J = reinterpret_cast<TJ*>(c->d_Jraw);
   TJ* Jb = reinterpret_cast<TJ*>(c->d_Jb);
   if constexpr (sizeof(TJ) == sizeof(float)) {
@@ -912,6 +1059,39 @@ int fos_jac_assemble(fos_ctx* c, const double* y) {
                                            : jac_assemble_t<double>(c, y);
   if (rc) return rc;
   c->has_jac = true;
+  c->jraw_valid = true;
+  return 0;
+}
+
+// The fused FP32 set-up: primitives and boundary ghosts of y, then one k_pset32 launch per
+// level (colour) -- J assembled row by row inside the factor, never stored.
+int fos_pset_fused(fos_ctx* c, const double* y, double gamma) {
+  if (int rc = fos_prim_hl_launch(c, y)) return rc;
+  if (c->nFb)
+    fos_launch(c, k_jac_ghost64, nb(c->nFb), kT, c->nFi, c->nF, c->nC, (const int2*)c->d_faceLR,
+               (const float4*)c->d_faceNA32, y, (const int*)c->d_bcT, (const double*)c->d_bcP,
+               c->maxP, c->gamm, c->r, c->d_F);
+  const int big = 0x7fffffff;
+  FOS_CUDA(cudaMemcpyAsync(c->d_ierr, &big, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  for (int l = 0; l < c->ilu_nlev_f; l++) {
+    const int n = c->lev_f[l + 1] - c->lev_f[l];
+    const int* rows = c->d_lrows_f ? c->d_lrows_f + c->lev_f[l] : nullptr;
+    auto k = c->ell_w == 4 ? k_pset32<4> : k_pset32<6>;
+    fos_launch(c, k, (n + 63) / 64, 64, n, rows, c->lev_f[l], (const int*)c->d_prow,
+               (const int*)c->d_pdiag, (const int*)c->d_ord, (const double*)c->d_invV, gamma,
+               c->nFi, (const int*)c->d_ell, (const int2*)c->d_faceLR,
+               (const float4*)c->d_faceNA32, (const int*)c->d_fslot, (const float*)c->d_Whl,
+               (const double*)c->d_F, (const float4*)c->d_closure32, c->gamm,
+               (const int*)c->d_upd_ptr, (const int3*)c->d_upd, (const int*)c->d_plst,
+               (const int*)c->d_pdu, c->d_LU32, c->d_ierr);
+  }
+  FOS_LAUNCH_CHECK();
+  int* h = (int*)c->h_scal;
+  FOS_CUDA(cudaMemcpyAsync(h, c->d_ierr, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  FOS_CUDA(cudaStreamSynchronize(c->stream));
+  c->ilu_ierr = (*h == big) ? 0 : *h;  // 1-based position of the first zero pivot
+  c->has_factor = true;
+  if (c->ilu_ierr) fos_set_error("block ILU(0): zero pivot");
   return 0;
 }
 
@@ -1005,6 +1185,10 @@ extern "C" long fos_euler_jac_copy(fos_ctx* c, int* rowptr, int* col, double* va
       fos_set_error("fos_euler_jac_copy: no Jacobian assembled yet");
       return -2;
     }
+    if (!c->jraw_valid) {  // fused set-up: assemble J of the last set-up's state now
+      if (jac_assemble_t<float>(c, c->d_yJ)) return -100;
+      c->jraw_valid = true;
+    }
     const size_t n = 25 * (size_t)c->nnzb;
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
       fos_set_error("fos_euler_jac_copy: stream error");
@@ -1039,6 +1223,7 @@ extern "C" int fos_euler_jac_set(fos_ctx* c, const double* val) {
     return -1;
   }
   if (int rc = fos_jac_setup(c)) return rc;
+  if (int rc = ensure_jraw(c)) return rc;
   const size_t n = 25 * (size_t)c->nnzb;
   FOS_CUDA(cudaStreamSynchronize(c->stream));
   if (c->flags & FOS_ILU_FP32) {
@@ -1049,6 +1234,8 @@ extern "C" int fos_euler_jac_set(fos_ctx* c, const double* val) {
     FOS_CUDA(cudaMemcpy(c->d_Jraw, val, n * sizeof(double), cudaMemcpyHostToDevice));
   }
   c->has_jac = true;
+  c->jraw_valid = true;
+  c->jac_user = true;
   return 0;
 }
 

@@ -90,7 +90,7 @@ def _duct_case(tmp_path, t_final, t_int):
     reference ships them, from tests/golden/duct.npz) with the run control shortened."""
     from test_meshio import write_duct_case
     case = write_duct_case(tmp_path / "duct")
-    (case / "sim").write_text(f"{t_final!r}  # final time [s]\n{t_int!r}  # output interval [s]\n")
+    (case / "sim").write_text(f"{float(t_final)!r}  # final time [s]\n{float(t_int)!r}  # output interval [s]\n")
     return case
 
 

@@ -127,3 +127,29 @@ def test_fp32_ilu_apply(cuda, name, extra):
     c.oracle.psol(0.0, None, None, r, z_ref, 5e-3)
     c.gpu.psol(0.0, y, None, r, z, 5e-3)
     assert rel_err(z, z_ref) <= 1e-5
+
+
+@pytest.mark.parametrize("name,extra", [("sine8", ILU_COLOR), ("sine8", 0), ("hex8", ILU_COLOR),
+                                        ("conds6", ILU_COLOR)])
+def test_fused_fp32_setup_equals_two_kernel_path(cuda, name, extra):
+    """The FP32 set-up assembles J inside the factor (k_pset32) and never stores it.  Its
+    factors must equal the two-kernel path's (k_jac_cell32 writes J, k_ilu_factor factors it)
+    bit for bit: J is materialised with fos_euler_jac_copy, loaded back with fos_euler_jac_set
+    and factored by pset(jok = 1) through the two-kernel path; both applies must agree
+    exactly.  jok = 1 without a loaded J reassembles J from the state of the last jok = 0
+    call, so a second state passed with jok = 1 must not change the factors either."""
+    c = Case(_workload(name), flags=ILU_FP32 | extra)
+    y = perturbed(c.y0, c.nC, 7)
+    g = 4e-3
+    assert c.gpu.pset(0.0, y, None, 0, g) == (0, 1)
+    r = np.random.default_rng(3).normal(size=c.N)
+    z_fused, z_reuse, z_two = (np.zeros_like(r) for _ in range(3))
+    assert c.gpu.psol(0.0, y, None, r, z_fused, g) == 0
+    assert c.gpu.pset(0.0, 1.5 * y, None, 1, g) == (0, 0)  # J of y, not of 1.5 y
+    assert c.gpu.psol(0.0, y, None, r, z_reuse, g) == 0
+    assert np.array_equal(z_fused, z_reuse)
+    rowptr, col, val = c.gpu.jacobian()
+    c.gpu.set_jacobian(val)
+    assert c.gpu.pset(0.0, y, None, 1, g) == (0, 0)
+    assert c.gpu.psol(0.0, y, None, r, z_two, g) == 0
+    assert np.array_equal(z_fused, z_two)
