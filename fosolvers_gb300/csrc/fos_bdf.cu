@@ -21,6 +21,22 @@
 #include "fos_internal.h"
 
 
+// Default scale of the finite-difference increment s = eps (1 + ||y||)/||v||.
+// FP64 flux: sqrt(DBL_EPSILON), the classic balance of truncation against rounding.
+// FP32 flux: 1e-5.  The flux-difference form rounds each face term relative to the face's
+// jump, not to the state, so the rounding noise of f is about FLT_EPSILON times the relative
+// jump between neighbours (1e-3 to 1e-2 on these meshes) and the balancing increment is
+// near 1e-5.  sqrt(FLT_EPSILON) = 3.5e-4 is too large: s v is a global perturbation of l2
+// norm eps (1 + ||y||), so on a Krylov vector concentrated on K of N unknowns (a shock) each
+// of them moves by eps ||y|| / sqrt(K), sqrt(N/K) times more than on a spread-out vector,
+// and the difference quotient leaves its linear range.  Measured: on the 2.36 M-tet bump at
+// CFL 5 the Newton iteration diverged at 3.5e-4 (FP32 and FP64 flux alike) and converged at
+// 1e-4 and below; on the 5.3 M-tet sine workload 1e-5 takes the FP64 path's Newton and
+// Krylov counts (10 and 26 over five steps, against 11 and 29 at 3.5e-4).
+static double jv_eps_default(const fos_ctx* c) {
+  return (c->flags & FOS_FLUX_FP32) ? 1e-5 : std::sqrt(DBL_EPSILON);
+}
+
 namespace {
 
 constexpr int kT = 256;
@@ -649,9 +665,7 @@ extern "C" int fos_bdf_run(fos_ctx* c, double t0, double* y, const fos_bdf_opts*
   const long N = wk.N;
   // resume: continue the BDF history of the previous call when y is its result
   const bool resume = opts->resume && wk.has_hist;
-  double eps = opts->jv_eps > 0.0 ? opts->jv_eps
-               : (c->flags & FOS_FLUX_FP32) ? std::sqrt((double)FLT_EPSILON)
-                                            : std::sqrt(DBL_EPSILON);
+  const double eps = opts->jv_eps > 0.0 ? opts->jv_eps : jv_eps_default(c);
   Driver dr{c, wk, *opts, st, eps};
   dr.ilu_ref_its = wk.ilu_ref_its;
   dr.ilu_ref_rate = wk.ilu_ref_rate;
@@ -828,9 +842,7 @@ extern "C" int fos_bdf_adaptive(fos_ctx* c, double t0, double tout, double* y,
   const long N = wk.N;
   const int qmax = ad->qmax;
   const long max_steps = ad->max_steps > 0 ? ad->max_steps : 100000;
-  double eps = nk->jv_eps > 0.0 ? nk->jv_eps
-               : (c->flags & FOS_FLUX_FP32) ? std::sqrt((double)FLT_EPSILON)
-                                            : std::sqrt(DBL_EPSILON);
+  const double eps = nk->jv_eps > 0.0 ? nk->jv_eps : jv_eps_default(c);
   Driver dr{c, wk, *nk, st, eps};
   dr.ilu_ref_its = wk.ilu_ref_its;
   dr.ilu_ref_rate = wk.ilu_ref_rate;
@@ -1009,9 +1021,7 @@ extern "C" int fos_linear_solve_dev(fos_ctx* c, double t, const double* y, const
   if (int rc = work_get(c, opts->maxl, &wkp)) return rc;
   Work& wk = *wkp;
   const long N = wk.N;
-  double eps = opts->jv_eps > 0.0 ? opts->jv_eps
-               : (c->flags & FOS_FLUX_FP32) ? std::sqrt((double)FLT_EPSILON)
-                                            : std::sqrt(DBL_EPSILON);
+  const double eps = opts->jv_eps > 0.0 ? opts->jv_eps : jv_eps_default(c);
   Driver dr{c, wk, *opts, st, eps};
   dr.ilu_ref_its = wk.ilu_ref_its;
   dr.ilu_ref_rate = wk.ilu_ref_rate;

@@ -28,6 +28,7 @@ ORDER_RCM, ORDER_NATURAL = 0, 2
 ILU_FP32, ILU_COLOR = 4, 8
 PREC_ILUT = 16  # pset/psol with ILUT (FP64) instead of block ILU(0)
 FLUX_HYBRID = 32  # with FLUX_FP32: faces with large density / pressure jumps in FP64
+JV_EPS_FP32 = 1e-5  # default finite-difference increment scale of the FP32 flux (the driver's)
 
 
 @dataclass
@@ -185,7 +186,7 @@ class FOEuler:
 
     def jv_dev(self, t, y_dev, fy_dev, v_dev, out_dev, a, b, ynorm, eps=0.0) -> int:
         if eps <= 0.0:
-            eps = float(np.sqrt(np.finfo(np.float32).eps)) if self.flags & FLUX_FP32 \
+            eps = JV_EPS_FP32 if self.flags & FLUX_FP32 \
                 else float(np.sqrt(np.finfo(np.float64).eps))
         return check(_lib.lib().fos_euler_jv_dev(self._h, t, y_dev.data_ptr(), fy_dev.data_ptr(),
                                                  v_dev.data_ptr(), out_dev.data_ptr(), a, b,
@@ -195,7 +196,7 @@ class FOEuler:
                      eps=0.0) -> int:
         """jv_dev with ||v||_2 known to the caller (no reduction pass over v)."""
         if eps <= 0.0:
-            eps = float(np.sqrt(np.finfo(np.float32).eps)) if self.flags & FLUX_FP32 \
+            eps = JV_EPS_FP32 if self.flags & FLUX_FP32 \
                 else float(np.sqrt(np.finfo(np.float64).eps))
         return check(_lib.lib().fos_euler_jv_dev_vnorm(self._h, t, y_dev.data_ptr(),
                                                        fy_dev.data_ptr(), v_dev.data_ptr(),

@@ -249,7 +249,9 @@ typedef struct {
   int maxl;           /* (F)GMRES restart length */
   int max_restarts;
   double lin_rtol;    /* Krylov: ||r|| <= lin_rtol ||b|| */
-  double jv_eps;      /* finite-difference increment scale (sqrt of machine epsilon) */
+  double jv_eps;      /* finite-difference increment scale; 0 = the default: sqrt(DBL_EPSILON)
+                         for the FP64 flux, 1e-5 for the FP32 flux (whose rounding is relative
+                         to the face jumps, not to the state) */
   int precond;        /* 0 = none, 1 = block ILU(0), 2 = learned network in flexible GMRES,
                          falling back to ILU(0) when it stagnates, falls behind the mean
                          residual reduction per iteration of the last ILU(0)-preconditioned
