@@ -65,7 +65,14 @@ __device__ __forceinline__ T nfj(int a, int b, const T n[3], const T u[3], T H, 
   return u[i] * n[j] + (T(1) - g) * n[i] * u[j] + (i == j ? vn : T(0));
 }
 
-// eulerANFJ as |vn| T0 + |vn - c| r- l-^T + |vn + c| r+ l+^T (row-major 25)
+// eulerANFJ (Euler.f90:279-333), row-major 25: |vn| T0 + |vn - c| r- l-^T + |vn + c| r+ l+^T,
+// where the entropy/shear projector T0 equals I - r- l-^T - r+ l+^T plus the reference's
+// entry at :300 (column 1, rows 2:4 hold -(1 + (g-1) M^2/2) u + vn n, i.e. an extra -u
+// against the exact projector).  So
+//   |A~| = |vn| (I + E) + (|vn - c| - |vn|) r- l-^T + (|vn + c| - |vn|) r+ l+^T,
+//   E(1 + i, 0) = -u_i,
+// the same matrix in two rank-1 updates of a diagonal instead of 25 T0 entries and two more
+// rank-1 terms.
 template <typename T>
 __device__ __forceinline__ void anfj(const T n[3], const T u[3], T H, T c, T g, T out[25]) {
   const T g1 = g - T(1);
@@ -74,33 +81,23 @@ __device__ __forceinline__ void anfj(const T n[3], const T u[3], T H, T c, T g, 
   const T ic = T(1) / c;
   const T M2 = v2 * ic * ic, Mn = vn * ic;
   const T be = g1 * ic * ic;
-  const T k1 = T(1) + T(0.5) * g1 * M2;
   const T av = fabs(vn);
-  // T0
-  out[0] = av * (T(1) - T(0.5) * g1 * M2);
-  for (int j = 0; j < 3; j++) out[1 + j] = av * (be * u[j]);
-  out[4] = av * (-be);
-  for (int i = 0; i < 3; i++) {
-    out[5 * (1 + i)] = av * (-k1 * u[i] + vn * n[i]);
-    for (int j = 0; j < 3; j++)
-      out[5 * (1 + i) + 1 + j] = av * (be * u[i] * u[j] - n[i] * n[j] + (i == j ? T(1) : T(0)));
-    out[5 * (1 + i) + 4] = av * (-be * u[i]);
-  }
-  out[20] = av * (vn * vn - T(0.5) * v2 * k1);
-  for (int j = 0; j < 3; j++) out[21 + j] = av * (k1 * u[j] - vn * n[j]);
-  out[24] = av * (-T(0.5) * g1 * M2);
+#pragma unroll
+  for (int k = 0; k < 25; k++) out[k] = (k % 6 == 0) ? av : T(0);
+#pragma unroll
+  for (int i = 0; i < 3; i++) out[5 * (1 + i)] = -av * u[i];
 #pragma unroll
   for (int sgn = -1; sgn <= 1; sgn += 2) {
-    T rr[5], ll[5];
+    T rr[5], wl[5];
     rr[0] = T(1);
     for (int i = 0; i < 3; i++) rr[1 + i] = u[i] + T(sgn) * c * n[i];
     rr[4] = H + T(sgn) * vn * c;
-    ll[0] = T(0.25) * g1 * M2 - T(sgn) * T(0.5) * Mn;
-    for (int j = 0; j < 3; j++) ll[1 + j] = -T(0.5) * be * u[j] + T(sgn) * T(0.5) * n[j] * ic;
-    ll[4] = T(0.5) * be;
-    const T lam = fabs(vn + T(sgn) * c);
+    const T w = fabs(vn + T(sgn) * c) - av;
+    wl[0] = w * (T(0.25) * g1 * M2 - T(sgn) * T(0.5) * Mn);
+    for (int j = 0; j < 3; j++) wl[1 + j] = w * (-T(0.5) * be * u[j] + T(sgn) * T(0.5) * n[j] * ic);
+    wl[4] = w * (T(0.5) * be);
     for (int a = 0; a < 5; a++)
-      for (int b = 0; b < 5; b++) out[5 * a + b] += lam * (rr[a] * ll[b]);
+      for (int b = 0; b < 5; b++) out[5 * a + b] = fma(rr[a], wl[b], out[5 * a + b]);
   }
 }
 
@@ -421,6 +418,39 @@ __device__ __forceinline__ bool inv5(T a[25]) {
 // (i, j) at 5 j + i), so each store instruction here (lane a writes entry (a, k)) and each
 // load instruction of the sweeps touches five consecutive floats per block row instead of
 // five floats 20 bytes apart.
+// The 5x5 block arithmetic of the factorisation, written out so that every kernel that
+// factors (k_ilu_factor, k_pset32) rounds the same way:
+//   (A B)(i, b) = sum_k A(i, k) B(k, b), k ascending, one fused multiply-add per term;
+//   Gauss--Jordan step k on row a of D with rk = row k before the step.
+__device__ __forceinline__ float ilu_dot5(const float A[5], const float* Bcol) {
+  float acc = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 5; k++) acc = fmaf(A[k], Bcol[k], acc);
+  return acc;
+}
+__device__ __forceinline__ double ilu_dot5(const double A[5], const double* Bcol) {
+  double acc = 0.0;
+#pragma unroll
+  for (int k = 0; k < 5; k++) acc = fma(A[k], Bcol[k], acc);
+  return acc;
+}
+template <typename TF>
+__device__ __forceinline__ TF ilu_mul(TF a, TF b) {
+  if constexpr (sizeof(TF) == 4) return __fmul_rn(a, b); else return __dmul_rn(a, b);
+}
+template <typename TF>
+__device__ __forceinline__ void ilu_gj_step(int a, int k, const TF rk[5], TF Da[5]) {
+  const TF ip = TF(1) / rk[k];
+  if (a == k) {
+#pragma unroll
+    for (int b = 0; b < 5; b++) Da[b] = (b == k) ? ip : ilu_mul(rk[b], ip);
+  } else {
+    const TF f = Da[k];
+#pragma unroll
+    for (int b = 0; b < 5; b++) Da[b] = (b == k) ? -ilu_mul(f, ip) : fma(-f, ilu_mul(rk[b], ip), Da[b]);
+  }
+}
+
 template <typename TF>
 __device__ __forceinline__ TF from64(double x) {
   if constexpr (sizeof(TF) == 4) return d2f_trunc(x); else return (TF)x;
@@ -504,9 +534,10 @@ __global__ void __launch_bounds__(kT) k_ilu_factor(
       TF* dst = sm(lrow, (op.z < 0 ? op.x : op.z) - s0) + 5 * a;
 #pragma unroll
       for (int b = 0; b < 5; b++) {
-        TF acc = 0;
+        TF Bc[5];
 #pragma unroll
-        for (int k = 0; k < 5; k++) acc += A[k] * B[5 * b + k];
+        for (int k = 0; k < 5; k++) Bc[k] = B[5 * b + k];
+        const TF acc = ilu_dot5(A, Bc);
         dst[b] = op.z < 0 ? acc : dst[b] - acc;
       }
     }
@@ -520,17 +551,8 @@ __global__ void __launch_bounds__(kT) k_ilu_factor(
     TF rk[5];
 #pragma unroll
     for (int b = 0; b < 5; b++) rk[b] = __shfl_sync(0xffffffffu, D[b], base + k < 32 ? base + k : 0);
-    const TF piv = rk[k];
-    ok &= !(active && piv == TF(0));
-    const TF ip = TF(1) / piv;
-    if (a == k) {
-#pragma unroll
-      for (int b = 0; b < 5; b++) D[b] = (b == k) ? ip : D[b] * ip;
-    } else {
-      const TF f = D[k];
-#pragma unroll
-      for (int b = 0; b < 5; b++) D[b] = (b == k) ? -f * ip : D[b] - f * (rk[b] * ip);
-    }
+    ok &= !(active && rk[k] == TF(0));
+    ilu_gj_step<TF>(a, k, rk, D);  // lane a's own row: D[b] == rk[b] when a == k
   }
   if (!active) return;
   if (!ok) atomicMin(ierr, p + 1);
@@ -547,14 +569,18 @@ __global__ void __launch_bounds__(kT) k_ilu_factor(
 
 // Fused FP32 set-up: one level (colour) of the block ILU(0) factorisation of
 // P = I - gamma diag(1/v) J with the rows of J assembled in the same kernel, so J is never
-// written to or read back from HBM.  A warp takes 32 rows of the level:
-//   A. thread per row: the row's Jacobian blocks (jac_row32, the arithmetic of k_jac_cell32)
-//      staged in shared memory, then P = delta - (gamma/v) J in place (the same fmaf as
-//      k_ilu_factor, so the factors equal the two-kernel path's bit for bit);
-//   B. five lanes per row, six rows at a time (k_ilu_factor's scheme): the update operations
-//      with the finished rows of earlier levels (inv(D_q), U_qj from LU), the Gauss--Jordan
-//      inverse of the diagonal block across the row's five lanes, and the column-major stores
-//      into the L and D/U regions.
+// written to or read back from HBM.  Thread per row, a warp takes 32 rows of the level:
+//   A. the row's Jacobian blocks (jac_row32, the arithmetic of k_jac_cell32) staged in shared
+//      memory, then P = delta - (gamma/v) J in place;
+//   B. the update operations with the finished rows of earlier levels (L_pq = P_pq inv(D_q),
+//      P_pj -= L_pq U_qj, operands from LU), then the Gauss--Jordan inverse of the diagonal
+//      block in registers -- every lane its own row, so the 32 rows' operand loads are in
+//      flight together;
+//   C. the warp stores its 32 rows one after another, each as its two contiguous ranges (L
+//      blocks, then inverted diagonal and U blocks), transposed to the column-major factor
+//      layout on the way, so the stores are coalesced.
+// The arithmetic is k_ilu_factor's operation for operation (ilu_mul_sub, ilu_gj_step), so the
+// factors equal the two-kernel path's bit for bit.
 template <int kW>
 __global__ void __launch_bounds__(64) k_pset32(
     int n, const int* __restrict__ rows, int p0, const int* __restrict__ prow,
@@ -568,17 +594,16 @@ __global__ void __launch_bounds__(64) k_pset32(
   constexpr int kRow = (kW + 1) * 25;
   __shared__ float stg[2][32][kRow];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int t0 = (blockIdx.x * 2 + warp) * 32;  // first row of the warp within the level
-  const int t = t0 + lane;
-  // A: this lane's row
+  const int t = (blockIdx.x * 2 + warp) * 32 + lane;
+  float* st = stg[warp][lane];
   int p = 0, s0 = 0, nb = 0, sd = 0;
   if (t < n) {
+    // A
     p = rows ? rows[t] : p0 + t;
     s0 = prow[p];
     nb = prow[p + 1] - s0;
     sd = pdiag[p] - s0;
     const int c = ord[p];
-    float* st = stg[warp][lane];
     jac_row32<kW>(c, nFi, s0, sd, ell, faceLR, faceNA32, fslot, Whl, Gb, Sc, d2f_trunc(g), st);
     const float sc = d2f_trunc(gamma * invV[c]);
     for (int b = 0; b < nb; b++) {
@@ -587,72 +612,60 @@ __global__ void __launch_bounds__(64) k_pset32(
       for (int k = 0; k < 25; k++)
         blk[k] = fmaf(-sc, blk[k], (b == sd && k % 6 == 0) ? 1.0f : 0.0f);
     }
-  }
-  __syncwarp();
-  // B: rows r0 .. r0 + 5 of the warp, five lanes each (lane a owns row a of every block)
-  const int sub = lane / 5, a = lane - 5 * sub;
-  for (int r0 = 0; r0 < 32; r0 += 6) {
-    const int r = r0 + sub;
-    const int src = (sub < 6 && r < 32) ? r : 0;
-    const int pr = __shfl_sync(0xffffffffu, p, src);
-    const int s0r = __shfl_sync(0xffffffffu, s0, src);
-    const int nbr = __shfl_sync(0xffffffffu, nb, src);
-    const int sdr = __shfl_sync(0xffffffffu, sd, src);
-    const bool active = sub < 6 && r < 32 && t0 + r < n;
-    float* st = stg[warp][src];
-    float D[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-    if (active) {
-      const int o0 = upd_ptr[pr], o1 = upd_ptr[pr + 1];
-      for (int o = o0; o < o1; o++) {
-        const int3 op = upd[o];
-        float A[5];
-        const float* Ar = st + 25 * (op.x - s0r) + 5 * a;
+    // B
+    const int o1 = upd_ptr[p + 1];
+    for (int o = upd_ptr[p]; o < o1; o++) {
+      const int3 op = upd[o];
+      const float* Ab = st + 25 * (op.x - s0);
+      const float* B = LU + 25 * (size_t)op.y;  // column-major, finished in earlier levels
+      float* dst = st + 25 * ((op.z < 0 ? op.x : op.z) - s0);
+      float Bv[25];
 #pragma unroll
-        for (int k = 0; k < 5; k++) A[k] = Ar[k];
-        const float* B = LU + 25 * (size_t)op.y;  // column-major, finished in earlier levels
-        float* dst = st + 25 * ((op.z < 0 ? op.x : op.z) - s0r) + 5 * a;
+      for (int k = 0; k < 25; k++) Bv[k] = __ldg(B + k);
+#pragma unroll
+      for (int i = 0; i < 5; i++) {
+        float A[5];
+#pragma unroll
+        for (int k = 0; k < 5; k++) A[k] = Ab[5 * i + k];
 #pragma unroll
         for (int b = 0; b < 5; b++) {
-          float acc = 0.0f;
-#pragma unroll
-          for (int k = 0; k < 5; k++) acc += A[k] * __ldg(B + 5 * b + k);
-          dst[b] = op.z < 0 ? acc : dst[b] - acc;
+          const float acc = ilu_dot5(A, Bv + 5 * b);
+          dst[5 * i + b] = op.z < 0 ? acc : dst[5 * i + b] - acc;
         }
       }
-#pragma unroll
-      for (int b = 0; b < 5; b++) D[b] = st[25 * sdr + 5 * a + b];
     }
-    const int base = lane - a;
+    float D[25];
+#pragma unroll
+    for (int k = 0; k < 25; k++) D[k] = st[25 * sd + k];
     bool ok = true;
 #pragma unroll
     for (int k = 0; k < 5; k++) {
       float rk[5];
 #pragma unroll
-      for (int b = 0; b < 5; b++) rk[b] = __shfl_sync(0xffffffffu, D[b], base + k < 32 ? base + k : 0);
-      const float piv = rk[k];
-      ok &= !(active && piv == 0.0f);
-      const float ip = 1.0f / piv;
-      if (a == k) {
+      for (int b = 0; b < 5; b++) rk[b] = D[5 * k + b];
+      ok &= rk[k] != 0.0f;
 #pragma unroll
-        for (int b = 0; b < 5; b++) D[b] = (b == k) ? ip : D[b] * ip;
-      } else {
-        const float f = D[k];
-#pragma unroll
-        for (int b = 0; b < 5; b++) D[b] = (b == k) ? -f * ip : D[b] - f * (rk[b] * ip);
-      }
+      for (int a = 0; a < 5; a++) ilu_gj_step<float>(a, k, rk, D + 5 * a);
     }
-    if (active) {
-      if (!ok) atomicMin(ierr, pr + 1);
+    if (!ok) atomicMin(ierr, p + 1);
 #pragma unroll
-      for (int b = 0; b < 5; b++) st[25 * sdr + 5 * a + b] = D[b];
-      const int bl = plst[pr], bdu = pdu[pr];
-      for (int b = 0; b < nbr; b++) {
-        float* dst = LU + 25 * (size_t)(b < sdr ? bl + b : bdu + (b - sdr)) + a;
-#pragma unroll
-        for (int k = 0; k < 5; k++) dst[5 * k] = st[25 * b + 5 * a + k];
-      }
+    for (int k = 0; k < 25; k++) st[25 * sd + k] = D[k];
+  }
+  __syncwarp();
+  // C: row r's blocks [0, sd_r) go to the L region at plst, [sd_r, nb_r) to the D/U region at
+  // pdu; factor entry (i, j) of a block sits at 5 j + i (column-major), staging at 5 i + j
+  for (int rr = 0; rr < 32; rr++) {
+    const int nbr = __shfl_sync(0xffffffffu, nb, rr);
+    if (nbr == 0) continue;  // row past the end of the level
+    const int sdr = __shfl_sync(0xffffffffu, sd, rr);
+    const int pr = __shfl_sync(0xffffffffu, p, rr);
+    const float* src = stg[warp][rr];
+    float* dl = LU + 25 * (size_t)plst[pr];
+    float* du = LU + 25 * (size_t)pdu[pr] - 25 * (size_t)sdr;
+    for (int e = lane; e < 25 * nbr; e += 32) {
+      const int b = e / 25, r = e - 25 * b, i = r % 5, j = r / 5;
+      (b < sdr ? dl : du)[e] = src[25 * b + 5 * i + j];
     }
-    __syncwarp();
   }
 }
 
