@@ -228,6 +228,11 @@ struct fos_bdf_work {
   double ilu_ref_rate = 1.0;  // learned mode: its mean residual reduction per iteration
   int learned_backoff = 0;  // learned mode: solves skipped after the last fallback
   int learned_skip = 0;     // learned mode: solves still to run with ILU(0) alone
+  int setup_age = -1;       // set-up policy: steps since the last set-up at the end of the
+                            // last call (-1: none that a resumed call may keep)
+  double gamma_setup = 0.0; // and the gamma it was made for
+  long setup_serial = -1;   // the context's set-up count then (a set-up made outside the
+                            // driver in between voids the kept one)
   double t_last = 0.0;
   double *V = nullptr, *Z = nullptr, *w = nullptr, *yn = nullptr, *ym = nullptr,
          *hist = nullptr, *f = nullptr, *b = nullptr, *d = nullptr, *part = nullptr,
@@ -673,9 +678,17 @@ extern "C" int fos_bdf_run(fos_ctx* c, double t0, double* y, const fos_bdf_opts*
   FOS_CUDA(cudaMemcpyAsync(wk.yn, y, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
   if (!resume) wk.has_hist = false;
   int status = 0;
-  // preconditioner set-up policy (opts->msbp > 1: CVODE's cvLsSetup conditions)
-  int last_setup = -1;
+  // preconditioner set-up policy (opts->msbp > 1: CVODE's cvLsSetup conditions); a resumed
+  // call continues the previous call's count, as CVODE keeps its set-up across CVode calls
+  bool have_setup = false;
+  int last_setup = 0;
   double gamma_setup = 0.0;
+  if (resume && wk.setup_age >= 0 && c->has_factor && wk.setup_serial == c->n_setup) {
+    have_setup = true;
+    last_setup = -wk.setup_age;
+    gamma_setup = wk.gamma_setup;
+  }
+  int steps_done = 0;
   for (int s = 0; s < opts->nsteps && !status; s++) {
     const int q = (opts->order == 2 && (s >= 1 || resume)) ? 2 : 1;
     const double gamma = q == 1 ? opts->dt : 2.0 * opts->dt / 3.0;
@@ -683,7 +696,7 @@ extern "C" int fos_bdf_run(fos_ctx* c, double t0, double* y, const fos_bdf_opts*
     fos_launch(c, k_hist, nb(N), kT, N, q, wk.yn, wk.ym, wk.hist);
     // the Newton iteration starts from y_n, which y holds: yn was copied from y before the
     // first step and from the accepted y after every step
-    const bool reuse = opts->msbp > 1 && last_setup >= 0 && c->has_factor &&
+    const bool reuse = opts->msbp > 1 && have_setup && c->has_factor &&
                        s - last_setup < opts->msbp &&
                        std::fabs(gamma / gamma_setup - 1.0) <= 0.3;
     dr.keep_setup = reuse;
@@ -695,6 +708,7 @@ extern "C" int fos_bdf_run(fos_ctx* c, double t0, double* y, const fos_bdf_opts*
       nrc = dr.newton(y, gamma, wk.hist, tn);
     }
     if (dr.setup_made) {
+      have_setup = true;
       last_setup = s;
       gamma_setup = gamma;
     }
@@ -711,9 +725,13 @@ extern "C" int fos_bdf_run(fos_ctx* c, double t0, double* y, const fos_bdf_opts*
     FOS_CUDA(cudaMemcpyAsync(wk.yn, y, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
     t = tn;
     st.n_steps++;
+    steps_done = s + 1;
     wk.has_hist = true;
   }
   if (status) wk.has_hist = false;
+  wk.setup_age = (have_setup && !status) ? steps_done - last_setup : -1;
+  wk.gamma_setup = gamma_setup;
+  wk.setup_serial = c->n_setup;
   wk.ilu_ref_its = dr.ilu_ref_its;
   wk.ilu_ref_rate = dr.ilu_ref_rate;
   st.t = t;

@@ -535,6 +535,7 @@ extern "C" int fos_euler_pset_dev(fos_ctx* c, double t, const double* y, int jok
   }
   int rc = fos_jac_setup(c);
   if (rc) return rc;
+  c->n_setup++;
   if (fos_pset_is_fused(c)) {
     // J is assembled inside the factor; jok = 1 reassembles it from the state of the last
     // jok = 0 call (the same J, bit for bit), or factors the caller's J (fos_euler_jac_set)

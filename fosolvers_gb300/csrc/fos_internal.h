@@ -137,6 +137,7 @@ struct fos_ctx {
   double* d_vol = nullptr;        // [nC]
   double* d_ilut_x = nullptr;     // [5nC] position-order work vector
   long n_launch = 0;            // kernels launched through fos_launch
+  long n_setup = 0;             // preconditioner set-ups (fos_euler_pset_dev calls) so far
   fos_gnn* gnn = nullptr;       // learned preconditioner (not owned)
 
   ~fos_ctx();

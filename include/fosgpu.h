@@ -262,7 +262,9 @@ typedef struct {
                          correction, z = u + N(y; u) with u = ILU(0) r, with the fallback
                          of 2; 5 = the same without fallback */
   int jac_reuse;      /* 0 = assemble J every BDF step (jok = 0), 1 = keep J from the first step */
-  int resume;         /* 1 = continue the BDF history of the previous call (y must be its result) */
+  int resume;         /* 1 = continue the BDF history of the previous call (y must be its
+                         result), and with msbp > 1 its preconditioner set-up count: CVODE
+                         keeps its set-up across CVode calls */
   int msbp;           /* preconditioner set-up policy: 1 = pset at every BDF step (default);
                          m > 1 = CVODE's (cvLsSetup: MSBP = 20, DGMAX = 0.3): pset at the
                          first step of the call, when m steps have passed since the last one

@@ -206,3 +206,33 @@ def test_cvode_setup_policy_matches_oracle(cuda, msbp):
         assert st[k] == st_ref[k], k
     assert st["n_pset"] < 12
     assert rel_err(y, y_ref) <= 1e-10
+
+
+def test_resumed_calls_keep_the_setup_policy(cuda):
+    """Twelve one-step calls with resume = 1 under CVODE's set-up policy (MSBP 5) make the
+    same psets and reach the same state, bit for bit, as one twelve-step call: the set-up
+    count carries across calls as CVODE's does across CVode calls.  A pset made outside the
+    driver in between voids the kept set-up (the next step sets up again)."""
+    import torch
+    wl = M.make_workload("sine96", scale=8, seed=1)
+    c = Case(wl)
+    y_one, st_one = gpu_run(c, nsteps=12, msbp=5)
+    yr = torch.from_numpy(c.y0).cuda()
+    y = torch.empty_like(yr)
+    c.gpu.to_internal(yr, y)
+    n_pset = 0
+    for k in range(12):
+        rc, st = c.gpu.bdf_run(y, c.gpu.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=1,
+                                                     precond=1, msbp=5, resume=1 if k else 0),
+                               t0=k * wl.dt)
+        assert rc == 0
+        n_pset += st["n_pset"]
+    assert n_pset == st_one["n_pset"] < 12
+    c.gpu.to_reference(y, yr)
+    torch.cuda.synchronize()
+    assert np.array_equal(yr.cpu().numpy(), y_one)
+    # an outside pset between two resumed calls: the next call sets up afresh
+    c.gpu.pset_dev(0.0, y, 0, 2.0 * wl.dt / 3.0)
+    rc, st = c.gpu.bdf_run(y, c.gpu.bdf_defaults(order=wl.order, dt=wl.dt, nsteps=1, precond=1,
+                                                 msbp=5, resume=1), t0=12 * wl.dt)
+    assert rc == 0 and st["n_pset"] == 1
