@@ -30,11 +30,17 @@ def _nvcc() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libfosgpu.so")
 
 
+# Host code is compiled without multiply-add contraction (g++ contracts by default on AArch64
+# but not on x86-64), so the host-side set-up -- face geometry, closure vectors, renumbering --
+# gives the same numbers on both machines.  Device code keeps nvcc's default.
+HOST_FLAGS = ["-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
+
+
 def _compile(src: Path, obj: Path, extra: list[str]) -> None:
-    cmd = [_nvcc(), "-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC",
+    cmd = [_nvcc(), "-std=c++17", "-O3", "-lineinfo", *ARCH, *HOST_FLAGS,
            "-I", str(HERE.parent / "include"), *extra, "-c", str(src), "-o", str(obj)]
     if src.suffix == ".cpp":
-        cmd = [_nvcc(), "-std=c++17", "-O3", "-Xcompiler", "-fPIC",
+        cmd = [_nvcc(), "-std=c++17", "-O3", *HOST_FLAGS,
                "-I", str(HERE.parent / "include"), "-x", "c++", "-c", str(src), "-o", str(obj)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -9,7 +9,10 @@ oracle_sod16.npz   config 1 (16^3 x 6 = 24,576 tets, Sod, walls): the residual f
                    z = P^-1 r from pset (gamma 5e-3) + psol on that state (r: seed 8), and
                    the state after the configuration's 20 BDF1 steps (dt 1e-3, Newton 1e-8,
                    GMRES(30) + ILU(0)).
-oracle_sine12.npz  config 2's state on a 12^3 x 6 mesh (seed 3): residual and Jv as above.
+oracle_sine12.npz  config 2's state on a 12^3 x 6 mesh (seed 3): residual and Jv as above,
+                   with the perturbed state y itself (the sinusoidal state comes from numpy's
+                   sin, whose last bit differs between x86-64 and AArch64 builds, and the
+                   difference quotient magnifies that by 1/s ~ 1e8).
 """
 from __future__ import annotations
 
@@ -57,8 +60,8 @@ def sod16():
 
 def sine12():
     c = Case(M.make_workload("sine96", scale=12, seed=3))
-    _, f, _, jv = residual_and_jv(c)
-    return dict(f=f, jv=jv)
+    y, f, _, jv = residual_and_jv(c)
+    return dict(f=f, jv=jv, y=y)
 
 
 def main():
