@@ -403,7 +403,7 @@ struct Driver {
     st.n_rhs++;
     int rc = have_sq ? 0 : fos_norm2_dev(c, v, wk.N, c->d_scal);
     if (rc) return rc;
-    rc = fos_jv_sigma(c, c->d_scal, ynorm, eps);
+    rc = fos_jv_sigma(c, c->d_scal, ynorm, eps, -gamma);
     if (rc) return rc;
     return fos_residual_launch(c, y, v, c->d_scal + 1, fy, w, 1.0, -gamma, 1);
   }

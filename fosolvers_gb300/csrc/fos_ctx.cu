@@ -474,7 +474,7 @@ extern "C" int fos_euler_jv_dev(fos_ctx* c, double t, const double* y, const dou
   // s = eps (1 + ||y||) / ||v|| evaluated on the device (scal[0] = ||v||^2, scal[1] = s)
   int rc = fos_norm2_dev(c, v, 5L * c->nC, c->d_scal);
   if (rc) return rc;
-  rc = fos_jv_sigma(c, c->d_scal, ynorm, eps);
+  rc = fos_jv_sigma(c, c->d_scal, ynorm, eps, b);
   if (rc) return rc;
   return fos_residual_launch(c, y, v, c->d_scal + 1, fy, out, a, b, 1);
 }
@@ -487,7 +487,7 @@ extern "C" int fos_euler_jv_dev_vnorm(fos_ctx* c, double t, const double* y, con
     fos_set_error("fos_euler_jv_dev_vnorm: bad arguments");
     return -1;
   }
-  int rc = fos_jv_sigma_known(c, c->d_scal, ynorm, vnorm, eps);
+  int rc = fos_jv_sigma_known(c, c->d_scal, ynorm, vnorm, eps, b);
   if (rc) return rc;
   return fos_residual_launch(c, y, v, c->d_scal + 1, fy, out, a, b, 1);
 }

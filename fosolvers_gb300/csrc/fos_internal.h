@@ -165,8 +165,10 @@ int fos_permute_plane(fos_ctx* c, const double* in, double* out, int dir, int q)
 // waiting for the last copy (synchronise c->stream before reading h)
 int fos_h2d_internal(fos_ctx* c, const double* h, double* d_internal);
 int fos_d2h_reference(fos_ctx* c, const double* d_internal, double* h);
-int fos_jv_sigma(fos_ctx* c, double* d_scal, double ynorm, double eps);
-int fos_jv_sigma_known(fos_ctx* c, double* d_scal, double ynorm, double vnorm, double eps);
+// s = eps (1 + ynorm)/||v||, 1/s and b/s into d_scal[1..3] (||v||^2 in d_scal[0])
+int fos_jv_sigma(fos_ctx* c, double* d_scal, double ynorm, double eps, double b);
+int fos_jv_sigma_known(fos_ctx* c, double* d_scal, double ynorm, double vnorm, double eps,
+                       double b);
 int fos_prim_hl_launch(fos_ctx* c, const double* y);  // FP32 (hi, lo) primitives
 int fos_prim_launch(fos_ctx* c, const double* y);
 int fos_gnn_precond(fos_ctx* c, const double* y, const double* r, double gamma, double* z);

@@ -171,11 +171,13 @@ __device__ __forceinline__ void load_ell(const int* __restrict__ ell, int c, int
 }
 
 // out = acc / v (mode 0) or the Jv combination a v + (b / s)(acc / v - fy) (mode 1), in
-// FP64; non-finite results are flagged from the exponent bits (no FP64 compares)
+// FP64; b / s comes precomputed in d_s[2] (k_sigma), and amode says whether a is 1 (1), 0 (0)
+// or neither (2), so no FP64 compare or multiply runs per cell for the coefficients;
+// non-finite results are flagged from the exponent bits (no FP64 compares)
 __device__ __forceinline__ void gather_epilogue(int nC, int c, const double acc[5], double iv,
                                                 int mode, const double* __restrict__ vv,
                                                 const double* __restrict__ fy,
-                                                const double* __restrict__ d_s, double a, double b,
+                                                const double* __restrict__ d_s, double a, int amode,
                                                 double* __restrict__ out, int* __restrict__ flag) {
   bool ok = true;
   if (mode == 0) {
@@ -186,12 +188,12 @@ __device__ __forceinline__ void gather_epilogue(int nC, int c, const double acc[
       out[(size_t)q * nC + c] = o;
     }
   } else {
-    const double bs = d_s[0] > 0.0 ? b * d_s[1] : 0.0;  // b / s
+    const double bs = __ldg(d_s + 2);  // b / s
 #pragma unroll
     for (int q = 0; q < 5; q++) {
       const size_t k = (size_t)q * nC + c;
       const double t = fma(acc[q], iv, -fy[k]);
-      const double o = a == 1.0 ? fma(bs, t, vv[k]) : a == 0.0 ? bs * t : fma(bs, t, a * vv[k]);
+      const double o = amode == 1 ? fma(bs, t, vv[k]) : amode == 0 ? bs * t : fma(bs, t, a * vv[k]);
       ok &= finite_bits(o);
       out[k] = o;
     }
@@ -203,7 +205,7 @@ template <int kW>
 __global__ void __launch_bounds__(kThreads) k_gather(
     int nC, const int* __restrict__ ell, const double* __restrict__ F,
     const double* __restrict__ invV, int mode, const double* __restrict__ vv,
-    const double* __restrict__ fy, const double* __restrict__ d_s, double a, double b,
+    const double* __restrict__ fy, const double* __restrict__ d_s, double a, int amode,
     double* __restrict__ out, int* __restrict__ flag) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nC) return;
@@ -219,7 +221,7 @@ __global__ void __launch_bounds__(kThreads) k_gather(
     acc[0] += sg * a0.x; acc[1] += sg * a0.y; acc[2] += sg * a1.x; acc[3] += sg * a1.y;
     acc[4] += sg * a2.x;
   }
-  gather_epilogue(nC, c, acc, __ldg(invV + c), mode, vv, fy, d_s, a, b, out, flag);
+  gather_epilogue(nC, c, acc, __ldg(invV + c), mode, vv, fy, d_s, a, amode, out, flag);
 }
 
 // ------------------------------------------------------------------ FP32 flux
@@ -389,7 +391,7 @@ __global__ void __launch_bounds__(kThreads) k_cell32(
     const double* __restrict__ Fb, const float4* __restrict__ Sc,
     const double* __restrict__ invV, int mode,
     const double* __restrict__ vv, const double* __restrict__ fy, const double* __restrict__ d_s,
-    double a, double b, double* __restrict__ out, int* __restrict__ flag,
+    double a, int amode, double* __restrict__ out, int* __restrict__ flag,
     const double2* __restrict__ faceNA64, unsigned char* __restrict__ fsel, float theta,
     double gm1d) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -471,7 +473,7 @@ __global__ void __launch_bounds__(kThreads) k_cell32(
     acc[3] -= f2d_bits(fmaf(t, P.h[3], P.h[5] * S.z));
     acc[4] -= f2d_bits(t * P.h[4]);
   }
-  gather_epilogue(nC, c, acc, __ldg(invV + c), mode, vv, fy, d_s, a, b, out, flag);
+  gather_epilogue(nC, c, acc, __ldg(invV + c), mode, vv, fy, d_s, a, amode, out, flag);
 }
 
 using cell32_fn = decltype(&k_cell32<4, false>);
@@ -526,19 +528,22 @@ __global__ void k_sum_final(const double* __restrict__ part, int np, double* __r
   }
 }
 
-__global__ void k_sigma(double* scal, double ynorm, double eps) {
+// s, 1/s and b/s of the Jv (scal[1..3]; the epilogue reads them as d_s[0..2])
+__global__ void k_sigma(double* scal, double ynorm, double eps, double b) {
   const double vn2 = scal[0];
   const double s = vn2 > 0.0 ? eps * (1.0 + ynorm) / sqrt(vn2) : 0.0;
   scal[1] = s;
   scal[2] = s > 0.0 ? 1.0 / s : 0.0;
+  scal[3] = s > 0.0 ? b * scal[2] : 0.0;  // b (1/s), as the epilogue formed it
 }
 
 // the same with ||v||_2 supplied by the caller (no reduction pass over v)
-__global__ void k_sigma_known(double* scal, double ynorm, double vnorm, double eps) {
+__global__ void k_sigma_known(double* scal, double ynorm, double vnorm, double eps, double b) {
   const double s = vnorm > 0.0 ? eps * (1.0 + ynorm) / vnorm : 0.0;
   scal[0] = vnorm * vnorm;
   scal[1] = s;
   scal[2] = s > 0.0 ? 1.0 / s : 0.0;
+  scal[3] = s > 0.0 ? b * scal[2] : 0.0;  // b (1/s), as the epilogue formed it
 }
 
 inline int nblk(long n, int t = kThreads) { return (int)((n + t - 1) / t); }
@@ -547,7 +552,9 @@ inline int nblk(long n, int t = kThreads) { return (int)((n + t - 1) / t); }
 
 int fos_residual_launch(fos_ctx* c, const double* y, const double* v, const double* d_s,
                         const double* fy, double* out, double a, double b, int mode) {
+  (void)b;  // b / s comes from the preceding fos_jv_sigma* (d_s[2])
   const double gm1 = c->gamm - 1.0;
+  const int amode = a == 1.0 ? 1 : a == 0.0 ? 0 : 2;
   if (c->flags & FOS_FLUX_FP32) {
     fos_launch(c, k_prim_hl, nblk(c->nC), kThreads, c->nC, y, v, d_s, gm1, c->d_Whl);
     const bool hyb = (c->flags & FOS_FLUX_HYBRID) != 0;
@@ -560,7 +567,7 @@ int fos_residual_launch(fos_ctx* c, const double* y, const double* v, const doub
     fos_launch(c, cell32_kernel(c->ell_w, hyb), nblk(c->nC), kThreads, c->nC, c->nFi,
                (const int*)c->d_ell, (const int2*)c->d_faceLR, (const float4*)c->d_faceNA32,
                (const float*)c->d_Whl, (float)gm1, (const double*)c->d_F,
-               (const float4*)c->d_closure32, (const double*)c->d_invV, mode, v, fy, d_s, a, b,
+               (const float4*)c->d_closure32, (const double*)c->d_invV, mode, v, fy, d_s, a, amode,
                out, c->d_flag, (const double2*)c->d_faceNA, c->d_fsel, (float)c->hyb_theta, gm1);
   } else {
     fos_launch(c, k_prim64, nblk(c->nC), kThreads, c->nC, y, v, d_s, gm1, c->d_W);
@@ -570,11 +577,11 @@ int fos_residual_launch(fos_ctx* c, const double* y, const double* v, const doub
                c->d_F);
     if (c->ell_w == 4)
       fos_launch(c, k_gather<4>, nblk(c->nC), kThreads, c->nC, (const int*)c->d_ell,
-                 (const double*)c->d_F, (const double*)c->d_invV, mode, v, fy, d_s, a, b, out,
+                 (const double*)c->d_F, (const double*)c->d_invV, mode, v, fy, d_s, a, amode, out,
                  c->d_flag);
     else
       fos_launch(c, k_gather<6>, nblk(c->nC), kThreads, c->nC, (const int*)c->d_ell,
-                 (const double*)c->d_F, (const double*)c->d_invV, mode, v, fy, d_s, a, b, out,
+                 (const double*)c->d_F, (const double*)c->d_invV, mode, v, fy, d_s, a, amode, out,
                  c->d_flag);
   }
   FOS_LAUNCH_CHECK();
@@ -608,14 +615,15 @@ int fos_sum_partials(fos_ctx* c, int np, double* d_out) {
   return 0;
 }
 
-int fos_jv_sigma(fos_ctx* c, double* d_scal, double ynorm, double eps) {
-  fos_launch(c, k_sigma, 1, 1, d_scal, ynorm, eps);
+int fos_jv_sigma(fos_ctx* c, double* d_scal, double ynorm, double eps, double b) {
+  fos_launch(c, k_sigma, 1, 1, d_scal, ynorm, eps, b);
   FOS_LAUNCH_CHECK();
   return 0;
 }
 
-int fos_jv_sigma_known(fos_ctx* c, double* d_scal, double ynorm, double vnorm, double eps) {
-  fos_launch(c, k_sigma_known, 1, 1, d_scal, ynorm, vnorm, eps);
+int fos_jv_sigma_known(fos_ctx* c, double* d_scal, double ynorm, double vnorm, double eps,
+                       double b) {
+  fos_launch(c, k_sigma_known, 1, 1, d_scal, ynorm, vnorm, eps, b);
   FOS_LAUNCH_CHECK();
   return 0;
 }
@@ -713,7 +721,7 @@ extern "C" int fos_euler_rhs_dev_static(const fos_ctx* c, double t, const double
     // the face choice of the hybrid flux is made from this state (no record kept)
     cell32_kernel(c->ell_w, hyb)<<<nblk(c->nC), kThreads, 0, s>>>(
         c->nC, c->nFi, c->d_ell, c->d_faceLR, c->d_faceNA32, Whl, (float)gm1, F, c->d_closure32,
-        c->d_invV, 0, nullptr, nullptr, nullptr, 0.0, 0.0, ydot, nullptr, c->d_faceNA, nullptr,
+        c->d_invV, 0, nullptr, nullptr, nullptr, 0.0, 0, ydot, nullptr, c->d_faceNA, nullptr,
         (float)c->hyb_theta, gm1);
   } else {
     double* W = reinterpret_cast<double*>(bytes);
@@ -724,10 +732,10 @@ extern "C" int fos_euler_rhs_dev_static(const fos_ctx* c, double t, const double
                                               c->gamm, c->r, F);
     if (c->ell_w == 4)
       k_gather<4><<<nblk(c->nC), kThreads, 0, s>>>(c->nC, c->d_ell, F, c->d_invV, 0, nullptr,
-                                                   nullptr, nullptr, 0.0, 0.0, ydot, nullptr);
+                                                   nullptr, nullptr, 0.0, 0, ydot, nullptr);
     else
       k_gather<6><<<nblk(c->nC), kThreads, 0, s>>>(c->nC, c->d_ell, F, c->d_invV, 0, nullptr,
-                                                   nullptr, nullptr, 0.0, 0.0, ydot, nullptr);
+                                                   nullptr, nullptr, 0.0, 0, ydot, nullptr);
   }
   FOS_LAUNCH_CHECK();
   return 0;
