@@ -798,7 +798,8 @@ def main():
             "vs_fp64_ilu": vs64, "same_precision_ilu": alt or None,
             "alt_setup_policy": cvode,
             "stats": {k: st[k] for k in ("n_rhs", "n_jv", "n_psol", "n_pset", "n_newton",
-                                          "n_lin_iters", "n_steps", "n_fallback", "n_learned")},
+                                          "n_lin_iters", "n_steps", "n_fallback", "n_learned",
+                                          "n_gated")},
         }
         print(json.dumps(line), flush=True)
     if pg is not None:

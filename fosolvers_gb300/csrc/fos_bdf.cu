@@ -14,6 +14,7 @@
 // All reductions are deterministic two-stage warp-shuffle reductions.
 #include <algorithm>
 #include <cfloat>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -228,6 +229,11 @@ struct fos_bdf_work {
   double ilu_ref_rate = 1.0;  // learned mode: its mean residual reduction per iteration
   int learned_backoff = 0;  // learned mode: solves skipped after the last fallback
   int learned_skip = 0;     // learned mode: solves still to run with ILU(0) alone
+  // learned mode, the cost model that gates the network: the fastest Krylov iteration seen
+  // with ILU(0) and with the network (wall time, ms; 0 = none yet), and the network's mean
+  // residual reduction per iteration in its last solve (-1 = not tried yet)
+  double t_it_ilu = 0.0, t_it_net = 0.0;
+  double net_rate = -1.0;
   int setup_age = -1;       // set-up policy: steps since the last set-up at the end of the
                             // last call (-1: none that a resumed call may keep)
   double gamma_setup = 0.0; // and the gamma it was made for
@@ -384,6 +390,31 @@ struct Driver {
     if (have_sq) *have_sq = d_zsq != nullptr;
     return fos_ilu_apply(c, r, z, d_zsq);
   }
+  // Expected cost of one decade of residual reduction: iteration time / -log10(rate).  The
+  // network is not applied while its last solve's rate at its iteration time buys a decade
+  // no cheaper than the last ILU(0) solve did -- the history already predicts a loss.  A
+  // slower ILU(0) solve (a harder state) reopens the gate; a network that was never tried,
+  // or iterations not yet timed, leave it open.
+  bool network_predicted_to_lose() const {
+    if (wk.net_rate < 0.0 || ilu_ref_its < 0 || wk.t_it_ilu <= 0.0 || wk.t_it_net <= 0.0)
+      return false;
+    if (wk.net_rate >= 1.0) return true;
+    if (!(ilu_ref_rate > 0.0)) return true;  // ILU(0) converged at once
+    return wk.t_it_net * -std::log(ilu_ref_rate) >= wk.t_it_ilu * -std::log(wk.net_rate);
+  }
+  void note_iteration_time(double ms) {
+    double& t = pc == 1 ? wk.t_it_ilu : wk.t_it_net;
+    if (pc == 1 || pc == 2 || pc == 4) t = t > 0.0 ? std::min(t, ms) : ms;
+  }
+  // the network lost this solve: ILU(0) from here on, and the exponential back-off skips the
+  // network for the next 1, 4, 16, ... solves, so a network that keeps losing to ILU(0)
+  // costs a vanishing share of a long run
+  void note_fallback() {
+    st.n_fallback++;
+    wk.learned_backoff = wk.learned_backoff ? std::min(4 * wk.learned_backoff, 1 << 20) : 1;
+    wk.learned_skip = wk.learned_backoff;
+    pc = 1;
+  }
   int ensure_pset() {
     if (pset_done) return 0;
     int jcur = 0;
@@ -459,9 +490,9 @@ struct Driver {
   }
   // GMRES on J_G d = b; d starts at zero.  With a learned preconditioner (o.precond >= 2)
   // this is flexible GMRES (Z_j = M_j(V_j) kept); in modes 2 and 4 it falls back to ILU(0)
-  // -- restarting from the current iterate -- when the residual estimate stagnates (> 0.9
-  // of the previous one) or the iteration count reaches that of the last
-  // ILU(0)-preconditioned solve.  With y_add (the Newton iterate, read by the Jv until the
+  // when the residual estimate stagnates (> 0.9 of the previous one), falls behind the last
+  // ILU(0)-preconditioned solve's rate, or the iteration count reaches that solve's: the
+  // cycle goes on with ILU(0) (a non-finite estimate restarts it from the current iterate).  With y_add (the Newton iterate, read by the Jv until the
   // end), a solve that converges in its first cycle adds d to y_add instead of storing d
   // (*added); otherwise d is left in wk.d.  v0_is_b: V_0 already holds b (the Newton
   // residual kernel wrote it there), used unnormalised in the first cycle.
@@ -475,6 +506,10 @@ struct Driver {
     if (with_fallback && ilu_ref_its < 0) pc = 1;  // no ILU reference yet: this solve sets it
     if (with_fallback && pc != 1 && wk.learned_skip > 0) {  // back-off after a fallback
       wk.learned_skip--;
+      pc = 1;
+    }
+    if (with_fallback && pc != 1 && network_predicted_to_lose()) {
+      st.n_gated++;
       pc = 1;
     }
     const bool pure_ilu = pc == 1;
@@ -525,6 +560,7 @@ struct Driver {
         double* zj = wk.Z + (size_t)j * N;
         double* wj = wk.V + (size_t)(j + 1) * N;  // the new vector, orthogonalised in place
         bool have_sq = false;
+        const auto t_it = std::chrono::steady_clock::now();
         int rc = psolve(y, vj, zj, c->d_scal, &have_sq);
         if (rc) return rc;
         rc = jv(y, fy, zj, wj, gamma, ynorm, have_sq);
@@ -565,6 +601,9 @@ struct Driver {
           hn2 = hbuf[3 * kMaxVec];
           reorth++;
         }
+        // the fetch synchronised the stream: the host clock has the iteration's whole cost
+        note_iteration_time(std::chrono::duration<double, std::milli>(
+                                std::chrono::steady_clock::now() - t_it).count());
         const double wn = std::sqrt(hn2);  // ||W_{j+1}||
         const double hn = sig[j] * wn;
         col[j + 1] = hn;
@@ -589,16 +628,23 @@ struct Driver {
         kend = j + 1;
         if (std::fabs(g[j + 1]) <= o.lin_rtol * bnorm || hn == 0.0) { conv = true; break; }
         // learned modes fall back when they stagnate, reach the ILU(0) iteration count, or
-        // fall behind the ILU(0) solve's mean reduction per iteration
-        // (a non-finite estimate -- a network output with NaN or Inf -- falls back too, and
-        // its column is left out of the update)
+        // fall behind the ILU(0) solve's mean reduction per iteration: the rest of the cycle
+        // runs with ILU(0), and flexible GMRES keeps the directions the network gave.  A
+        // non-finite estimate (a network output with NaN or Inf) leaves its column out and
+        // restarts the cycle with ILU(0) from the current iterate.
         const bool bad = !std::isfinite(g[j + 1]) || !std::isfinite(hn);
         if ((pc == 2 || pc == 4) &&
             (bad || *its >= ilu_ref_its || std::fabs(g[j + 1]) > 0.9 * std::fabs(g[j]) ||
              std::fabs(g[j + 1]) > beta * std::pow(ilu_ref_rate, j + 1))) {
-          if (bad) kend = j;
-          fallback = true;
-          break;
+          if (bad) {
+            kend = j;
+            fallback = true;
+            break;
+          }
+          wk.net_rate = std::pow(std::fabs(g[j + 1]) / beta, 1.0 / (j + 1));
+          note_fallback();
+          if (int rc = ensure_pset()) return rc;
+          extra_cycles++;  // ILU(0) keeps its full restart budget
         }
       }
       for (int l = kend - 1; l >= 0; l--) {
@@ -617,16 +663,14 @@ struct Driver {
       else d_written = true;
       if (conv) {
         if (pure_ilu) set_ilu_ref(*its, std::fabs(g[kend]), bnorm);
-        if (with_fallback && pc != 1) wk.learned_backoff = 0;  // the network won this solve
+        if (with_fallback && pc != 1) {  // the network won this solve
+          wk.learned_backoff = 0;
+          wk.net_rate = *its > 0 ? std::pow(std::fabs(g[kend]) / bnorm, 1.0 / *its) : 0.0;
+        }
         return 0;
       }
       if (fallback) {  // continue with ILU(0) from the current iterate
-        st.n_fallback++;
-        // exponential back-off: skip the network for the next 1, 4, 16, ... solves, so a
-        // network that keeps losing to ILU(0) costs a vanishing share of a long run
-        wk.learned_backoff = wk.learned_backoff ? std::min(4 * wk.learned_backoff, 1 << 20) : 1;
-        wk.learned_skip = wk.learned_backoff;
-        pc = 1;
+        note_fallback();
         if (int rc = ensure_pset()) return rc;
         extra_cycles++;
       } else if (cyc == o.max_restarts + extra_cycles) {
