@@ -799,7 +799,7 @@ def main():
             "alt_setup_policy": cvode,
             "stats": {k: st[k] for k in ("n_rhs", "n_jv", "n_psol", "n_pset", "n_newton",
                                           "n_lin_iters", "n_steps", "n_fallback", "n_learned",
-                                          "n_gated")},
+                                          "n_gated", "n_reorth")},
         }
         print(json.dumps(line), flush=True)
     if pg is not None:

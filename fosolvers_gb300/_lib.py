@@ -32,7 +32,7 @@ class BdfStats(C.Structure):
                 ("n_pset", C.c_long), ("n_newton", C.c_long), ("n_lin_iters", C.c_long),
                 ("n_steps", C.c_long), ("fails", C.c_long), ("n_fallback", C.c_long),
                 ("last_gnorm", C.c_double), ("t", C.c_double), ("n_learned", C.c_long),
-                ("n_gated", C.c_long)]
+                ("n_gated", C.c_long), ("n_reorth", C.c_long)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

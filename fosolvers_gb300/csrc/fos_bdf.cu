@@ -7,7 +7,8 @@
 //   BDF2: G(y) = y - 2/3 dt f(y) - (4/3 y_n - 1/3 y_{n-1})  gamma = 2/3 dt (first step BDF1)
 //   Newton: y_0 = y_n; stop when ||G(y_k)||_2 <= rtol ||y_n||_2 + atol sqrt(N), in FP64
 //   linear: right-preconditioned restarted GMRES(maxl) on J_G d = -G, Arnoldi by classical
-//           Gram--Schmidt in FP64 with a second pass when ||w_1|| < ||w_0||/sqrt(2) (DGKS),
+//           Gram--Schmidt in FP64 with a second pass when ||w_1||^2 < min(1/2, lin_rtol)
+//           ||w_0||^2 (the DGKS test, threshold bounded by the Krylov tolerance),
 //           Givens least squares on the host, stop at ||r|| <= lin_rtol ||G||
 //   J_G v = v - gamma (f(y + s v) - f(y))/s, s = jv_eps (1 + ||y||)/||v|| (fused kernel)
 //   preconditioner: pset once per BDF step (jok = 0 unless jac_reuse), psol = block ILU(0)
@@ -149,20 +150,30 @@ __global__ void k_axpy(long n, double a, const double* __restrict__ x, double* _
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) y[i] += a * x[i];
 }
-// s = sum_l c[l] Z_l, summed from x (acc) or from zero; then x = s, or, with yadd, yadd += s
+// s = sum_l c[l] Z_l, summed from x (kAcc) or from zero; then x = s, or, with kAdd, yadd += s
 // and x is not touched (the first restart cycle's correction added straight to the Newton
-// iterate: the same sums as x = s followed by yadd += x)
+// iterate: the same sums as x = s followed by yadd += x).  The variants are compile-time and
+// the vector loop is not unrolled, so no FP64 instruction is issued predicated off.
+template <bool kAcc, bool kAdd>
 __global__ void k_comb(long n, int nv, const double* __restrict__ Z, long ldz,
-                       const double* __restrict__ cc, double* __restrict__ x, int acc,
+                       const double* __restrict__ cc, double* __restrict__ x,
                        double* __restrict__ yadd) {
   __shared__ double cs[kMaxVec];
   if (threadIdx.x < kMaxVec) cs[threadIdx.x] = threadIdx.x < nv ? cc[threadIdx.x] : 0.0;
   __syncthreads();
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double s = acc ? x[i] : 0.0;
-  for (int l = 0; l < nv; l++) s += cs[l] * Z[(size_t)l * ldz + i];
-  if (yadd) yadd[i] += s;
+  double s = 0.0;
+  int l0 = 0;
+  if constexpr (kAcc) {
+    s = x[i];
+  } else if (nv > 0) {
+    s = cs[0] * Z[i];
+    l0 = 1;
+  }
+#pragma unroll 1
+  for (int l = l0; l < nv; l++) s = fma(cs[l], Z[(size_t)l * ldz + i], s);
+  if constexpr (kAdd) yadd[i] += s;
   else x[i] = s;
 }
 // hist = y_n (q=1) or 4/3 y_n - 1/3 y_{n-1} (q=2)
@@ -183,11 +194,13 @@ __global__ void __launch_bounds__(kT) k_newton_res(long n, const double* __restr
   double acc[2] = {0.0, 0.0};
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     const double yi = y[i];
-    const double G = yi - gamma * f[i] - hist[i];
-    b[i] = -G;
-    b2[i] = -G;
-    acc[0] += G * G;
-    acc[1] += yi * yi;
+    // -G = (gamma f - y) + hist, formed directly: round-to-nearest is symmetric, so this is
+    // -(fma(-gamma, f, y) - hist) bit for bit, without a negation on the FP64 pipe
+    const double B = fma(gamma, f[i], -yi) + hist[i];
+    b[i] = B;
+    b2[i] = B;
+    acc[0] = fma(B, B, acc[0]);
+    acc[1] = fma(yi, yi, acc[1]);
   }
   block_reduce_store<2>(acc, 2, part);
 }
@@ -529,6 +542,14 @@ struct Driver {
     // sig[j] sig[l], and the solution is sum_l y_l sig[l] z'_l.  No pass over the basis
     // normalises it.
     std::vector<double> sig(m + 1, 1.0), sig2(m + 1, 1.0);
+    // Second Gram--Schmidt pass when ||w'||^2 < min(1/2, lin_rtol) ||w||^2: the DGKS test with
+    // its threshold bounded by the Krylov tolerance.  A single classical pass that cancelled
+    // a factor k = ||w|| / ||w'|| leaves the new vector orthogonal to ~eps k; with k below
+    // lin_rtol^(-1/2) (32 at the default 1e-3) that is ~1e-14, far inside what a solve to
+    // lin_rtol notices, and the second pass -- nearly a full sweep over the basis in FP64
+    // -- runs only on the steps that cancel more (the plain 1/2 threshold reran it on
+    // almost every step of a well-preconditioned solve, where J M^-1 v is close to v).
+    const double reorth_frac = std::min(0.5, o.lin_rtol);
     double* d_sig2 = wk.sc + 5 * kMaxVec;
     if (added) *added = false;
     bool d_written = false;  // wk.d holds the correction of the cycles so far
@@ -567,8 +588,8 @@ struct Driver {
         if (rc) return rc;
         (*its)++;
         const int nv = j + 1;
-        // classical Gram--Schmidt, re-orthogonalised only when the first pass removed more
-        // than 1 - 1/sqrt(2) of ||w|| (Daniel--Gragg--Kaufman--Stewart criterion)
+        // classical Gram--Schmidt, re-orthogonalised only when the first pass cancelled
+        // more than the threshold above (Daniel--Gragg--Kaufman--Stewart test)
         // When the previous step needed the second pass, the first update also returns
         // V^T w' (MODE 2) so the second pass needs no separate sweep over V for its
         // coefficients; otherwise it returns ||w'||^2 only (MODE 1).
@@ -587,7 +608,7 @@ struct Driver {
         double* col = &H[(size_t)(m + 1) * j];
         for (int l = 0; l < nv; l++) col[l] = sig[j] * sig[l] * hbuf[l];
         double hn2 = hbuf[kMaxVec + nv];
-        last_reorth = hn2 < 0.5 * hbuf[nv];
+        last_reorth = hn2 < reorth_frac * hbuf[nv];
         if (last_reorth) {
           const double* h2 = wk.sc + kMaxVec;  // V^T w' (device), from MODE 2 or a sweep
           if (!fused) {
@@ -600,6 +621,7 @@ struct Driver {
           for (int l = 0; l < nv; l++) col[l] += sig[j] * sig[l] * hbuf[kMaxVec + l];
           hn2 = hbuf[3 * kMaxVec];
           reorth++;
+          st.n_reorth++;
         }
         // the fetch synchronised the stream: the host clock has the iteration's whole cost
         note_iteration_time(std::chrono::duration<double, std::milli>(
@@ -656,8 +678,16 @@ struct Driver {
       FOS_CUDA(cudaMemcpyAsync(wk.sc + 4 * kMaxVec, yv.data(), sizeof(double) * kend,
                                cudaMemcpyHostToDevice, c->stream));
       double* yadd = (conv && !d_written && y_add) ? y_add : nullptr;
-      fos_launch(c, k_comb, nb(N), kT, N, kend, (const double*)wk.Z, N,
-                 (const double*)(wk.sc + 4 * kMaxVec), wk.d, d_written ? 1 : 0, yadd);
+      {
+        const double* cz = wk.sc + 4 * kMaxVec;
+        const double* Zc = wk.Z;
+        if (yadd)  // (only while d holds nothing yet)
+          fos_launch(c, k_comb<false, true>, nb(N), kT, N, kend, Zc, N, cz, wk.d, yadd);
+        else if (d_written)
+          fos_launch(c, k_comb<true, false>, nb(N), kT, N, kend, Zc, N, cz, wk.d, yadd);
+        else
+          fos_launch(c, k_comb<false, false>, nb(N), kT, N, kend, Zc, N, cz, wk.d, yadd);
+      }
       FOS_LAUNCH_CHECK();
       if (yadd) *added = true;
       else d_written = true;

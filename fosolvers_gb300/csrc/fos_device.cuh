@@ -188,10 +188,14 @@ __device__ __forceinline__ df2 df_from_double(double x) {
   }
   return {d2f_trunc(x), l};
 }
-// finiteness from the exponent field (integer instructions, no FP64 compare)
+// -x by flipping the sign bit (an integer instruction, not the FP64 pipe)
+__device__ __forceinline__ double neg_bits(double x) {
+  return __hiloint2double(__double2hiint(x) ^ (int)0x80000000u, __double2loint(x));
+}
+// finiteness from the exponent field of the high word (one 32-bit integer test, no FP64
+// compare)
 __device__ __forceinline__ bool finite_bits(double x) {
-  return ((unsigned long long)__double_as_longlong(x) & 0x7ff0000000000000ull) !=
-         0x7ff0000000000000ull;
+  return ((unsigned)__double2hiint(x) & 0x7ff00000u) != 0x7ff00000u;
 }
 
 // 1/a in FP64 by Newton--Raphson iteration x <- x (2 - a x) from an FP32 seed (two steps

@@ -705,22 +705,27 @@ __global__ void k_ilu_out(int nC, const int* __restrict__ ipos, const TF* __rest
 
 // k_ilu_out plus the partial sums of z^2 (the norm the finite-difference Jv of z needs):
 // fixed grid (kRedBlocks x kRedThreads), cells by grid stride, one partial per block in a
-// fixed order, so the sum is deterministic
+// fixed order, so the sum is deterministic.  With FP32 factors each thread sums its squares
+// in FP32 (the norm only scales the increment s, and the Jv divides by the same s; a
+// relative error of ~1e-6 in s is immaterial) and the block sums those partials in FP64:
+// no FP64 instruction per element, the pipe GB300 has least of.
 template <typename TF>
 __global__ void __launch_bounds__(kRedThreads) k_ilu_out_sq(int nC, const int* __restrict__ ipos,
                                                             const TF* __restrict__ zv,
                                                             double* __restrict__ z,
                                                             double* __restrict__ part) {
-  double acc = 0.0;
+  TF acc_t = TF(0);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nC; i += gridDim.x * blockDim.x) {
     const TF* src = zv + 8 * (size_t)ipos[i];
 #pragma unroll
     for (int a = 0; a < 5; a++) {
-      const double v = to64<TF>(src[a]);
-      z[(size_t)a * nC + i] = v;
-      acc = fma(v, v, acc);
+      const TF v = src[a];
+      z[(size_t)a * nC + i] = to64<TF>(v);
+      if constexpr (sizeof(TF) == 4) acc_t = fmaf(v, v, acc_t);
+      else acc_t = fma(v, v, acc_t);
     }
   }
+  double acc = to64<TF>(acc_t);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   __shared__ double sh[kRedThreads / 32];

@@ -158,7 +158,7 @@ __global__ void __launch_bounds__(kThreads) k_face64(
 // Per-cell gather.  ELL layout: every cell has kW entry slots (face << 1 | cell-is-R,
 // -1 = empty), loaded as one int4 for kW = 4 (tetrahedra), so all face loads of a cell
 // are issued together; the fixed slot order gives a deterministic summation order.
-// mode 0: out = sum/v ; mode 1: out = a*v + b*(sum/v - fy)/s
+// residual: out = sum/v ; Jv: out = a*v + b*(sum/v - fy)/s (gather_epilogue)
 template <int kW>
 __device__ __forceinline__ void load_ell(const int* __restrict__ ell, int c, int e[kW]) {
   if (kW == 4) {
@@ -170,17 +170,25 @@ __device__ __forceinline__ void load_ell(const int* __restrict__ ell, int c, int
   }
 }
 
-// out = acc / v (mode 0) or the Jv combination a v + (b / s)(acc / v - fy) (mode 1), in
-// FP64; b / s comes precomputed in d_s[2] (k_sigma), and amode says whether a is 1 (1), 0 (0)
-// or neither (2), so no FP64 compare or multiply runs per cell for the coefficients;
-// non-finite results are flagged from the exponent bits (no FP64 compares)
+// The epilogue kind, a template parameter so that each kernel carries only its own FP64
+// instructions (the FP64 pipe is GB300's scarcest): kEpiRhs out = acc / v; the Jv
+// combination a v + (b / s)(acc / v - fy) with a = 1 (kEpiJv1), a = 0 (kEpiJv0) or any a
+// (kEpiJvA).
+enum { kEpiRhs = 0, kEpiJv1 = 1, kEpiJv0 = 2, kEpiJvA = 3 };
+inline int epi_kind(int mode, double a) {
+  return mode == 0 ? kEpiRhs : a == 1.0 ? kEpiJv1 : a == 0.0 ? kEpiJv0 : kEpiJvA;
+}
+
+// The epilogue in FP64; b / s comes precomputed in d_s[2] (k_sigma); non-finite results are
+// flagged from the exponent bits (no FP64 compares)
+template <int kE>
 __device__ __forceinline__ void gather_epilogue(int nC, int c, const double acc[5], double iv,
-                                                int mode, const double* __restrict__ vv,
+                                                const double* __restrict__ vv,
                                                 const double* __restrict__ fy,
-                                                const double* __restrict__ d_s, double a, int amode,
+                                                const double* __restrict__ d_s, double a,
                                                 double* __restrict__ out, int* __restrict__ flag) {
   bool ok = true;
-  if (mode == 0) {
+  if constexpr (kE == kEpiRhs) {
 #pragma unroll
     for (int q = 0; q < 5; q++) {
       const double o = acc[q] * iv;
@@ -193,7 +201,10 @@ __device__ __forceinline__ void gather_epilogue(int nC, int c, const double acc[
     for (int q = 0; q < 5; q++) {
       const size_t k = (size_t)q * nC + c;
       const double t = fma(acc[q], iv, -fy[k]);
-      const double o = amode == 1 ? fma(bs, t, vv[k]) : amode == 0 ? bs * t : fma(bs, t, a * vv[k]);
+      double o;
+      if constexpr (kE == kEpiJv1) o = fma(bs, t, vv[k]);
+      else if constexpr (kE == kEpiJv0) o = bs * t;
+      else o = fma(bs, t, a * vv[k]);
       ok &= finite_bits(o);
       out[k] = o;
     }
@@ -201,11 +212,11 @@ __device__ __forceinline__ void gather_epilogue(int nC, int c, const double acc[
   if (!ok && flag) atomicOr(flag, 1);
 }
 
-template <int kW>
+template <int kW, int kE>
 __global__ void __launch_bounds__(kThreads) k_gather(
     int nC, const int* __restrict__ ell, const double* __restrict__ F,
-    const double* __restrict__ invV, int mode, const double* __restrict__ vv,
-    const double* __restrict__ fy, const double* __restrict__ d_s, double a, int amode,
+    const double* __restrict__ invV, const double* __restrict__ vv,
+    const double* __restrict__ fy, const double* __restrict__ d_s, double a,
     double* __restrict__ out, int* __restrict__ flag) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nC) return;
@@ -221,7 +232,21 @@ __global__ void __launch_bounds__(kThreads) k_gather(
     acc[0] += sg * a0.x; acc[1] += sg * a0.y; acc[2] += sg * a1.x; acc[3] += sg * a1.y;
     acc[4] += sg * a2.x;
   }
-  gather_epilogue(nC, c, acc, __ldg(invV + c), mode, vv, fy, d_s, a, amode, out, flag);
+  gather_epilogue<kE>(nC, c, acc, __ldg(invV + c), vv, fy, d_s, a, out, flag);
+}
+
+using gather_fn = decltype(&k_gather<4, kEpiRhs>);
+template <int kW>
+gather_fn gather_kernel_w(int ek) {
+  switch (ek) {
+    case kEpiRhs: return k_gather<kW, kEpiRhs>;
+    case kEpiJv1: return k_gather<kW, kEpiJv1>;
+    case kEpiJv0: return k_gather<kW, kEpiJv0>;
+    default: return k_gather<kW, kEpiJvA>;
+  }
+}
+gather_fn gather_kernel(int ell_w, int ek) {
+  return ell_w == 4 ? gather_kernel_w<4>(ek) : gather_kernel_w<6>(ek);
 }
 
 // ------------------------------------------------------------------ FP32 flux
@@ -231,6 +256,9 @@ __global__ void __launch_bounds__(kThreads) k_gather(
 // double-float arithmetic (df_*: FP32 pipe); only the Jv perturbation y + s v is FP64.
 // Layout: 16 floats (64 B) per cell = (rho, u, v, w, H, p) hi, (rho, u, v, w, H, p) lo,
 // sqrt(rho), 0, 0, 0.
+// kV: the state is y + s v (a Jv), else y; a compile-time switch, so a residual issues no
+// predicated-off FP64 FMAs
+template <bool kV>
 __global__ void __launch_bounds__(kThreads) k_prim_hl(int nC, const double* __restrict__ y,
                                                       const double* __restrict__ v,
                                                       const double* __restrict__ d_s, double gm1,
@@ -240,7 +268,7 @@ __global__ void __launch_bounds__(kThreads) k_prim_hl(int nC, const double* __re
   double U[5];
 #pragma unroll
   for (int q = 0; q < 5; q++) U[q] = y[(size_t)q * nC + c];
-  if (v) {
+  if constexpr (kV) {
     const double s = *d_s;
 #pragma unroll
     for (int q = 0; q < 5; q++) U[q] = fma(s, v[(size_t)q * nC + c], U[q]);
@@ -382,16 +410,16 @@ __global__ void __launch_bounds__(kThreads) k_bface32(
 // kHyb (FOS_FLUX_HYBRID): a face whose relative density or pressure jump exceeds theta is
 // evaluated in FP64 (the same expressions, from the FP64 values of the (hi, lo) pairs and
 // the FP64 geometry); both cells decide from the same face-oriented values, so they agree.
-// A residual (mode 0) records the choice per face (fsel, written by the face's L cell); a
-// Jv (mode 1) reuses it, so f(y + s v) and f(y) evaluate every face the same way.
-template <int kW, bool kHyb>
+// A residual (kEpiRhs) records the choice per face (fsel, written by the face's L cell); a
+// Jv reuses it, so f(y + s v) and f(y) evaluate every face the same way.
+template <int kW, bool kHyb, int kE, bool kSc>
 __global__ void __launch_bounds__(kThreads) k_cell32(
     int nC, int nFi, const int* __restrict__ ell, const int2* __restrict__ faceLR,
     const float4* __restrict__ faceNA, const float* __restrict__ W, float gm1,
     const double* __restrict__ Fb, const float4* __restrict__ Sc,
-    const double* __restrict__ invV, int mode,
+    const double* __restrict__ invV,
     const double* __restrict__ vv, const double* __restrict__ fy, const double* __restrict__ d_s,
-    double a, int amode, double* __restrict__ out, int* __restrict__ flag,
+    double a, double* __restrict__ out, int* __restrict__ flag,
     const double2* __restrict__ faceNA64, unsigned char* __restrict__ fsel, float theta,
     double gm1d) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -401,7 +429,9 @@ __global__ void __launch_bounds__(kThreads) k_cell32(
   PHL P;
   load_hl(W, c, P);
   // FP64 accumulation in ELL order; the first face initialises the sums (every cell has
-  // at least one face, and ELL rows are padded at the end)
+  // at least one face, and ELL rows are padded at the end).  The terms come negated from
+  // the face arithmetic (FP32 or FP64, where negation is exact), so the sums are plain
+  // additions: acc = n_0 + n_1 + ..., no FP64 negation for the first term
   double acc[5];
 #pragma unroll
   for (int k = 0; k < kW; k++) {
@@ -425,10 +455,10 @@ __global__ void __launch_bounds__(kThreads) k_cell32(
       }
       bool f64 = false;
       if (kHyb) {
-        if (mode == 0 || !fsel) {
+        if (kE == kEpiRhs || !fsel) {
           f64 = fabsf(d[0]) > theta * fminf(L.h[0], R.h[0]) ||
                 fabsf(d[5]) > theta * fminf(L.h[5], R.h[5]);
-          if (mode == 0 && fsel && !isR) fsel[f] = f64 ? 1 : 0;
+          if (kE == kEpiRhs && fsel && !isR) fsel[f] = f64 ? 1 : 0;
         } else {
           f64 = __ldg(fsel + f) != 0;
         }
@@ -449,22 +479,26 @@ __global__ void __launch_bounds__(kThreads) k_cell32(
                              dd[4], dd[5], sqrt(rl), sqrt(rr), n01.x, n01.y, n2a.x, n2a.y, gm1d,
                              dF64, dw64);
 #pragma unroll
-        for (int q = 0; q < 5; q++) t[q] = isR ? dF64[q] + dw64[q] : dF64[q] - dw64[q];
+        for (int q = 0; q < 5; q++) t[q] = isR ? -dF64[q] - dw64[q] : dw64[q] - dF64[q];
       } else {
         roe_split_mj<float>(m[0], d[0], m[1], d[1], m[2], d[2], m[3], d[3], m[4], d[4], d[5],
                             L.s, R.s, na.x, na.y, na.z, na.w, gm1, dF, dw);
 #pragma unroll
-        for (int q = 0; q < 5; q++) t[q] = f2d_bits(fmaf(sw, dw[q], dF[q]));
+        for (int q = 0; q < 5; q++) t[q] = f2d_bits(fmaf(-sw, dw[q], -dF[q]));
       }
-    } else {  // boundary face (cell is L): the FP64 difference of k_bface32
+    } else {  // boundary face (cell is L): the FP64 difference of k_bface32, negated
       const double2* F2 = reinterpret_cast<const double2*>(Fb + 6 * (size_t)f);
       const double2 a0 = __ldg(F2), a1 = __ldg(F2 + 1), a2 = __ldg(F2 + 2);
-      t[0] = a0.x; t[1] = a0.y; t[2] = a1.x; t[3] = a1.y; t[4] = a2.x;
+      t[0] = neg_bits(a0.x); t[1] = neg_bits(a0.y); t[2] = neg_bits(a1.x);
+      t[3] = neg_bits(a1.y); t[4] = neg_bits(a2.x);
     }
 #pragma unroll
-    for (int q = 0; q < 5; q++) acc[q] = k == 0 ? -t[q] : acc[q] - t[q];
+    for (int q = 0; q < 5; q++) acc[q] = k == 0 ? t[q] : acc[q] + t[q];
   }
-  if (Sc) {  // own flux through the closure vector: rho u.S, rho u u.S + p S, rho H u.S
+  // own flux through the closure vector (kSc: the grid has cells whose faces do not close):
+  // rho u.S, rho u u.S + p S, rho H u.S.  A compile-time switch: as a run-time branch the
+  // five FP64 subtractions were issued predicated off on every cell, occupying the FP64 pipe
+  if constexpr (kSc) {
     const float4 S = __ldg(Sc + c);
     const float t = P.h[0] * (P.h[1] * S.x + P.h[2] * S.y + P.h[3] * S.z);
     acc[0] -= f2d_bits(t);
@@ -473,13 +507,27 @@ __global__ void __launch_bounds__(kThreads) k_cell32(
     acc[3] -= f2d_bits(fmaf(t, P.h[3], P.h[5] * S.z));
     acc[4] -= f2d_bits(t * P.h[4]);
   }
-  gather_epilogue(nC, c, acc, __ldg(invV + c), mode, vv, fy, d_s, a, amode, out, flag);
+  gather_epilogue<kE>(nC, c, acc, __ldg(invV + c), vv, fy, d_s, a, out, flag);
 }
 
-using cell32_fn = decltype(&k_cell32<4, false>);
-cell32_fn cell32_kernel(int ell_w, bool hyb) {
-  if (ell_w == 4) return hyb ? k_cell32<4, true> : k_cell32<4, false>;
-  return hyb ? k_cell32<6, true> : k_cell32<6, false>;
+using cell32_fn = decltype(&k_cell32<4, false, kEpiRhs, false>);
+template <int kW, bool kHyb, bool kSc>
+cell32_fn cell32_kernel_whs(int ek) {
+  switch (ek) {
+    case kEpiRhs: return k_cell32<kW, kHyb, kEpiRhs, kSc>;
+    case kEpiJv1: return k_cell32<kW, kHyb, kEpiJv1, kSc>;
+    case kEpiJv0: return k_cell32<kW, kHyb, kEpiJv0, kSc>;
+    default: return k_cell32<kW, kHyb, kEpiJvA, kSc>;
+  }
+}
+template <int kW, bool kHyb>
+cell32_fn cell32_kernel_wh(int ek, bool sc) {
+  return sc ? cell32_kernel_whs<kW, kHyb, true>(ek) : cell32_kernel_whs<kW, kHyb, false>(ek);
+}
+cell32_fn cell32_kernel(int ell_w, bool hyb, int ek, bool sc) {
+  if (ell_w == 4)
+    return hyb ? cell32_kernel_wh<4, true>(ek, sc) : cell32_kernel_wh<4, false>(ek, sc);
+  return hyb ? cell32_kernel_wh<6, true>(ek, sc) : cell32_kernel_wh<6, false>(ek, sc);
 }
 
 __global__ void k_permute(int nC, int nplanes, const int* __restrict__ idx,
@@ -554,9 +602,10 @@ int fos_residual_launch(fos_ctx* c, const double* y, const double* v, const doub
                         const double* fy, double* out, double a, double b, int mode) {
   (void)b;  // b / s comes from the preceding fos_jv_sigma* (d_s[2])
   const double gm1 = c->gamm - 1.0;
-  const int amode = a == 1.0 ? 1 : a == 0.0 ? 0 : 2;
+  const int ek = epi_kind(mode, a);
   if (c->flags & FOS_FLUX_FP32) {
-    fos_launch(c, k_prim_hl, nblk(c->nC), kThreads, c->nC, y, v, d_s, gm1, c->d_Whl);
+    if (v) fos_launch(c, k_prim_hl<true>, nblk(c->nC), kThreads, c->nC, y, v, d_s, gm1, c->d_Whl);
+    else fos_launch(c, k_prim_hl<false>, nblk(c->nC), kThreads, c->nC, y, v, d_s, gm1, c->d_Whl);
     const bool hyb = (c->flags & FOS_FLUX_HYBRID) != 0;
     if (c->nFb)
       fos_launch(c, k_bface32, nblk(c->nFb), kThreads, c->nFi, c->nF, c->nC,
@@ -564,10 +613,10 @@ int fos_residual_launch(fos_ctx* c, const double* y, const double* v, const doub
                  (const float4*)c->d_faceNA32, (const float*)c->d_Whl, (float)gm1, y, v, d_s,
                  (const int*)c->d_bcT, (const double*)c->d_bcP, c->maxP, c->gamm, c->r, c->d_F,
                  hyb ? 1 : 0);
-    fos_launch(c, cell32_kernel(c->ell_w, hyb), nblk(c->nC), kThreads, c->nC, c->nFi,
+    fos_launch(c, cell32_kernel(c->ell_w, hyb, ek, c->d_closure32 != nullptr), nblk(c->nC), kThreads, c->nC, c->nFi,
                (const int*)c->d_ell, (const int2*)c->d_faceLR, (const float4*)c->d_faceNA32,
                (const float*)c->d_Whl, (float)gm1, (const double*)c->d_F,
-               (const float4*)c->d_closure32, (const double*)c->d_invV, mode, v, fy, d_s, a, amode,
+               (const float4*)c->d_closure32, (const double*)c->d_invV, v, fy, d_s, a,
                out, c->d_flag, (const double2*)c->d_faceNA, c->d_fsel, (float)c->hyb_theta, gm1);
   } else {
     fos_launch(c, k_prim64, nblk(c->nC), kThreads, c->nC, y, v, d_s, gm1, c->d_W);
@@ -575,21 +624,16 @@ int fos_residual_launch(fos_ctx* c, const double* y, const double* v, const doub
                (const int2*)c->d_faceLR, (const double2*)c->d_faceNA, (const double*)c->d_W, y, v,
                d_s, (const int*)c->d_bcT, (const double*)c->d_bcP, c->maxP, c->gamm, c->r,
                c->d_F);
-    if (c->ell_w == 4)
-      fos_launch(c, k_gather<4>, nblk(c->nC), kThreads, c->nC, (const int*)c->d_ell,
-                 (const double*)c->d_F, (const double*)c->d_invV, mode, v, fy, d_s, a, amode, out,
-                 c->d_flag);
-    else
-      fos_launch(c, k_gather<6>, nblk(c->nC), kThreads, c->nC, (const int*)c->d_ell,
-                 (const double*)c->d_F, (const double*)c->d_invV, mode, v, fy, d_s, a, amode, out,
-                 c->d_flag);
+    fos_launch(c, gather_kernel(c->ell_w, ek), nblk(c->nC), kThreads, c->nC,
+               (const int*)c->d_ell, (const double*)c->d_F, (const double*)c->d_invV, v, fy, d_s,
+               a, out, c->d_flag);
   }
   FOS_LAUNCH_CHECK();
   return 0;
 }
 
 int fos_prim_hl_launch(fos_ctx* c, const double* y) {
-  fos_launch(c, k_prim_hl, nblk(c->nC), kThreads, c->nC, y, nullptr, nullptr, c->gamm - 1.0,
+  fos_launch(c, k_prim_hl<false>, nblk(c->nC), kThreads, c->nC, y, nullptr, nullptr, c->gamm - 1.0,
              c->d_Whl);
   FOS_LAUNCH_CHECK();
   return 0;
@@ -711,7 +755,7 @@ extern "C" int fos_euler_rhs_dev_static(const fos_ctx* c, double t, const double
   if (c->flags & FOS_FLUX_FP32) {
     float* Whl = reinterpret_cast<float*>(bytes);
     double* F = reinterpret_cast<double*>(bytes + kStaticCellBytes);
-    k_prim_hl<<<nblk(c->nC), kThreads, 0, s>>>(c->nC, y, nullptr, nullptr, gm1, Whl);
+    k_prim_hl<false><<<nblk(c->nC), kThreads, 0, s>>>(c->nC, y, nullptr, nullptr, gm1, Whl);
     const bool hyb = (c->flags & FOS_FLUX_HYBRID) != 0;
     if (c->nFb)
       k_bface32<<<nblk(c->nFb), kThreads, 0, s>>>(c->nFi, c->nF, c->nC, c->d_faceLR,
@@ -719,9 +763,9 @@ extern "C" int fos_euler_rhs_dev_static(const fos_ctx* c, double t, const double
                                                   nullptr, nullptr, c->d_bcT, c->d_bcP, c->maxP,
                                                   c->gamm, c->r, F, hyb ? 1 : 0);
     // the face choice of the hybrid flux is made from this state (no record kept)
-    cell32_kernel(c->ell_w, hyb)<<<nblk(c->nC), kThreads, 0, s>>>(
+    cell32_kernel(c->ell_w, hyb, kEpiRhs, c->d_closure32 != nullptr)<<<nblk(c->nC), kThreads, 0, s>>>(
         c->nC, c->nFi, c->d_ell, c->d_faceLR, c->d_faceNA32, Whl, (float)gm1, F, c->d_closure32,
-        c->d_invV, 0, nullptr, nullptr, nullptr, 0.0, 0, ydot, nullptr, c->d_faceNA, nullptr,
+        c->d_invV, nullptr, nullptr, nullptr, 0.0, ydot, nullptr, c->d_faceNA, nullptr,
         (float)c->hyb_theta, gm1);
   } else {
     double* W = reinterpret_cast<double*>(bytes);
@@ -730,12 +774,8 @@ extern "C" int fos_euler_rhs_dev_static(const fos_ctx* c, double t, const double
     k_face64<<<nblk(c->nF), kThreads, 0, s>>>(c->nFi, c->nF, c->nC, c->d_faceLR, c->d_faceNA, W,
                                               y, nullptr, nullptr, c->d_bcT, c->d_bcP, c->maxP,
                                               c->gamm, c->r, F);
-    if (c->ell_w == 4)
-      k_gather<4><<<nblk(c->nC), kThreads, 0, s>>>(c->nC, c->d_ell, F, c->d_invV, 0, nullptr,
-                                                   nullptr, nullptr, 0.0, 0, ydot, nullptr);
-    else
-      k_gather<6><<<nblk(c->nC), kThreads, 0, s>>>(c->nC, c->d_ell, F, c->d_invV, 0, nullptr,
-                                                   nullptr, nullptr, 0.0, 0, ydot, nullptr);
+    gather_kernel(c->ell_w, kEpiRhs)<<<nblk(c->nC), kThreads, 0, s>>>(
+        c->nC, c->d_ell, F, c->d_invV, nullptr, nullptr, nullptr, 0.0, ydot, nullptr);
   }
   FOS_LAUNCH_CHECK();
   return 0;

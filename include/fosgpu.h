@@ -280,6 +280,7 @@ typedef struct {
   long n_learned;     /* applications of the learned preconditioner (of n_psol) */
   long n_gated;       /* learned mode: solves run with ILU(0) alone because the network's
                          last measured cost per decade of residual was no better */
+  long n_reorth;      /* Arnoldi steps that needed the second Gram--Schmidt pass */
 } fos_bdf_stats;
 
 void fos_bdf_defaults(fos_bdf_opts* o);
