@@ -7,8 +7,8 @@
 //   BDF2: G(y) = y - 2/3 dt f(y) - (4/3 y_n - 1/3 y_{n-1})  gamma = 2/3 dt (first step BDF1)
 //   Newton: y_0 = y_n; stop when ||G(y_k)||_2 <= rtol ||y_n||_2 + atol sqrt(N), in FP64
 //   linear: right-preconditioned restarted GMRES(maxl) on J_G d = -G, Arnoldi by classical
-//           Gram--Schmidt in FP64 with a second pass when ||w_1||^2 < min(1/2, lin_rtol)
-//           ||w_0||^2 (the DGKS test, threshold bounded by the Krylov tolerance),
+//           Gram--Schmidt in FP64 with a second pass when ||w_1|| < min(1/sqrt(2), lin_rtol)
+//           ||w_0|| (the DGKS test, threshold bounded by the Krylov tolerance),
 //           Givens least squares on the host, stop at ||r|| <= lin_rtol ||G||
 //   J_G v = v - gamma (f(y + s v) - f(y))/s, s = jv_eps (1 + ||y||)/||v|| (fused kernel)
 //   preconditioner: pset once per BDF step (jok = 0 unless jac_reuse), psol = block ILU(0)
@@ -542,14 +542,15 @@ struct Driver {
     // sig[j] sig[l], and the solution is sum_l y_l sig[l] z'_l.  No pass over the basis
     // normalises it.
     std::vector<double> sig(m + 1, 1.0), sig2(m + 1, 1.0);
-    // Second Gram--Schmidt pass when ||w'||^2 < min(1/2, lin_rtol) ||w||^2: the DGKS test with
-    // its threshold bounded by the Krylov tolerance.  A single classical pass that cancelled
-    // a factor k = ||w|| / ||w'|| leaves the new vector orthogonal to ~eps k; with k below
-    // lin_rtol^(-1/2) (32 at the default 1e-3) that is ~1e-14, far inside what a solve to
-    // lin_rtol notices, and the second pass -- nearly a full sweep over the basis in FP64
-    // -- runs only on the steps that cancel more (the plain 1/2 threshold reran it on
-    // almost every step of a well-preconditioned solve, where J M^-1 v is close to v).
-    const double reorth_frac = std::min(0.5, o.lin_rtol);
+    // Second Gram--Schmidt pass when ||w'|| < min(1/sqrt(2), lin_rtol) ||w||: the DGKS test
+    // with its threshold bounded by the Krylov tolerance.  A single classical pass that
+    // cancelled a factor k = ||w|| / ||w'|| leaves the new vector orthogonal to the basis to
+    // ~eps k; with k below 1 / lin_rtol that is at most eps / lin_rtol per step (2e-13 at the
+    // default 1e-3, 7e-12 over 30 steps), six orders inside the tolerance the solve is
+    // checked against.  The second pass -- nearly a full sweep over the basis in FP64 -- runs
+    // only on the steps that cancel more (the plain 1/sqrt(2) threshold reran it on almost
+    // every step of a well-preconditioned solve, where J M^-1 v is close to v).
+    const double reorth_frac = std::min(0.5, o.lin_rtol * o.lin_rtol);
     double* d_sig2 = wk.sc + 5 * kMaxVec;
     if (added) *added = false;
     bool d_written = false;  // wk.d holds the correction of the cycles so far

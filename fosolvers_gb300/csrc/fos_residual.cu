@@ -96,6 +96,8 @@ __device__ __forceinline__ void roe_flow64(const P64& L, const P64& R, double nx
   flow[4] = aP * (0.5 * (mL * L.H + mR * R.H) - 0.5 * d4);
 }
 
+// kV: the state is y + s v (a Jv), else y (compile-time, as in k_prim_hl)
+template <bool kV>
 __global__ void __launch_bounds__(kThreads) k_prim64(int nC, const double* __restrict__ y,
                                                      const double* __restrict__ v,
                                                      const double* __restrict__ d_s, double gm1,
@@ -105,7 +107,7 @@ __global__ void __launch_bounds__(kThreads) k_prim64(int nC, const double* __res
   double U[5];
 #pragma unroll
   for (int q = 0; q < 5; q++) U[q] = y[(size_t)q * nC + c];
-  if (v) {
+  if constexpr (kV) {
     const double s = *d_s;
 #pragma unroll
     for (int q = 0; q < 5; q++) U[q] = U[q] + s * v[(size_t)q * nC + c];
@@ -619,7 +621,8 @@ int fos_residual_launch(fos_ctx* c, const double* y, const double* v, const doub
                (const float4*)c->d_closure32, (const double*)c->d_invV, v, fy, d_s, a,
                out, c->d_flag, (const double2*)c->d_faceNA, c->d_fsel, (float)c->hyb_theta, gm1);
   } else {
-    fos_launch(c, k_prim64, nblk(c->nC), kThreads, c->nC, y, v, d_s, gm1, c->d_W);
+    if (v) fos_launch(c, k_prim64<true>, nblk(c->nC), kThreads, c->nC, y, v, d_s, gm1, c->d_W);
+    else fos_launch(c, k_prim64<false>, nblk(c->nC), kThreads, c->nC, y, v, d_s, gm1, c->d_W);
     fos_launch(c, k_face64, nblk(c->nF), kThreads, c->nFi, c->nF, c->nC,
                (const int2*)c->d_faceLR, (const double2*)c->d_faceNA, (const double*)c->d_W, y, v,
                d_s, (const int*)c->d_bcT, (const double*)c->d_bcP, c->maxP, c->gamm, c->r,
@@ -640,7 +643,7 @@ int fos_prim_hl_launch(fos_ctx* c, const double* y) {
 }
 
 int fos_prim_launch(fos_ctx* c, const double* y) {
-  fos_launch(c, k_prim64, nblk(c->nC), kThreads, c->nC, y, nullptr, nullptr, c->gamm - 1.0,
+  fos_launch(c, k_prim64<false>, nblk(c->nC), kThreads, c->nC, y, nullptr, nullptr, c->gamm - 1.0,
                                                     c->d_W);
   FOS_LAUNCH_CHECK();
   return 0;
@@ -770,7 +773,7 @@ extern "C" int fos_euler_rhs_dev_static(const fos_ctx* c, double t, const double
   } else {
     double* W = reinterpret_cast<double*>(bytes);
     double* F = reinterpret_cast<double*>(bytes + kStaticCellBytes);
-    k_prim64<<<nblk(c->nC), kThreads, 0, s>>>(c->nC, y, nullptr, nullptr, gm1, W);
+    k_prim64<false><<<nblk(c->nC), kThreads, 0, s>>>(c->nC, y, nullptr, nullptr, gm1, W);
     k_face64<<<nblk(c->nF), kThreads, 0, s>>>(c->nFi, c->nF, c->nC, c->d_faceLR, c->d_faceNA, W,
                                               y, nullptr, nullptr, c->d_bcT, c->d_bcP, c->maxP,
                                               c->gamm, c->r, F);

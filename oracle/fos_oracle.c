@@ -1238,8 +1238,8 @@ int oe_ilu_ierr(const oe_ctx* c) { return c->ierr; }
  *   G(y) = y - gamma f(t,y) - h,  gamma = beta*dt, h = history combination
  *   J_G v ~ v - gamma (f(y + s v) - f(y))/s,  s = jv_eps (1 + ||y||_2)/||v||_2
  *   right-preconditioned restarted GMRES(maxl), classical Gram-Schmidt with a second
- *   pass when ||w1||^2 < min(1/2, lin_rtol) ||w0||^2 (DGKS test, threshold bounded by the
- *   Krylov tolerance), Givens least squares, stop at ||r|| <= lin_rtol ||b||
+ *   pass when ||w1|| < min(1/sqrt(2), lin_rtol) ||w0|| (DGKS test, threshold bounded by
+ *   the Krylov tolerance), Givens least squares, stop at ||r|| <= lin_rtol ||b||
  *   Newton stops when ||G(y_k)||_2 <= rtol ||y_n||_2 + atol sqrt(n) (FP64 residual norm). */
 typedef struct {
   int n;
@@ -1326,12 +1326,12 @@ static int nk_gmres(nk_op* op, const double* b, double* x, int m, int max_restar
       rc = nk_matvec(op, zj, w);
       if (rc) { status = rc < 0 ? rc : -2; goto done; }
       it++;
-      /* classical Gram--Schmidt; second pass only when ||w1||^2 < min(1/2, rtol) ||w0||^2 */
+      /* classical Gram--Schmidt; second pass only when ||w1|| < min(1/sqrt(2), rtol) ||w0|| */
       double w0 = vdot(n, w, w);
       for (int l = 0; l <= j; l++) h[l] = vdot(n, V + (size_t)n * l, w);
       for (int l = 0; l <= j; l++) { const double* vl = V + (size_t)n * l; for (int i = 0; i < n; i++) w[i] -= h[l] * vl[i]; }
       double w1 = vdot(n, w, w);
-      if (w1 < (rtol < 0.5 ? rtol : 0.5) * w0) {
+      if (w1 < (rtol * rtol < 0.5 ? rtol * rtol : 0.5) * w0) {
         for (int l = 0; l <= j; l++) h2[l] = vdot(n, V + (size_t)n * l, w);
         for (int l = 0; l <= j; l++) { const double* vl = V + (size_t)n * l; for (int i = 0; i < n; i++) w[i] -= h2[l] * vl[i]; }
         for (int l = 0; l <= j; l++) h[l] += h2[l];
