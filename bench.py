@@ -51,6 +51,11 @@ GNN_BYTES_PER_CELL = 120 + 216 + 3 * 368 + 208
 # command: profiles/traffic_sine64_fp32.md
 TRAFFIC_FP32_BYTES_PER_CELL = {"residual": 235.0, "jv": 403.1,
                                "ilu_apply": 800.0, "gnn_apply": 1162.1}
+# FP64-pipe lane-instructions per cell of the FP32 form's residual (k_prim_hl<0> +
+# k_cell32 residual epilogue) and Jv (k_prim_hl<1> + k_cell32 Jv epilogue), counted by ncu
+# (sm__inst_executed_pipe_fp64 x 32 / cells; profiles/fp64_pipe_sine64.md).  GB300 retires
+# 2 FP64 lanes per clock per SM, so these put a second roof under the operations, beside HBM.
+FP64_INSTR_PER_CELL_FP32 = {"residual": 20.0, "jv": 30.0}
 
 
 def parse():
@@ -751,6 +756,17 @@ def main():
                                "frac": round(v["GBps"] / hbm, 4), "per_step": v["count"] / args.steps,
                                "ms_per_step": round(v["ms_per_step"], 3)}
                            for k, v in ops.items()}}
+        if args.mode == "fp32":
+            # the FP64 pipe's share of the operation's time: its FP64 lane-instructions at
+            # 2 per clock per SM, at the median SM clock sampled during the timed region
+            sms = torch.cuda.get_device_properties(dev).multi_processor_count
+            mhz = (clk or {}).get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+            for k, n in FP64_INSTR_PER_CELL_FP32.items():
+                if k in roof["per_op"]:
+                    t_fp64 = n * nC / (2.0 * sms * mhz * 1e6)
+                    roof["per_op"][k]["fp64_pipe"] = {
+                        "instr_per_cell": n, "ms_at_pipe_peak": round(t_fp64 * 1e3, 4),
+                        "frac": round(t_fp64 / (ops[k]["ms"] * 1e-3), 4)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

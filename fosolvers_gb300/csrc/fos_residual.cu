@@ -306,7 +306,7 @@ __device__ __forceinline__ void load_hl(const float* __restrict__ W, int c, PHL&
 // and dw = aP |A~| (U_R - U_L) / 2 from the Roe average (Euler.f90:90-126)
 template <typename T>
 __device__ __forceinline__ void roe_split_mj(T rm, T dr, T um, T du, T vm, T dv, T wm, T dww,
-                                             T Hm, T dH, T dp, T sL, T sR, T nx, T ny, T nz,
+                                             T Hm, T dH, T dp, T ds, T ss, T ps, T nx, T ny, T nz,
                                              T aP, T gm1, T dF[5], T dw[5]) {
   const T half = T(0.5), quarter = T(0.25);
   const T unm = um * nx + vm * ny + wm * nz;
@@ -319,9 +319,9 @@ __device__ __forceinline__ void roe_split_mj(T rm, T dr, T um, T du, T vm, T dv,
   dF[2] = h * (mm * dv + dm * vm + dp * ny);
   dF[3] = h * (mm * dww + dm * wm + dp * nz);
   dF[4] = h * (mm * dH + dm * Hm);
-  const T kap = half * (sR - sL) / (sL + sR);
+  const T kap = half * ds / ss;
   const T ua = um + kap * du, va = vm + kap * dv, wa = wm + kap * dww, Ha = Hm + kap * dH;
-  const T rhoA = sL * sR;
+  const T rhoA = ps;
   const T q2 = ua * ua + va * va + wa * wa;
   const T c2 = gm1 * (Ha - half * q2);
   const T ca = sqrt(c2);
@@ -447,25 +447,28 @@ __global__ void __launch_bounds__(kThreads) k_cell32(
       const float4 na = __ldg(faceNA + f);
       PHL Q;
       load_hl(W, isR ? lr.x : lr.y, Q);
-      const PHL& L = isR ? Q : P;
-      const PHL& R = isR ? P : Q;
+      // Orientation by signs, not by selecting L and R: the means are formed from P + Q
+      // (symmetric) and the jumps as -sw ((Q.h - P.h) + (Q.l - P.l)), which is R - L bit for
+      // bit either way (negation commutes with round-to-nearest)
       float m[6], d[6], dF[5], dw[5];
 #pragma unroll
       for (int j = 0; j < 6; j++) {
-        m[j] = 0.5f * (L.h[j] + R.h[j]) + 0.5f * (L.l[j] + R.l[j]);
-        d[j] = (R.h[j] - L.h[j]) + (R.l[j] - L.l[j]);
+        m[j] = 0.5f * (P.h[j] + Q.h[j]) + 0.5f * (P.l[j] + Q.l[j]);
+        d[j] = -sw * ((Q.h[j] - P.h[j]) + (Q.l[j] - P.l[j]));
       }
       bool f64 = false;
       if (kHyb) {
         if (kE == kEpiRhs || !fsel) {
-          f64 = fabsf(d[0]) > theta * fminf(L.h[0], R.h[0]) ||
-                fabsf(d[5]) > theta * fminf(L.h[5], R.h[5]);
+          f64 = fabsf(d[0]) > theta * fminf(P.h[0], Q.h[0]) ||
+                fabsf(d[5]) > theta * fminf(P.h[5], Q.h[5]);
           if (kE == kEpiRhs && fsel && !isR) fsel[f] = f64 ? 1 : 0;
         } else {
           f64 = __ldg(fsel + f) != 0;
         }
       }
       if (kHyb && f64) {
+        const PHL& L = isR ? Q : P;
+        const PHL& R = isR ? P : Q;
         double md[6], dd[6], rl = 0.0, rr = 0.0;
 #pragma unroll
         for (int j = 0; j < 6; j++) {
@@ -477,14 +480,16 @@ __global__ void __launch_bounds__(kThreads) k_cell32(
         }
         const double2 n01 = __ldg(faceNA64 + 2 * (size_t)f), n2a = __ldg(faceNA64 + 2 * (size_t)f + 1);
         double dF64[5], dw64[5];
+        const double sl = sqrt(rl), sr = sqrt(rr);
         roe_split_mj<double>(md[0], dd[0], md[1], dd[1], md[2], dd[2], md[3], dd[3], md[4],
-                             dd[4], dd[5], sqrt(rl), sqrt(rr), n01.x, n01.y, n2a.x, n2a.y, gm1d,
-                             dF64, dw64);
+                             dd[4], dd[5], sr - sl, sl + sr, sl * sr, n01.x, n01.y, n2a.x,
+                             n2a.y, gm1d, dF64, dw64);
 #pragma unroll
         for (int q = 0; q < 5; q++) t[q] = isR ? -dF64[q] - dw64[q] : dw64[q] - dF64[q];
       } else {
         roe_split_mj<float>(m[0], d[0], m[1], d[1], m[2], d[2], m[3], d[3], m[4], d[4], d[5],
-                            L.s, R.s, na.x, na.y, na.z, na.w, gm1, dF, dw);
+                            -sw * (Q.s - P.s), P.s + Q.s, P.s * Q.s, na.x, na.y, na.z, na.w,
+                            gm1, dF, dw);
 #pragma unroll
         for (int q = 0; q < 5; q++) t[q] = f2d_bits(fmaf(-sw, dw[q], -dF[q]));
       }
