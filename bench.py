@@ -586,6 +586,15 @@ def main():
         cvode = {"msbp": alt_msbp, "value": world * args.steps / (allmax(pg, ms_c, dev) / 1e3),
                  "ms_per_step": ms_c / args.steps, "n_pset": st_c["n_pset"],
                  "n_lin_iters": st_c["n_lin_iters"]}
+    # the headline arm with CVODE's constant-step BDF predictor as Newton's first iterate
+    # (fos_bdf_opts.predictor = 1; the default starts from y_n)
+    alt_pred = None
+    if not args.no_compare and not args.no_cvode:
+        mk_p = lambda n, **kw: mk(n, predictor=1, **kw)
+        ms_p, st_p, _, _, _ = timed_bdf(ctx, y0, mk_p, args, dev, stream, pg)
+        alt_pred = {"predictor": 1, "value": world * args.steps / (allmax(pg, ms_p, dev) / 1e3),
+                    "ms_per_step": ms_p / args.steps, "n_newton": st_p["n_newton"],
+                    "n_lin_iters": st_p["n_lin_iters"]}
 
     # end to end: host buffer in the caller's cell order, copied in and out every step
     e2e = None
@@ -812,7 +821,7 @@ def main():
             "clocks": clk, "e2e": e2e, "gpu_launches": launches,
             "roofline": roof, "throughput": thr, "cpu_baseline": cpu,
             "vs_fp64_ilu": vs64, "same_precision_ilu": alt or None,
-            "alt_setup_policy": cvode,
+            "alt_setup_policy": cvode, "alt_predictor": alt_pred,
             "stats": {k: st[k] for k in ("n_rhs", "n_jv", "n_psol", "n_pset", "n_newton",
                                           "n_lin_iters", "n_steps", "n_fallback", "n_learned",
                                           "n_gated", "n_reorth")},

@@ -183,6 +183,17 @@ __global__ void k_hist(long n, int q, const double* __restrict__ yn, const doubl
   if (i >= n) return;
   h[i] = q == 1 ? yn[i] : (4.0 / 3.0) * yn[i] - (1.0 / 3.0) * ym[i];
 }
+// Newton's first iterate, the extrapolation of order p through y_n, y_{n-1}, y_{n-2} at a
+// constant step (CVODE's BDF predictor): p = 1: (y_n - y_{n-1}) + y_n; p = 2:
+// 3 (y_n - y_{n-1}) + y_{n-2} (rounded operation by operation, as the oracle forms it)
+template <int P>
+__global__ void k_predict(long n, const double* __restrict__ yn, const double* __restrict__ ym,
+                          const double* __restrict__ ym2, double* __restrict__ y) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double dlt = __dsub_rn(yn[i], ym[i]);
+  y[i] = P == 1 ? __dadd_rn(dlt, yn[i]) : __dadd_rn(__dmul_rn(3.0, dlt), ym2[i]);
+}
 // G = y - gamma f - hist; b = -G (also into b2: the first Arnoldi vector, unnormalised);
 // part0 <- sum G^2, part1 <- sum y^2
 __global__ void __launch_bounds__(kT) k_newton_res(long n, const double* __restrict__ y,
@@ -238,6 +249,7 @@ struct fos_bdf_work {
   long N = 0;
   int maxl = 0;
   bool has_hist = false;  // yn holds the last accepted state, ym the one before
+  int nhist = 0;          // accepted states held in yn, ym, ym2 (at most 3)
   int ilu_ref_its = -1;   // learned mode: iterations of the last ILU(0)-preconditioned solve
   double ilu_ref_rate = 1.0;  // learned mode: its mean residual reduction per iteration
   int learned_backoff = 0;  // learned mode: solves skipped after the last fallback
@@ -253,6 +265,7 @@ struct fos_bdf_work {
   long setup_serial = -1;   // the context's set-up count then (a set-up made outside the
                             // driver in between voids the kept one)
   double t_last = 0.0;
+  double* ym2 = nullptr;  // the accepted state before ym (the order-2 predictor)
   double *V = nullptr, *Z = nullptr, *w = nullptr, *yn = nullptr, *ym = nullptr,
          *hist = nullptr, *f = nullptr, *b = nullptr, *d = nullptr, *part = nullptr,
          *sc = nullptr, *yh = nullptr, *u = nullptr;
@@ -261,7 +274,8 @@ struct fos_bdf_work {
   double* ay[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   double *ypred = nullptr, *E = nullptr, *Eprev = nullptr, *atmp = nullptr;
   ~fos_bdf_work() {
-    for (double* p : {V, Z, w, yn, ym, hist, f, b, d, part, sc, yh, u, ypred, E, Eprev, atmp})
+    for (double* p : {V, Z, w, yn, ym, ym2, hist, f, b, d, part, sc, yh, u, ypred, E, Eprev,
+                      atmp})
       if (p) cudaFree(p);
     for (double* p : ay)
       if (p) cudaFree(p);
@@ -287,7 +301,8 @@ int work_get(fos_ctx* c, int maxl, Work** out) {
   c->bdf = wk;
   FOS_CUDA(cudaMalloc(&wk->V, sizeof(double) * N * (maxl + 1)));
   FOS_CUDA(cudaMalloc(&wk->Z, sizeof(double) * N * maxl));
-  for (double** p : {&wk->w, &wk->yn, &wk->ym, &wk->hist, &wk->f, &wk->b, &wk->d, &wk->yh, &wk->u})
+  for (double** p : {&wk->w, &wk->yn, &wk->ym, &wk->ym2, &wk->hist, &wk->f, &wk->b, &wk->d,
+                     &wk->yh, &wk->u})
     FOS_CUDA(cudaMalloc(p, sizeof(double) * N));
   FOS_CUDA(cudaMalloc(&wk->part, sizeof(double) * kRedBlocks * kMaxVec));
   FOS_CUDA(cudaMalloc(&wk->sc, sizeof(double) * 6 * kMaxVec));
@@ -312,6 +327,7 @@ extern "C" void fos_bdf_defaults(fos_bdf_opts* o) {
   o->jac_reuse = 0;
   o->msbp = 1;
   o->resume = 0;
+  o->predictor = 0;
 }
 
 namespace {
@@ -751,7 +767,21 @@ extern "C" int fos_bdf_run(fos_ctx* c, double t0, double* y, const fos_bdf_opts*
   dr.ilu_ref_rate = wk.ilu_ref_rate;
   double t = t0;
   FOS_CUDA(cudaMemcpyAsync(wk.yn, y, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
-  if (!resume) wk.has_hist = false;
+  if (!resume) {
+    wk.has_hist = false;
+    wk.nhist = 1;
+  }
+  // Newton's first iterate in y: y_n (which y holds at the start of every step: yn was
+  // copied from y before the first step and from the accepted y after every step), or the
+  // extrapolation of order p through the history
+  auto pred_order = [&](int q) { return opts->predictor ? std::min(q, wk.nhist - 1) : 0; };
+  auto predict = [&](int p) -> int {
+    if (p == 1) fos_launch(c, k_predict<1>, nb(N), kT, N, wk.yn, wk.ym, wk.ym2, y);
+    else if (p == 2) fos_launch(c, k_predict<2>, nb(N), kT, N, wk.yn, wk.ym, wk.ym2, y);
+    else FOS_CUDA(cudaMemcpyAsync(y, wk.yn, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+    FOS_LAUNCH_CHECK();
+    return 0;
+  };
   int status = 0;
   // preconditioner set-up policy (opts->msbp > 1: CVODE's cvLsSetup conditions); a resumed
   // call continues the previous call's count, as CVODE keeps its set-up across CVode calls
@@ -769,16 +799,23 @@ extern "C" int fos_bdf_run(fos_ctx* c, double t0, double* y, const fos_bdf_opts*
     const double gamma = q == 1 ? opts->dt : 2.0 * opts->dt / 3.0;
     const double tn = t + opts->dt;
     fos_launch(c, k_hist, nb(N), kT, N, q, wk.yn, wk.ym, wk.hist);
-    // the Newton iteration starts from y_n, which y holds: yn was copied from y before the
-    // first step and from the accepted y after every step
+    const int p = pred_order(q);
+    if (p > 0)
+      if (int rc = predict(p)) return rc;
     const bool reuse = opts->msbp > 1 && have_setup && c->has_factor &&
                        s - last_setup < opts->msbp &&
                        std::fabs(gamma / gamma_setup - 1.0) <= 0.3;
     dr.keep_setup = reuse;
     dr.setup_made = false;
-    int nrc = dr.newton(y, gamma, wk.hist, tn);  // from y_0 = y_n
+    int nrc = dr.newton(y, gamma, wk.hist, tn);  // from the predicted y_0
     if (nrc == 1 && reuse) {  // failed on a reused set-up: retry the step with a fresh one
-      FOS_CUDA(cudaMemcpyAsync(y, wk.yn, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
+      if (int rc = predict(p)) return rc;
+      dr.keep_setup = false;
+      nrc = dr.newton(y, gamma, wk.hist, tn);
+    }
+    if ((nrc == 1 || nrc == 2) && p > 0) {  // the extrapolation failed (at a shock it can
+                                            // leave the physical states): retry from y_n
+      if (int rc = predict(0)) return rc;
       dr.keep_setup = false;
       nrc = dr.newton(y, gamma, wk.hist, tn);
     }
@@ -796,14 +833,19 @@ extern "C" int fos_bdf_run(fos_ctx* c, double t0, double* y, const fos_bdf_opts*
       FOS_CUDA(cudaMemcpyAsync(y, wk.yn, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
       break;
     }
+    std::swap(wk.ym2, wk.ym);  // y_{n-2} <- y_{n-1} <- y_n <- y
     std::swap(wk.ym, wk.yn);
     FOS_CUDA(cudaMemcpyAsync(wk.yn, y, sizeof(double) * N, cudaMemcpyDeviceToDevice, c->stream));
     t = tn;
     st.n_steps++;
     steps_done = s + 1;
     wk.has_hist = true;
+    wk.nhist = std::min(wk.nhist + 1, 3);
   }
-  if (status) wk.has_hist = false;
+  if (status) {
+    wk.has_hist = false;
+    wk.nhist = 1;
+  }
   wk.setup_age = (have_setup && !status) ? steps_done - last_setup : -1;
   wk.gamma_setup = gamma_setup;
   wk.setup_serial = c->n_setup;
@@ -1090,6 +1132,7 @@ extern "C" int fos_bdf_adaptive(fos_ctx* c, double t0, double tout, double* y,
   wk.ilu_ref_its = dr.ilu_ref_its;
   wk.ilu_ref_rate = dr.ilu_ref_rate;
   wk.has_hist = false;  // the fixed-step history does not continue an adaptive run
+  wk.nhist = 1;
   as.t = t;
   st.t = t;
   FOS_CUDA(cudaStreamSynchronize(c->stream));

@@ -271,6 +271,13 @@ typedef struct {
                          or gamma changed by more than 30% since it, and when a step's Newton
                          iteration fails on a reused set-up (the step is retried with a fresh
                          one); otherwise psol uses the last factorisation */
+  int predictor;      /* Newton's first iterate: 0 = y_n (default); 1 = CVODE's BDF predictor
+                         at a constant step, the extrapolation through the last q + 1
+                         accepted states (2 y_n - y_{n-1} at order 1, 3 y_n - 3 y_{n-1} +
+                         y_{n-2} at order 2, lower while the history is shorter), with a
+                         retry from y_n when Newton fails from it.  It pays on smooth flows
+                         (fewer Newton iterations) and costs at shocks and transients, where
+                         the fixed step cannot shrink as CVODE's would */
 } fos_bdf_opts;
 
 typedef struct {

@@ -1385,7 +1385,7 @@ void o_bdf_defaults(o_bdf_opts* o) {
   o->order = 1; o->dt = 1e-3; o->nsteps = 1;
   o->newton_rtol = 1e-8; o->newton_atol = 1e-12; o->max_newton = 10;
   o->maxl = 30; o->max_restarts = 4; o->lin_rtol = 1e-3;
-  o->jv_eps = 1.4901161193847656e-08; o->use_prec = 1; o->msbp = 1;
+  o->jv_eps = 1.4901161193847656e-08; o->use_prec = 1; o->msbp = 1; o->predictor = 0;
 }
 
 
@@ -1430,12 +1430,24 @@ static int o_newton(int n, o_rhs_fn rhs, o_pset_fn pset, o_psol_fn psol, void* u
   return 1;
 }
 
+/* Newton's first iterate at a constant step: the extrapolation of order p through
+ * y_n, y_{n-1}, y_{n-2} (p = 0: y_n; 1: 2 y_n - y_{n-1} = (y_n - y_{n-1}) + y_n;
+ * 2: 3 y_n - 3 y_{n-1} + y_{n-2} = 3 (y_n - y_{n-1}) + y_{n-2}) */
+static void o_bdf_predict(int n, int p, const double* yn, const double* ynm1, const double* ynm2,
+                          double* y) {
+  if (p == 0) memcpy(y, yn, sizeof(double) * n);
+  else if (p == 1) for (int i = 0; i < n; i++) y[i] = (yn[i] - ynm1[i]) + yn[i];
+  else for (int i = 0; i < n; i++) y[i] = 3.0 * (yn[i] - ynm1[i]) + ynm2[i];
+}
+
 int o_bdf_run(int n, o_rhs_fn rhs, o_pset_fn pset, o_psol_fn psol, void* ud, double t0,
               double* y, const o_bdf_opts* opts, o_bdf_stats* st) {
   o_bdf_stats dummy;
   if (!st) st = &dummy;
   memset(st, 0, sizeof(*st));
   double *yn = (double*)xcalloc(n, sizeof(double)), *ynm1 = (double*)xcalloc(n, sizeof(double));
+  double* ynm2 = (double*)xcalloc(n, sizeof(double));
+  int nh = 1; /* accepted states held: yn, ynm1, ynm2 */
   double *hist = (double*)xcalloc(n, sizeof(double)), *f = (double*)xcalloc(n, sizeof(double));
   double *G = (double*)xcalloc(n, sizeof(double)), *d = (double*)xcalloc(n, sizeof(double));
   double *ytmp = (double*)xcalloc(n, sizeof(double)), *ftmp = (double*)xcalloc(n, sizeof(double));
@@ -1455,13 +1467,20 @@ int o_bdf_run(int n, o_rhs_fn rhs, o_pset_fn pset, o_psol_fn psol, void* ud, dou
       for (int i = 0; i < n; i++) hist[i] = (4.0 / 3.0) * yn[i] - (1.0 / 3.0) * ynm1[i];
     }
     double tn = t + opts->dt;
-    memcpy(y, yn, sizeof(double) * n); /* predictor: previous state */
+    const int p = opts->predictor ? (q < nh - 1 ? q : nh - 1) : 0;
+    o_bdf_predict(n, p, yn, ynm1, ynm2, y);
     const int reuse = opts->msbp > 1 && last_setup >= 0 && s - last_setup < opts->msbp &&
                       fabs(gamma / gamma_setup - 1.0) <= 0.3;
     int made = 0;
     int nrc = o_newton(n, rhs, pset, psol, ud, tn, y, gamma, hist, opts, st, f, G, d, ytmp, ftmp,
                        reuse, &made);
     if (nrc == 1 && reuse) { /* failed on a reused set-up: retry the step with a fresh one */
+      o_bdf_predict(n, p, yn, ynm1, ynm2, y);
+      nrc = o_newton(n, rhs, pset, psol, ud, tn, y, gamma, hist, opts, st, f, G, d, ytmp, ftmp,
+                     0, &made);
+    }
+    if ((nrc == 1 || nrc == 2) && p > 0) { /* the extrapolation failed (at a shock it can leave
+                                              the physical states): retry from y_n */
       memcpy(y, yn, sizeof(double) * n);
       nrc = o_newton(n, rhs, pset, psol, ud, tn, y, gamma, hist, opts, st, f, G, d, ytmp, ftmp,
                      0, &made);
@@ -1476,12 +1495,14 @@ int o_bdf_run(int n, o_rhs_fn rhs, o_pset_fn pset, o_psol_fn psol, void* ud, dou
       memcpy(y, yn, sizeof(double) * n);
       break;
     }
+    memcpy(ynm2, ynm1, sizeof(double) * n);
     memcpy(ynm1, yn, sizeof(double) * n);
     memcpy(yn, y, sizeof(double) * n);
+    if (nh < 3) nh++;
     t = tn;
     st->n_steps++;
   }
-  free(yn); free(ynm1); free(hist); free(f); free(G); free(d); free(ytmp); free(ftmp);
+  free(yn); free(ynm1); free(ynm2); free(hist); free(f); free(G); free(d); free(ytmp); free(ftmp);
   return status;
 }
 

@@ -131,6 +131,11 @@ typedef struct {
   int msbp;           /* 1 = pset every step; m > 1 = CVODE's set-up policy (cvLsSetup:
                          at most m steps between set-ups, or a > 30% gamma change, or a
                          Newton failure on a reused set-up, after which the step is retried) */
+  int predictor;      /* Newton's first iterate: 0 = y_n (default); 1 = extrapolation through
+                         the last q + 1 accepted states (CVODE's BDF predictor at a constant
+                         step: 2 y_n - y_{n-1} at order 1, 3 y_n - 3 y_{n-1} + y_{n-2} at
+                         order 2; lower order while the history is shorter), retried from
+                         y_n when Newton fails from it */
 } o_bdf_opts;
 typedef struct {
   long n_rhs, n_jv, n_psol, n_pset, n_newton, n_lin_iters, n_steps, fails;

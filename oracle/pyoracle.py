@@ -26,7 +26,7 @@ class BdfOpts(C.Structure):
                 ("newton_rtol", C.c_double), ("newton_atol", C.c_double),
                 ("max_newton", C.c_int), ("maxl", C.c_int), ("max_restarts", C.c_int),
                 ("lin_rtol", C.c_double), ("jv_eps", C.c_double), ("use_prec", C.c_int),
-                ("msbp", C.c_int)]
+                ("msbp", C.c_int), ("predictor", C.c_int)]
 
 
 class AdaptOpts(C.Structure):
