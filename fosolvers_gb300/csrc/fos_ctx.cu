@@ -34,7 +34,7 @@ fos_ctx::~fos_ctx() {
                   d_flag, d_prow, d_pcol, d_pdiag, d_cdiag, d_ipos, d_ord, d_fslot, d_Jraw,
                   d_LU, d_LU32, d_lrows_f, d_lrows_b, d_upd_ptr, d_upd, d_ilu_tmp, d_Jb, d_ierr,
                   d_closure32, d_pia, d_pja, d_pa, d_vol, d_ilut_x, d_plst, d_pdu, d_fsel,
-                  d_yJ};
+                  d_yJ, d_cnb, d_cna32};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h_scal) cudaFreeHost(h_scal);
@@ -326,6 +326,24 @@ extern "C" int fos_ctx_create(fos_ctx** out, int nC, int nE, int nPi, int nPb, c
   FOS_TRY(upload(&c->d_crow, crow.data(), nC + 1));
   FOS_TRY(upload(&c->d_cent, cent.data(), cent.size()));
   FOS_TRY(upload(&c->d_ell, ell.data(), ell.size()));
+  if (flags & FOS_FLUX_FP32) {  // per-cell face slots of the FP32 flux (copies of face data)
+    const int w = c->ell_w;
+    std::vector<int> cnb((size_t)w * nC);
+    std::vector<float4> cna((size_t)w * nC, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    for (int i = 0; i < nC; i++)
+      for (int k = 0; k < w; k++) {
+        const int e = ell[(size_t)w * i + k];
+        int nb = i;
+        if (e >= 0) {
+          const int f = e >> 1;
+          if (f < nPi) nb = (e & 1) ? faceLR[f].x : faceLR[f].y;
+          cna[(size_t)k * nC + i] = faceNA32[f];
+        }
+        cnb[(size_t)w * i + k] = nb;
+      }
+    FOS_TRY(upload(&c->d_cnb, cnb.data(), cnb.size()));
+    FOS_TRY(upload(&c->d_cna32, cna.data(), cna.size()));
+  }
   FOS_TRY(dalloc(&c->d_Whl, 16 * (size_t)nC));
   if (flags & FOS_FLUX_HYBRID) {
     FOS_TRY(dalloc(&c->d_fsel, (size_t)nP));

@@ -416,8 +416,8 @@ __global__ void __launch_bounds__(kThreads) k_bface32(
 // Jv reuses it, so f(y + s v) and f(y) evaluate every face the same way.
 template <int kW, bool kHyb, int kE, bool kSc>
 __global__ void __launch_bounds__(kThreads) k_cell32(
-    int nC, int nFi, const int* __restrict__ ell, const int2* __restrict__ faceLR,
-    const float4* __restrict__ faceNA, const float* __restrict__ W, float gm1,
+    int nC, int nFi, const int* __restrict__ ell, const int* __restrict__ cnb,
+    const float4* __restrict__ cna, const float* __restrict__ W, float gm1,
     const double* __restrict__ Fb, const float4* __restrict__ Sc,
     const double* __restrict__ invV,
     const double* __restrict__ vv, const double* __restrict__ fy, const double* __restrict__ d_s,
@@ -426,8 +426,9 @@ __global__ void __launch_bounds__(kThreads) k_cell32(
     double gm1d) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nC) return;
-  int e[kW];
+  int e[kW], nbr[kW];
   load_ell<kW>(ell, c, e);
+  load_ell<kW>(cnb, c, nbr);  // the cells across the faces: no wait on the face arrays
   PHL P;
   load_hl(W, c, P);
   // FP64 accumulation in ELL order; the first face initialises the sums (every cell has
@@ -443,10 +444,9 @@ __global__ void __launch_bounds__(kThreads) k_cell32(
     double t[5];  // the face's term: -(dF - dw) (cell is L) or -(dF + dw) (cell is R)
     if (f < nFi) {
       const float sw = isR ? 1.0f : -1.0f;
-      const int2 lr = __ldg(faceLR + f);
-      const float4 na = __ldg(faceNA + f);
+      const float4 na = __ldg(cna + (size_t)k * nC + c);
       PHL Q;
-      load_hl(W, isR ? lr.x : lr.y, Q);
+      load_hl(W, nbr[k], Q);
       // Orientation by signs, not by selecting L and R: the means are formed from P + Q
       // (symmetric) and the jumps as -sw ((Q.h - P.h) + (Q.l - P.l)), which is R - L bit for
       // bit either way (negation commutes with round-to-nearest)
@@ -621,7 +621,7 @@ int fos_residual_launch(fos_ctx* c, const double* y, const double* v, const doub
                  (const int*)c->d_bcT, (const double*)c->d_bcP, c->maxP, c->gamm, c->r, c->d_F,
                  hyb ? 1 : 0);
     fos_launch(c, cell32_kernel(c->ell_w, hyb, ek, c->d_closure32 != nullptr), nblk(c->nC), kThreads, c->nC, c->nFi,
-               (const int*)c->d_ell, (const int2*)c->d_faceLR, (const float4*)c->d_faceNA32,
+               (const int*)c->d_ell, (const int*)c->d_cnb, (const float4*)c->d_cna32,
                (const float*)c->d_Whl, (float)gm1, (const double*)c->d_F,
                (const float4*)c->d_closure32, (const double*)c->d_invV, v, fy, d_s, a,
                out, c->d_flag, (const double2*)c->d_faceNA, c->d_fsel, (float)c->hyb_theta, gm1);
@@ -772,7 +772,7 @@ extern "C" int fos_euler_rhs_dev_static(const fos_ctx* c, double t, const double
                                                   c->gamm, c->r, F, hyb ? 1 : 0);
     // the face choice of the hybrid flux is made from this state (no record kept)
     cell32_kernel(c->ell_w, hyb, kEpiRhs, c->d_closure32 != nullptr)<<<nblk(c->nC), kThreads, 0, s>>>(
-        c->nC, c->nFi, c->d_ell, c->d_faceLR, c->d_faceNA32, Whl, (float)gm1, F, c->d_closure32,
+        c->nC, c->nFi, c->d_ell, c->d_cnb, c->d_cna32, Whl, (float)gm1, F, c->d_closure32,
         c->d_invV, nullptr, nullptr, nullptr, 0.0, ydot, nullptr, c->d_faceNA, nullptr,
         (float)c->hyb_theta, gm1);
   } else {
