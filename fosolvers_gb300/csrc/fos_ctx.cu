@@ -326,7 +326,8 @@ extern "C" int fos_ctx_create(fos_ctx** out, int nC, int nE, int nPi, int nPb, c
   FOS_TRY(upload(&c->d_crow, crow.data(), nC + 1));
   FOS_TRY(upload(&c->d_cent, cent.data(), cent.size()));
   FOS_TRY(upload(&c->d_ell, ell.data(), ell.size()));
-  if (flags & FOS_FLUX_FP32) {  // per-cell face slots of the FP32 flux (copies of face data)
+  if (flags & (FOS_FLUX_FP32 | FOS_ILU_FP32)) {  // per-cell face slots of the FP32 flux and
+                                                // Jacobian (copies of face data)
     const int w = c->ell_w;
     std::vector<int> cnb((size_t)w * nC);
     std::vector<float4> cna((size_t)w * nC, make_float4(0.0f, 0.0f, 0.0f, 0.0f));

@@ -61,7 +61,8 @@ struct fos_ctx {
   int* d_crow = nullptr;      // [nC+1] cell -> face entries
   int* d_cent = nullptr;      // (face << 1) | (cell is R)
   int* d_ell = nullptr;       // [ell_w*nC] the same entries, fixed width, -1 = empty
-  // the FP32 flux's per-cell face slots, so a cell's gathers wait on one index load, not
+  // the FP32 flux's and Jacobian's per-cell face slots, so a cell's gathers wait on one
+  // index load, not
   // two: [ell_w*nC] the cell across each face (the cell itself for boundary faces and empty
   // slots), and [ell_w][nC] slot-major copies of the faces' FP32 (nx, ny, nz, aP)
   int* d_cnb = nullptr;

@@ -244,10 +244,10 @@ __device__ __forceinline__ PrimT<float> load_prim_f32(const float* __restrict__ 
 // st + 25 (slot - s0)); sdiag = the diagonal block's slot - s0.  The multiply-adds are
 // written out (fmaf), so both kernels produce the same bits.
 template <int kW>
-__device__ __forceinline__ void jac_row32(int c, int nFi, int s0, int sdiag,
+__device__ __forceinline__ void jac_row32(int c, int nC, int nFi, int s0, int sdiag,
                                           const int* __restrict__ ell,
-                                          const int2* __restrict__ faceLR,
-                                          const float4* __restrict__ faceNA32,
+                                          const int* __restrict__ cnb,
+                                          const float4* __restrict__ cna,
                                           const int* __restrict__ fslot,
                                           const float* __restrict__ Whl,
                                           const double* __restrict__ Gb,
@@ -263,12 +263,11 @@ __device__ __forceinline__ void jac_row32(int c, int nFi, int s0, int sdiag,
     if (ek < 0) continue;
     const int f = ek >> 1;
     const bool isR = ek & 1;
-    const int2 lr = __ldg(faceLR + f);
-    const float4 na = __ldg(faceNA32 + f);
+    const float4 na = __ldg(cna + (size_t)k * nC + c);  // the face's FP32 geometry, per cell
     const float n[3] = {na.x, na.y, na.z};
     PrimT<float> Q;
     if (f < nFi) {
-      Q = load_prim_f32(Whl, isR ? lr.x : lr.y);
+      Q = load_prim_f32(Whl, __ldg(cnb + (size_t)kW * c + k));  // the cell across the face
     } else {  // ghost primitives of k_jac_ghost64
       const double2* G2 = reinterpret_cast<const double2*>(Gb + 6 * (size_t)f);
       const double2 a0 = __ldg(G2), a1 = __ldg(G2 + 1), a2 = __ldg(G2 + 2);
@@ -324,8 +323,8 @@ __device__ __forceinline__ void jac_row32(int c, int nFi, int s0, int sdiag,
 template <int kW>
 __global__ void __launch_bounds__(64) k_jac_cell32(
     int nC, int nFi, const int* __restrict__ ipos, const int* __restrict__ prow,
-    const int* __restrict__ cdiag, const int* __restrict__ ell, const int2* __restrict__ faceLR,
-    const float4* __restrict__ faceNA32, const int* __restrict__ fslot,
+    const int* __restrict__ cdiag, const int* __restrict__ ell, const int* __restrict__ cnb,
+    const float4* __restrict__ cna, const int* __restrict__ fslot,
     const float* __restrict__ Whl, const double* __restrict__ Gb, const float4* __restrict__ Sc,
     double g, float* __restrict__ J) {
   constexpr int kRow = (kW + 1) * 25;  // floats of a full block row
@@ -338,7 +337,7 @@ __global__ void __launch_bounds__(64) k_jac_cell32(
     const int p = ipos[c];
     s0 = prow[p];
     nbk = prow[p + 1] - s0;
-    jac_row32<kW>(c, nFi, s0, cdiag[c] - s0, ell, faceLR, faceNA32, fslot, Whl, Gb, Sc,
+    jac_row32<kW>(c, nC, nFi, s0, cdiag[c] - s0, ell, cnb, cna, fslot, Whl, Gb, Sc,
                   d2f_trunc(g), st);
   }
   __syncwarp();
@@ -585,8 +584,8 @@ template <int kW>
 __global__ void __launch_bounds__(64) k_pset32(
     int n, const int* __restrict__ rows, int p0, const int* __restrict__ prow,
     const int* __restrict__ pdiag, const int* __restrict__ ord, const double* __restrict__ invV,
-    double gamma, int nFi, const int* __restrict__ ell, const int2* __restrict__ faceLR,
-    const float4* __restrict__ faceNA32, const int* __restrict__ fslot,
+    double gamma, int nC, int nFi, const int* __restrict__ ell, const int* __restrict__ cnb,
+    const float4* __restrict__ cna, const int* __restrict__ fslot,
     const float* __restrict__ Whl, const double* __restrict__ Gb, const float4* __restrict__ Sc,
     double g, const int* __restrict__ upd_ptr, const int3* __restrict__ upd,
     const int* __restrict__ plst, const int* __restrict__ pdu, float* __restrict__ LU,
@@ -604,7 +603,7 @@ __global__ void __launch_bounds__(64) k_pset32(
     nb = prow[p + 1] - s0;
     sd = pdiag[p] - s0;
     const int c = ord[p];
-    jac_row32<kW>(c, nFi, s0, sd, ell, faceLR, faceNA32, fslot, Whl, Gb, Sc, d2f_trunc(g), st);
+    jac_row32<kW>(c, nC, nFi, s0, sd, ell, cnb, cna, fslot, Whl, Gb, Sc, d2f_trunc(g), st);
     const float sc = d2f_trunc(gamma * invV[c]);
     for (int b = 0; b < nb; b++) {
       float* blk = st + 25 * b;
@@ -1046,13 +1045,13 @@ static int jac_assemble_t(fos_ctx* c, const double* y) {
     if (c->ell_w == 4)
       fos_launch(c, k_jac_cell32<4>, grid, 64, c->nC, c->nFi, (const int*)c->d_ipos,
                  (const int*)c->d_prow, (const int*)c->d_cdiag, (const int*)c->d_ell,
-                 (const int2*)c->d_faceLR, (const float4*)c->d_faceNA32, (const int*)c->d_fslot,
+                 (const int*)c->d_cnb, (const float4*)c->d_cna32, (const int*)c->d_fslot,
                  (const float*)c->d_Whl, (const double*)c->d_F, (const float4*)c->d_closure32,
                  c->gamm, J);
     else
       fos_launch(c, k_jac_cell32<6>, grid, 64, c->nC, c->nFi, (const int*)c->d_ipos,
                  (const int*)c->d_prow, (const int*)c->d_cdiag, (const int*)c->d_ell,
-                 (const int2*)c->d_faceLR, (const float4*)c->d_faceNA32, (const int*)c->d_fslot,
+                 (const int*)c->d_cnb, (const float4*)c->d_cna32, (const int*)c->d_fslot,
                  (const float*)c->d_Whl, (const double*)c->d_F, (const float4*)c->d_closure32,
                  c->gamm, J);
     FOS_LAUNCH_CHECK();
@@ -1097,8 +1096,8 @@ int fos_pset_fused(fos_ctx* c, const double* y, double gamma) {
     auto k = c->ell_w == 4 ? k_pset32<4> : k_pset32<6>;
     fos_launch(c, k, (n + 63) / 64, 64, n, rows, c->lev_f[l], (const int*)c->d_prow,
                (const int*)c->d_pdiag, (const int*)c->d_ord, (const double*)c->d_invV, gamma,
-               c->nFi, (const int*)c->d_ell, (const int2*)c->d_faceLR,
-               (const float4*)c->d_faceNA32, (const int*)c->d_fslot, (const float*)c->d_Whl,
+               c->nC, c->nFi, (const int*)c->d_ell, (const int*)c->d_cnb,
+               (const float4*)c->d_cna32, (const int*)c->d_fslot, (const float*)c->d_Whl,
                (const double*)c->d_F, (const float4*)c->d_closure32, c->gamm,
                (const int*)c->d_upd_ptr, (const int3*)c->d_upd, (const int*)c->d_plst,
                (const int*)c->d_pdu, c->d_LU32, c->d_ierr);
