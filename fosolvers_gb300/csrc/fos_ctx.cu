@@ -34,7 +34,7 @@ fos_ctx::~fos_ctx() {
                   d_flag, d_prow, d_pcol, d_pdiag, d_cdiag, d_ipos, d_ord, d_fslot, d_Jraw,
                   d_LU, d_LU32, d_lrows_f, d_lrows_b, d_upd_ptr, d_upd, d_ilu_tmp, d_Jb, d_ierr,
                   d_closure32, d_pia, d_pja, d_pa, d_vol, d_ilut_x, d_plst, d_pdu, d_fsel,
-                  d_yJ, d_cnb, d_cna32};
+                  d_yJ, d_cnb, d_cna32, d_pnbL, d_pnbU};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h_scal) cudaFreeHost(h_scal);

@@ -114,6 +114,11 @@ struct fos_ctx {
   // plst[p] + (s - prow[p]) below the diagonal, pdu[p] + (s - pdiag[p]) from it on.
   double* d_LU = nullptr;     // [25*nnzb] factors (FP64)
   float* d_LU32 = nullptr;    // [25*nnzb] factors (FP32)
+  // the sweeps' neighbour lists at a fixed width (4, or 8 beyond four neighbours), by
+  // position: L neighbours and U neighbours in block order, -1 padded
+  int* d_pnbL = nullptr;
+  int* d_pnbU = nullptr;
+  int ilu_nbw = 4;
   int* d_plst = nullptr;      // [nC] storage block of the first L block of every position
   int* d_pdu = nullptr;       // [nC] storage block of the diagonal block of every position
   int ilu_nlev_f = 0, ilu_nlev_b = 0;

@@ -760,13 +760,24 @@ __device__ __forceinline__ void ilu_diag_store(int lane, int a, bool active, int
   if (a < 3) zv[8 * (size_t)p + 5 + a] = TF(0);
 }
 
+// a row's neighbour positions, kNW of them (-1 padded), in one or two 16-byte loads
+template <int kNW>
+__device__ __forceinline__ void load_nbrs(const int* __restrict__ nb, int p, int q[kNW]) {
+  const int4* n4 = reinterpret_cast<const int4*>(nb + (size_t)kNW * p);
+#pragma unroll
+  for (int i = 0; i < kNW / 4; i++) {
+    const int4 v = __ldg(n4 + i);
+    q[4 * i] = v.x; q[4 * i + 1] = v.y; q[4 * i + 2] = v.z; q[4 * i + 3] = v.w;
+  }
+}
+
 // kDiag: the level has no U blocks and is also the backward sweep's first level, so the
-// launch finishes those rows (z_p = inv(D_p) y_p) instead of storing y_p
-template <typename TF, bool kDiag>
+// launch finishes those rows (z_p = inv(D_p) y_p) instead of storing y_p.  The row's
+// neighbours come from the fixed-width list nbL (kNW wide), so the gathers of the earlier
+// rows' values wait on one index load, not on a load per column position.
+template <typename TF, bool kDiag, int kNW>
 __global__ void __launch_bounds__(kT) k_ilu_fwd(int n, const int* __restrict__ rows, int p0,
-                                                const int* __restrict__ prow,
-                                                const int* __restrict__ pcol,
-                                                const int* __restrict__ pdiag,
+                                                const int* __restrict__ nbL,
                                                 const int* __restrict__ plst,
                                                 const int* __restrict__ pdu,
                                                 const TF* __restrict__ LU, TF* __restrict__ yv,
@@ -779,14 +790,18 @@ __global__ void __launch_bounds__(kT) k_ilu_fwd(int n, const int* __restrict__ r
   const int p = active ? (rows ? rows[t] : p0 + t) : 0;
   TF acc = TF(0);
   if (active) {
+    int q[kNW];
+    load_nbrs<kNW>(nbL, p, q);
     acc = yv[8 * (size_t)p + a];
-    const int s0 = prow[p], s1 = pdiag[p];
     const TF* Lp = LU + 25 * (size_t)plst[p] + a;  // the row's L blocks, in order
-    for (int s = s0; s < s1; s++) {
-      const TF* yq = yv + 8 * (size_t)pcol[s];
-      const TF* B = Lp + 25 * (s - s0);
 #pragma unroll
-      for (int b = 0; b < 5; b++) acc -= __ldg(B + 5 * b) * yq[b];
+    for (int k = 0; k < kNW; k++) {
+      if (q[k] >= 0) {
+        const TF* yq = yv + 8 * (size_t)q[k];
+        const TF* B = Lp + 25 * k;
+#pragma unroll
+        for (int b = 0; b < 5; b++) acc -= __ldg(B + 5 * b) * yq[b];
+      }
     }
   }
   if constexpr (kDiag)
@@ -795,11 +810,9 @@ __global__ void __launch_bounds__(kT) k_ilu_fwd(int n, const int* __restrict__ r
     yv[8 * (size_t)p + a] = acc;
 }
 
-template <typename TF>
+template <typename TF, int kNW>
 __global__ void __launch_bounds__(kT) k_ilu_bwd(int n, const int* __restrict__ rows, int p0,
-                                                const int* __restrict__ prow,
-                                                const int* __restrict__ pcol,
-                                                const int* __restrict__ pdiag,
+                                                const int* __restrict__ nbU,
                                                 const int* __restrict__ pdu,
                                                 const TF* __restrict__ LU,
                                                 const TF* __restrict__ yv, TF* __restrict__ zv) {
@@ -811,14 +824,18 @@ __global__ void __launch_bounds__(kT) k_ilu_bwd(int n, const int* __restrict__ r
   TF acc = TF(0);
   const TF* Dp = LU + a;  // inv(D_p), followed by the row's U blocks in order
   if (active) {
+    int q[kNW];
+    load_nbrs<kNW>(nbU, p, q);
     acc = yv[8 * (size_t)p + a];
-    const int sd = pdiag[p], s1 = prow[p + 1];
     Dp += 25 * (size_t)pdu[p];
-    for (int s = sd + 1; s < s1; s++) {
-      const TF* zq = zv + 8 * (size_t)pcol[s];
-      const TF* B = Dp + 25 * (s - sd);
 #pragma unroll
-      for (int b = 0; b < 5; b++) acc -= __ldg(B + 5 * b) * zq[b];
+    for (int k = 0; k < kNW; k++) {
+      if (q[k] >= 0) {
+        const TF* zq = zv + 8 * (size_t)q[k];
+        const TF* B = Dp + 25 * (k + 1);
+#pragma unroll
+        for (int b = 0; b < 5; b++) acc -= __ldg(B + 5 * b) * zq[b];
+      }
     }
   }
   ilu_diag_store(lane, a, active, p, acc, Dp, zv);
@@ -993,6 +1010,26 @@ int fos_jac_setup(fos_ctx* c) {
     }
     upd_ptr[p + 1] = (int)upd.size();
   }
+  // the sweeps' fixed-width neighbour lists (one or two int4 loads per row instead of a
+  // dependent load of every column position)
+  {
+    int mx = 0;
+    for (int p = 0; p < nC; p++)
+      mx = std::max(mx, std::max(pdiag[p] - prow[p], prow[p + 1] - pdiag[p] - 1));
+    c->ilu_nbw = mx <= 4 ? 4 : 8;
+    if (mx > 8) {
+      fos_set_error("block ILU(0): a row has more than 8 neighbours");
+      return -2;
+    }
+    const int w = c->ilu_nbw;
+    std::vector<int> nbL((size_t)w * nC, -1), nbU((size_t)w * nC, -1);
+    for (int p = 0; p < nC; p++) {
+      for (int s = prow[p]; s < pdiag[p]; s++) nbL[(size_t)w * p + (s - prow[p])] = pcol[s];
+      for (int s = pdiag[p] + 1; s < prow[p + 1]; s++)
+        nbU[(size_t)w * p + (s - pdiag[p] - 1)] = pcol[s];
+    }
+    if (up(&c->d_pnbL, nbL) || up(&c->d_pnbU, nbU)) return -100;
+  }
   c->h_prow = prow;
   c->h_pcol = pcol;
   if (up(&c->d_prow, prow) || up(&c->d_pcol, pcol) || up(&c->d_pdiag, pdiag) ||
@@ -1152,22 +1189,20 @@ static int ilu_apply_t(fos_ctx* c, const TF* LU, const double* r, double* z,
   for (int l = 0; l < nf; l++) {
     const int n = c->lev_f[l + 1] - c->lev_f[l];
     const int* rows = c->d_lrows_f ? c->d_lrows_f + c->lev_f[l] : nullptr;
-    if (c->ilu_fuse_top && l == nf - 1)
-      fos_launch(c, k_ilu_fwd<TF, true>, nb_rows5(n), kT, n, rows, c->lev_f[l],
-                 (const int*)c->d_prow, (const int*)c->d_pcol, (const int*)c->d_pdiag,
-                 (const int*)c->d_plst, (const int*)c->d_pdu, LU, yv, zv);
-    else if (c->lev_f_hasL[l])  // a level without L blocks keeps y = r
-      fos_launch(c, k_ilu_fwd<TF, false>, nb_rows5(n), kT, n, rows, c->lev_f[l],
-                 (const int*)c->d_prow, (const int*)c->d_pcol, (const int*)c->d_pdiag,
-                 (const int*)c->d_plst, (const int*)c->d_pdu, LU, yv, zv);
+    const bool top = c->ilu_fuse_top && l == nf - 1;
+    if (!top && !c->lev_f_hasL[l]) continue;  // a level without L blocks keeps y = r
+    auto k = top ? (c->ilu_nbw == 4 ? k_ilu_fwd<TF, true, 4> : k_ilu_fwd<TF, true, 8>)
+                 : (c->ilu_nbw == 4 ? k_ilu_fwd<TF, false, 4> : k_ilu_fwd<TF, false, 8>);
+    fos_launch(c, k, nb_rows5(n), kT, n, rows, c->lev_f[l], (const int*)c->d_pnbL,
+               (const int*)c->d_plst, (const int*)c->d_pdu, LU, yv, zv);
   }
   for (int l = c->ilu_fuse_top ? 1 : 0; l < c->ilu_nlev_b; l++) {
     // colours run backwards for the upper sweep
     const int lc = c->ilu_colors ? c->ilu_nlev_b - 1 - l : l;
     const int n = c->lev_b[lc + 1] - c->lev_b[lc];
     const int* rows = c->d_lrows_b ? c->d_lrows_b + c->lev_b[lc] : nullptr;
-    fos_launch(c, k_ilu_bwd<TF>, nb_rows5(n), kT, n, rows, c->lev_b[lc], (const int*)c->d_prow,
-               (const int*)c->d_pcol, (const int*)c->d_pdiag, (const int*)c->d_pdu, LU,
+    fos_launch(c, c->ilu_nbw == 4 ? k_ilu_bwd<TF, 4> : k_ilu_bwd<TF, 8>, nb_rows5(n), kT, n,
+               rows, c->lev_b[lc], (const int*)c->d_pnbU, (const int*)c->d_pdu, LU,
                (const TF*)yv, zv);
   }
   if (d_zsq) {
