@@ -79,3 +79,38 @@ def test_grid_build_rejects_bad_node_ids(fos_lib):
     rc = fos_lib.fos_grid_build(C.byref(h), 4, _lib.dptr(pN), 1, 4, _lib.iptr(np.array([20], np.int32)),
                                 _lib.iptr(np.array([4], np.int32)), _lib.iptr(iNE), None)
     assert rc < 0 and "range" in _lib.last_error()
+
+
+STRUCTS = {"fos_bdf_opts": "BdfOpts", "fos_bdf_stats": "BdfStats",
+           "fos_bdf_adapt_opts": "AdaptOpts", "fos_bdf_adapt_stats": "AdaptStats"}
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """The ctypes mirrors of the option and statistics structs have the header's size and
+    field offsets (a field added on one side only would shift every later field), checked
+    against gcc's own layout of include/fosgpu.h."""
+    import shutil
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "fosgpu.h"', 'int main(void) {']
+    for cname, pyname in STRUCTS.items():
+        st = getattr(_lib, pyname)
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in st._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ['  return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", str(ROOT / "include"), str(src), "-o", str(exe)],
+                   check=True, capture_output=True)
+    got = {}
+    for line in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n"):
+        if line:
+            a, b, v = line.split()
+            got[a, b] = int(v)
+    for cname, pyname in STRUCTS.items():
+        st = getattr(_lib, pyname)
+        assert got[cname, "size"] == C.sizeof(st), cname
+        for fname, _ in st._fields_:
+            assert got[cname, fname] == getattr(st, fname).offset, (cname, fname)

@@ -343,3 +343,38 @@ def test_bdf_predictor_extrapolates():
     assert res[1, 8][1]["n_newton"] < res[0, 8][1]["n_newton"]
     a, b = res[0, 8][0].reshape(5, -1), res[1, 8][0].reshape(5, -1)
     assert max(np.abs(a[q] - b[q]).max() / np.abs(a[q]).max() for q in range(5)) < 1e-5
+
+
+def test_oracle_struct_layouts_match_header(tmp_path):
+    """The ctypes mirrors of the oracle's option and statistics structs have the header's
+    size and field offsets, checked against gcc's layout of oracle/fos_oracle.h."""
+    import shutil
+    import subprocess
+    from pathlib import Path
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    root = Path(__file__).resolve().parents[1]
+    structs = {"o_bdf_opts": O.BdfOpts, "o_bdf_stats": O.BdfStats, "o_adapt_opts": O.AdaptOpts,
+               "o_adapt_stats": O.AdaptStats}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "fos_oracle.h"',
+             'int main(void) {']
+    for cname, st in structs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in st._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ['  return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", str(root / "oracle"), str(src), "-o", str(exe)],
+                   check=True, capture_output=True)
+    got = {}
+    for line in subprocess.run([str(exe)], check=True, capture_output=True,
+                               text=True).stdout.split("\n"):
+        if line:
+            a, b, v = line.split()
+            got[a, b] = int(v)
+    for cname, st in structs.items():
+        assert got[cname, "size"] == C.sizeof(st), cname
+        for fname, _ in st._fields_:
+            assert got[cname, fname] == getattr(st, fname).offset, (cname, fname)
