@@ -5,7 +5,8 @@
 // (the workloads prescribe fixed-step BDF1/BDF2) and keeps every vector in HBM:
 //   BDF1: G(y) = y - dt f(y) - y_n                      gamma = dt
 //   BDF2: G(y) = y - 2/3 dt f(y) - (4/3 y_n - 1/3 y_{n-1})  gamma = 2/3 dt (first step BDF1)
-//   Newton: y_0 = y_n; stop when ||G(y_k)||_2 <= rtol ||y_n||_2 + atol sqrt(N), in FP64
+//   Newton: y_0 = y_n (or, with opts->predictor, the constant-step BDF extrapolation);
+//           stop when ||G(y_k)||_2 <= rtol ||y_0||_2 + atol sqrt(N), in FP64
 //   linear: right-preconditioned restarted GMRES(maxl) on J_G d = -G, Arnoldi by classical
 //           Gram--Schmidt in FP64 with a second pass when ||w_1|| < min(1/sqrt(2), lin_rtol)
 //           ||w_0|| (the DGKS test, threshold bounded by the Krylov tolerance),
@@ -419,9 +420,10 @@ struct Driver {
     if (have_sq) *have_sq = d_zsq != nullptr;
     return fos_ilu_apply(c, r, z, d_zsq);
   }
-  // Expected cost of one decade of residual reduction: iteration time / -log10(rate).  The
-  // network is not applied while its last solve's rate at its iteration time buys a decade
-  // no cheaper than the last ILU(0) solve did -- the history already predicts a loss.  A
+  // Expected cost of a fixed residual reduction: iteration time / -log(rate per iteration).
+  // The network is not applied while its last solve's rate at its iteration time buys that
+  // reduction no cheaper than the last ILU(0) solve did -- the history already predicts a
+  // loss.  A
   // slower ILU(0) solve (a harder state) reopens the gate; a network that was never tried,
   // or iterations not yet timed, leave it open.
   bool network_predicted_to_lose() const {
@@ -521,7 +523,8 @@ struct Driver {
   // this is flexible GMRES (Z_j = M_j(V_j) kept); in modes 2 and 4 it falls back to ILU(0)
   // when the residual estimate stagnates (> 0.9 of the previous one), falls behind the last
   // ILU(0)-preconditioned solve's rate, or the iteration count reaches that solve's: the
-  // cycle goes on with ILU(0) (a non-finite estimate restarts it from the current iterate).  With y_add (the Newton iterate, read by the Jv until the
+  // cycle goes on with ILU(0) (a non-finite estimate restarts it from the current iterate).
+  // With y_add (the Newton iterate, read by the Jv until the
   // end), a solve that converges in its first cycle adds d to y_add instead of storing d
   // (*added); otherwise d is left in wk.d.  v0_is_b: V_0 already holds b (the Newton
   // residual kernel wrote it there), used unnormalised in the first cycle.
